@@ -1,0 +1,147 @@
+// Device-side types and math shared by the TIS kernels (sm_103a).
+//
+// Precision policy (mixed mode): pair, bonded, stacking and hydrogen-bond
+// geometry in FP32 from EXACT integer coordinate differences (positions are
+// also kept as 32-bit fixed point over the periodic box, so a difference is an
+// exact int32 whose wrap-around is the minimum image); every force
+// contribution is converted to 64-bit fixed point (2^-32 kcal/mol/A) before it
+// is summed, so sums are order-independent and deterministic; integration,
+// thermostat and energy sums in FP64.  FP64 mode evaluates everything in FP64
+// from the FP64 positions with the reference's own image convention.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tis {
+
+constexpr int kBlock = 128;          // particles per block; replicas are padded to it
+constexpr int kNoise = 3000;         // shared Gaussians per step (E:2598)
+constexpr int kNE = 11;              // energies vector (tis_energy_index)
+constexpr double kSig0 = 1.5852;     // LJ length scale (E:749-821)
+constexpr double kFixScale = 4294967296.0;   // 2^32 fixed-point units per kcal/mol/A
+constexpr float kFixScaleF = 4294967296.0f;
+constexpr float kFixLimit = 1.0e9f;  // |contribution| clamp (int64 range / 2^32 with margin)
+
+enum ErrBits : int { kErrCapacity = 1, kErrNonFinite = 2, kErrRange = 4 };
+
+// Per-replica constants (uploaded once).
+struct RepParams {
+    double box[3], hbox[3], qinv[3], lcell[3];
+    float qstep[3];
+    int mc[3];
+    int c0, nc;                  // first cell, number of cells
+    int p0, n, npad, center;     // first particle, particles, padded, recentring bead (global)
+    int nrna;                    // particles [p0, p0+nrna) are RNA beads
+    int lr_interval;
+    double T, h, lB, rc2, r2sr, r2lr, skin;
+    float rc2f, r2srf, r2lrf, Tf;
+    double mass[10], k1[10], k2[10], sigma[10], vcap[10];
+    // pair tables, 1..45 (E:2908-2938); dm = D_LJ - 1.5852
+    float dlj2[46], dm[46], flj[46], elj[46], d2min[46], qclb[46];
+    double dlj2_d[46], dlj_d[46], flj_d[46], elj_d[46], d2min_d[46], qclb_d[46];
+    unsigned long long seed;
+    int bt0, bt1, s30, s31, s20, s21, hb0, hb1, hba0, hba1, ca0, ca1;
+    int kscr0, maxk;             // hb_K scratch offset and size
+};
+
+// Per-replica dynamic state.
+struct RepState {
+    long long klok, rebuilds;
+    unsigned long long ctr;      // rand() draws consumed
+    unsigned long long maxd2;    // bit pattern of max |x - x_old|^2 (non-negative double)
+    double progress;
+    int rebuild, lr_now, err, n_active;
+    double e2hb, e3hb, e2st, e3st;
+};
+
+// ---- Philox-4x32-10 (Salmon et al., SC'11) --------------------------------
+__host__ __device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        c[1] = (uint32_t)p1;
+        c[3] = (uint32_t)p0;
+        c[0] = n0;
+        c[2] = n2;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+// Draw k of the rand() stream of a replica: an integer in [1, 2^31-1].
+__host__ __device__ inline uint32_t rand_value(unsigned long long seed, unsigned long long k)
+{
+    unsigned long long blk = k >> 2;
+    uint32_t c[4] = {(uint32_t)blk, (uint32_t)(blk >> 32), 0u, 0u};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    uint32_t v = c[k & 3u] >> 1;
+    return v ? v : 1u;
+}
+
+#ifdef __CUDACC__
+// FP64 uniform exactly as the reference forms it: (double) rand () / RAND_MAX.
+__device__ inline double rand_uniform(unsigned long long seed, unsigned long long k)
+{
+    return (double)rand_value(seed, k) / 2147483647.0;
+}
+
+// sqrt(-2 ln u) for u = v / (2^31-1), accurate in FP32 over the whole range.
+__device__ inline float bm_radius(uint32_t v)
+{
+    const float inv = 1.0f / 2147483647.0f;
+    float lg;
+    if (v < 1073741824u) lg = logf((float)v * inv);
+    else lg = log1pf(-(float)(2147483647u - v) * inv);
+    return sqrtf(-2.0f * lg);
+}
+
+// ---- fixed point ----------------------------------------------------------
+__device__ inline long long to_fix(float v, int &err)
+{
+    if (!(fabsf(v) < kFixLimit)) {
+        if (v != v) { err |= kErrNonFinite; return 0; }
+        err |= kErrNonFinite;
+        v = v > 0 ? kFixLimit : -kFixLimit;
+    }
+    return __float2ll_rn(v * kFixScaleF);
+}
+
+__device__ inline void atomic_add_fix(unsigned long long *a, long long v)
+{
+    atomicAdd(a, (unsigned long long)v);
+}
+
+__device__ inline int jn12(int a, int b)  // E:1803-1805
+{
+    if (a < b) return (a - 1) * 9 - (a - 1) * a / 2 + b;
+    return (b - 1) * 9 - (b - 1) * b / 2 + a;
+}
+
+#endif  // __CUDACC__
+
+template <class R>
+struct V3 {
+    R x, y, z;
+};
+#ifdef __CUDACC__
+template <class R>
+__device__ inline V3<R> operator-(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class R>
+__device__ inline V3<R> operator+(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class R>
+__device__ inline V3<R> operator*(R s, V3<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class R>
+__device__ inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class R>
+__device__ inline V3<R> cross(V3<R> a, V3<R> b)
+{
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+#endif  // __CUDACC__
+
+}  // namespace tis

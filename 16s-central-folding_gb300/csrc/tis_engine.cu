@@ -1,0 +1,910 @@
+// Engine handle: packs replicas into device arrays and implements the C ABI
+// entry points of include/tis_gpu.h that drive the kernels.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tis_host.h"
+#include "tis_kernels.cuh"
+
+using tis::fail;
+
+#define TIS_CUDA(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(TIS_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                                \
+    } while (0)
+
+namespace {
+
+struct RepHost {
+    int n, nrna, npad, p0, c0, nc, mc[3];
+    int bt0, bt1, s30, s31, s20, s21, hb0, hb1, hba0, hba1;
+};
+
+template <class T>
+int dalloc(std::vector<void *> &owned, T **p, size_t count)
+{
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) return fail(TIS_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
+    owned.push_back((void *)*p);
+    e = cudaMemset(*p, 0, count * sizeof(T));
+    if (e != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaMemset: %s", cudaGetErrorString(e));
+    return TIS_OK;
+}
+
+template <class T>
+int dupload(std::vector<void *> &owned, T **p, const std::vector<T> &h)
+{
+    int rc = dalloc(owned, p, h.size());
+    if (rc) return rc;
+    if (!h.empty()) {
+        cudaError_t e = cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaMemcpy H2D: %s", cudaGetErrorString(e));
+    }
+    return TIS_OK;
+}
+
+const tis::Array *need(const tis_system *s, const char *name, int r, int dtype, int64_t count = -1)
+{
+    const tis::Array *a = s->get(name);
+    if (!a) {
+        fail(TIS_ERR_ARG, "replica %d: system array '%s' missing", r, name);
+        return nullptr;
+    }
+    if (a->dtype != dtype) {
+        fail(TIS_ERR_ARG, "replica %d: system array '%s' has dtype %d, expected %d", r, name, a->dtype, dtype);
+        return nullptr;
+    }
+    if (count >= 0 && a->count() != count) {
+        fail(TIS_ERR_ARG, "replica %d: system array '%s' has %lld entries, expected %lld", r, name,
+             (long long)a->count(), (long long)count);
+        return nullptr;
+    }
+    return a;
+}
+
+double scalar_f64(const tis_system *s, const char *name, double def)
+{
+    const tis::Array *a = s->get(name);
+    if (!a || a->count() < 1) return def;
+    if (a->dtype == TIS_F64) return a->as<double>()[0];
+    if (a->dtype == TIS_I64) return (double)a->as<int64_t>()[0];
+    return (double)a->as<int32_t>()[0];
+}
+
+int64_t scalar_i64(const tis_system *s, const char *name, int64_t def)
+{
+    const tis::Array *a = s->get(name);
+    if (!a || a->count() < 1) return def;
+    if (a->dtype == TIS_I64) return a->as<int64_t>()[0];
+    if (a->dtype == TIS_I32) return a->as<int32_t>()[0];
+    return (int64_t)a->as<double>()[0];
+}
+
+int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+}  // namespace
+
+struct tis_handle {
+    int R = 0, P = 0, C = 0, nblk = 0;
+    tis_run_params prm{};
+    cudaStream_t stream = nullptr;
+    std::vector<void *> owned;
+    std::vector<RepHost> rep;
+    tis::Dev dev{};
+    bool lists_built = false;
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    long long launches = 0;
+    double *d_scalar = nullptr;
+
+    ~tis_handle()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void *p : owned) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int check_flags(tis_handle *h)
+{
+    std::vector<tis::RepState> rs(h->R);
+    TIS_CUDA(cudaMemcpyAsync(rs.data(), h->dev.rs, sizeof(tis::RepState) * h->R, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    for (int r = 0; r < h->R; ++r) {
+        const int e = rs[r].err;
+        if (e & tis::kErrCapacity) return fail(TIS_ERR_CAPACITY, "replica %d: neighbour list capacity exceeded", r);
+        if (e & tis::kErrRange) return fail(TIS_ERR_RANGE, "replica %d: a particle left the cell grid's range", r);
+        if (e & tis::kErrNonFinite) return fail(TIS_ERR_NONFINITE, "replica %d: non-finite or runaway force/state", r);
+    }
+    return TIS_OK;
+}
+
+int clear_flags(tis_handle *h)
+{
+    // err is the 4th int after 4 eight-byte counters and a double; clear via a host round trip
+    std::vector<tis::RepState> rs(h->R);
+    TIS_CUDA(cudaMemcpyAsync(rs.data(), h->dev.rs, sizeof(tis::RepState) * h->R, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    for (auto &s : rs) s.err = 0;
+    TIS_CUDA(cudaMemcpyAsync(h->dev.rs, rs.data(), sizeof(tis::RepState) * h->R, cudaMemcpyHostToDevice, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return TIS_OK;
+}
+
+int grow_lists(tis_handle *h, int cap_sr, int cap_lr)
+{
+    // lists are the last allocations that depend on capacity; allocate anew
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    auto drop = [&](void *p) {
+        auto it = std::find(h->owned.begin(), h->owned.end(), p);
+        if (it != h->owned.end()) {
+            cudaFree(p);
+            h->owned.erase(it);
+        }
+    };
+    drop(h->dev.nbr_sr);
+    drop(h->dev.nbr_lr);
+    int rc;
+    if ((rc = dalloc(h->owned, &h->dev.nbr_sr, (size_t)cap_sr * h->P))) return rc;
+    if ((rc = dalloc(h->owned, &h->dev.nbr_lr, (size_t)cap_lr * h->P))) return rc;
+    h->dev.cap_sr = cap_sr;
+    h->dev.cap_lr = cap_lr;
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    return TIS_OK;
+}
+
+int populate(tis_handle *h)
+{
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        int rc = clear_flags(h);
+        if (rc) return rc;
+        tis::launch_force_all_rebuild(h->dev, h->stream);
+        tis::launch_rebuild(h->dev, h->stream);
+        TIS_CUDA(cudaGetLastError());
+        rc = check_flags(h);
+        if (rc != TIS_ERR_CAPACITY) {
+            if (rc == TIS_OK) h->lists_built = true;
+            return rc;
+        }
+        rc = grow_lists(h, round_up(h->dev.cap_sr * 3 / 2, 32), round_up(h->dev.cap_lr * 3 / 2, 32));
+        if (rc) return rc;
+    }
+    return fail(TIS_ERR_CAPACITY, "neighbour lists keep overflowing");
+}
+
+void enqueue_step(tis_handle *h)
+{
+    tis::launch_pair_sr(h->dev, h->stream, false);
+    tis::launch_pair_lr(h->dev, h->stream, false, false);
+    tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true);
+    tis::launch_integrate(h->dev, h->stream);
+    tis::launch_control(h->dev, h->stream);
+    tis::launch_rebuild(h->dev, h->stream);
+}
+
+int valid_replica(tis_handle *h, int r)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    if (r < 0 || r >= h->R) return fail(TIS_ERR_ARG, "replica %d out of range (0..%d)", r, h->R - 1);
+    return TIS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tis_run_params_default(tis_run_params *p)
+{
+    if (!p) return fail(TIS_ERR_ARG, "null params");
+    memset(p, 0, sizeof *p);
+    p->precision = TIS_PREC_MIXED;
+    p->noise = TIS_NOISE_REFERENCE;
+    p->sr = 12.0;
+    p->skin = 3.0;
+    p->lr_interval = 10;
+    p->use_graph = 1;
+    p->graph_steps = 20;
+    return TIS_OK;
+}
+
+int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_params *prm_in, tis_handle **out)
+{
+    tis::clear_error();
+    if (!systems || n_replicas < 1 || !out) return fail(TIS_ERR_ARG, "tis_create: bad argument");
+    tis_run_params prm;
+    if (prm_in) prm = *prm_in;
+    else tis_run_params_default(&prm);
+    if (prm.lr_interval < 1) prm.lr_interval = 10;
+    if (prm.graph_steps < 1) prm.graph_steps = 20;
+    if (prm.sr <= 0) prm.sr = 12.0;
+    if (prm.skin <= 0) prm.skin = 3.0;
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(TIS_ERR_CUDA, "no CUDA device available");
+    if (prm.device < 0 || prm.device >= ndev) return fail(TIS_ERR_ARG, "device %d out of range", prm.device);
+    TIS_CUDA(cudaSetDevice(prm.device));
+
+    tis_handle *h = new tis_handle();
+    h->prm = prm;
+    h->R = n_replicas;
+    auto bail = [&](int rc) {
+        delete h;
+        return rc;
+    };
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(TIS_ERR_CUDA, "cudaStreamCreate failed"));
+
+    std::vector<tis::RepParams> rp(n_replicas);
+    std::vector<int> code, blk_rep, rep_of, cell_rep;
+    std::vector<double> st[9];
+    std::vector<int4> bt_idx;
+    std::vector<double2> bt_par;
+    std::vector<int> st3_idx, st3_off, st2_idx, hb_idx, hb_dode, hb_aoff{0}, hb_aidx, hba_val, hba_coff{0}, hba_cidx,
+        hba_n, ca_list;
+    std::vector<double> st3_nat, st3_E, st2_r0, st2_E, hb_nat, hb_E;
+    int p0 = 0, c0 = 0, kscr = 0;
+    double max_rho = 0, max_rho_ch = 0;
+    const char *snames[9] = {"x", "y", "z", "ox", "oy", "oz", "vx", "vy", "vz"};
+
+    for (int r = 0; r < n_replicas; ++r) {
+        const tis_system *s = systems[r];
+        if (!s) return bail(fail(TIS_ERR_ARG, "replica %d: null system", r));
+        const int n = (int)scalar_i64(s, "n_particles", -1);
+        const int nrna = (int)scalar_i64(s, "n_rna", -1);
+        if (n <= 0 || nrna <= 0 || nrna > n) return bail(fail(TIS_ERR_ARG, "replica %d: bad n_particles/n_rna", r));
+        const tis::Array *box = need(s, "box", r, TIS_F64, 3);
+        const tis::Array *type = need(s, "type", r, TIS_I32, n), *kind = need(s, "kind", r, TIS_I32, n);
+        const tis::Array *mass = need(s, "mass", r, TIS_F64, 9), *rlj = need(s, "rlj", r, TIS_F64, 9);
+        const tis::Array *elj = need(s, "elj", r, TIS_F64, 9), *qc = need(s, "qc", r, TIS_F64, 9);
+        if (!box || !type || !kind || !mass || !rlj || !elj || !qc) return bail(TIS_ERR_ARG);
+        const tis::Array *sv[9];
+        for (int k = 0; k < 9; ++k)
+            if (!(sv[k] = need(s, snames[k], r, TIS_F64, n))) return bail(TIS_ERR_ARG);
+        const int center = (int)scalar_i64(s, "center", 499);
+        if (center < 0 || center >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: centre bead %d outside the RNA", r, center));
+
+        RepHost hr{};
+        hr.n = n;
+        hr.nrna = nrna;
+        hr.npad = round_up(n, tis::kBlock);
+        hr.p0 = p0;
+        tis::RepParams &R = rp[r];
+        memset(&R, 0, sizeof R);
+        const double T = scalar_f64(s, "T", 0.615), hstep = scalar_f64(s, "h", 0.05);
+        const double lB = scalar_f64(s, "lB", 332.0637090 * (0.03273600947 * T - 0.00669625750));
+        const double rc = scalar_f64(s, "rc", 50.0);
+        if (rc < prm.sr) return bail(fail(TIS_ERR_ARG, "replica %d: Coulomb cutoff %g below the SR radius %g", r, rc, prm.sr));
+        for (int k = 0; k < 3; ++k) {
+            const double L = box->as<double>()[k];
+            R.box[k] = L;
+            R.hbox[k] = 0.5 * L;
+            R.qinv[k] = 4294967296.0 / L;
+            R.qstep[k] = (float)(L / 4294967296.0);
+            R.mc[k] = (int)(L / (rc + prm.skin));  // E:1484-1490
+            if (R.mc[k] < 1) return bail(fail(TIS_ERR_ARG, "replica %d: box smaller than the LR list radius", r));
+            R.lcell[k] = L / R.mc[k];
+            hr.mc[k] = R.mc[k];
+        }
+        hr.c0 = c0;
+        hr.nc = R.mc[0] * R.mc[1] * R.mc[2];
+        R.c0 = c0;
+        R.nc = hr.nc;
+        R.p0 = p0;
+        R.n = n;
+        R.npad = hr.npad;
+        R.center = p0 + center;
+        R.nrna = nrna;
+        R.lr_interval = prm.lr_interval;
+        R.T = T;
+        R.h = hstep;
+        R.lB = lB;
+        R.rc2 = rc * rc;
+        R.r2sr = (prm.sr + prm.skin) * (prm.sr + prm.skin);
+        R.r2lr = (rc + prm.skin) * (rc + prm.skin);
+        R.skin = prm.skin;
+        R.rc2f = (float)R.rc2;
+        R.r2srf = (float)R.r2sr;
+        R.r2lrf = (float)R.r2lr;
+        R.Tf = (float)T;
+        // read_maxi_key (E:2883-2945)
+        for (int t = 1; t <= 9; ++t) {
+            const double m = mass->as<double>()[t - 1], Rl = rlj->as<double>()[t - 1];
+            const double visc = 0.555 * Rl;
+            R.mass[t] = m;
+            R.k1[t] = exp(-visc / m * hstep);
+            R.k2[t] = (1.0 - R.k1[t]) / visc;
+            R.sigma[t] = sqrt(2.0 * visc * T / hstep);
+            R.vcap[t] = m / (300.0 * T);
+        }
+        for (int a = 1; a <= 9; ++a)
+            for (int b = a; b <= 9; ++b) {
+                const int J = (a - 1) * 9 - (a - 1) * a / 2 + b;
+                const double Dl = (a <= 6 && b <= 6) ? 3.2 : rlj->as<double>()[a - 1] + rlj->as<double>()[b - 1];
+                const double El = sqrt(elj->as<double>()[a - 1] * elj->as<double>()[b - 1]);
+                const double Fl = 12.0 * El / (tis::kSig0 * tis::kSig0);
+                const double Q = qc->as<double>()[a - 1] * qc->as<double>()[b - 1];
+                const double dmin = (Dl - 0.4406141861 * tis::kSig0) * (Dl - 0.4406141861 * tis::kSig0);
+                R.dlj2_d[J] = Dl * Dl;
+                R.dlj_d[J] = Dl;
+                R.flj_d[J] = Fl;
+                R.elj_d[J] = El;
+                R.d2min_d[J] = dmin;
+                R.qclb_d[J] = Q * lB;
+                R.dlj2[J] = (float)(Dl * Dl);
+                R.dm[J] = (float)(Dl - tis::kSig0);
+                R.flj[J] = (float)Fl;
+                R.elj[J] = (float)El;
+                R.d2min[J] = (float)dmin;
+                R.qclb[J] = (float)(Q * lB);
+            }
+        R.seed = (unsigned long long)scalar_i64(s, "seed", r + 1);
+
+        // particles
+        for (int i = 0; i < hr.npad; ++i) {
+            if (i < n) {
+                const int t = type->as<int32_t>()[i], k = kind->as<int32_t>()[i];
+                if (t < 1 || t > 9 || k < 0 || k > 5) return bail(fail(TIS_ERR_ARG, "replica %d: bad type/kind of particle %d", r, i));
+                if ((i < nrna) != (k <= 2)) return bail(fail(TIS_ERR_ARG, "replica %d: RNA beads must precede the ions", r));
+                code.push_back(t | (k << 8) | (1 << 16));
+                for (int c = 0; c < 9; ++c) st[c].push_back(sv[c]->as<double>()[i]);
+            } else {
+                code.push_back(1);
+                for (int c = 0; c < 9; ++c) st[c].push_back(0.0);
+            }
+            rep_of.push_back(r);
+        }
+        for (int b = 0; b < hr.npad / tis::kBlock; ++b) blk_rep.push_back(r);
+        for (int c = 0; c < hr.nc; ++c) cell_rep.push_back(r);
+        double vol = R.box[0] * R.box[1] * R.box[2];
+        int nch = 0;
+        for (int i = 0; i < n; ++i) nch += (kind->as<int32_t>()[i] != 1 && kind->as<int32_t>()[i] != 2);
+        max_rho = std::max(max_rho, n / vol);
+        max_rho_ch = std::max(max_rho_ch, nch / vol);
+
+        // bonded terms (polymer_constraints order)
+        const tis::Array *btk = need(s, "bt_kind", r, TIS_I32);
+        if (!btk) return bail(TIS_ERR_ARG);
+        const int64_t nbt = btk->count();
+        const tis::Array *bta = need(s, "bt_a", r, TIS_I32, nbt), *btb = need(s, "bt_b", r, TIS_I32, nbt);
+        const tis::Array *btc = need(s, "bt_c", r, TIS_I32, nbt), *btk0 = need(s, "bt_k0", r, TIS_F64, nbt);
+        const tis::Array *btx0 = need(s, "bt_x0", r, TIS_F64, nbt);
+        if (!bta || !btb || !btc || !btk0 || !btx0) return bail(TIS_ERR_ARG);
+        hr.bt0 = (int)bt_idx.size();
+        for (int64_t t = 0; t < nbt; ++t) {
+            const int kd = btk->as<int32_t>()[t];
+            const int a = bta->as<int32_t>()[t], b = btb->as<int32_t>()[t], c = btc->as<int32_t>()[t];
+            if (a < 0 || a >= nrna || b < 0 || b >= nrna || (kd == 1 && (c < 0 || c >= nrna)))
+                return bail(fail(TIS_ERR_ARG, "replica %d: bonded term %lld has a bad index", r, (long long)t));
+            bt_idx.push_back(make_int4(p0 + a, p0 + b, kd == 1 ? p0 + c : p0 + b, kd));
+            bt_par.push_back(make_double2(btk0->as<double>()[t], btx0->as<double>()[t]));
+        }
+        hr.bt1 = (int)bt_idx.size();
+
+        // stacks
+        const tis::Array *s3E = need(s, "st3_E", r, TIS_F64), *s2E = need(s, "st2_E", r, TIS_F64);
+        if (!s3E || !s2E) return bail(TIS_ERR_ARG);
+        const int64_t n3 = s3E->count(), n2 = s2E->count();
+        const tis::Array *s3i = need(s, "st3_idx", r, TIS_I32, 6 * n3), *s3n = need(s, "st3_native", r, TIS_F64, 6 * n3);
+        const tis::Array *s2i = need(s, "st2_idx", r, TIS_I32, 7 * n2), *s2r = need(s, "st2_r0", r, TIS_F64, n2);
+        if (!s3i || !s3n || !s2i || !s2r) return bail(TIS_ERR_ARG);
+        std::vector<int> off3(2 * n3, -1);
+        if (const tis::Array *o = s->get("st3_off")) {
+            if (o->dtype != TIS_I32 || o->count() != 2 * n3) return bail(fail(TIS_ERR_ARG, "replica %d: bad st3_off", r));
+            for (int64_t t = 0; t < 2 * n3; ++t) off3[t] = o->as<int32_t>()[t];
+        } else {  // E:1960-1981: a site with ST_EXCESS == 1 switches off stack s3_N + ceil(site/2) - 1
+            const tis::Array *site = need(s, "st3_site", r, TIS_I32, 2 * n3);
+            const tis::Array *exc = need(s, "st_excess", r, TIS_I32);
+            if (!site || !exc) return bail(TIS_ERR_ARG);
+            for (int64_t t = 0; t < 2 * n3; ++t) {
+                const int e = site->as<int32_t>()[t];
+                if (e >= 1 && e <= exc->count() && exc->as<int32_t>()[e - 1] == 1) {
+                    const int idx = (int)ceil(0.5 * e) - 2;
+                    if (idx >= 0 && idx < n2) off3[t] = idx;
+                }
+            }
+        }
+        hr.s30 = (int)st3_E.size();
+        for (int64_t k = 0; k < n3; ++k) {
+            for (int c = 0; c < 6; ++c) {
+                const int v = s3i->as<int32_t>()[6 * k + c];
+                if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: tertiary stack %lld bad index", r, (long long)k));
+                st3_idx.push_back(p0 + v);
+                st3_nat.push_back(s3n->as<double>()[6 * k + c]);
+            }
+            st3_E.push_back(s3E->as<double>()[k]);
+            st3_off.push_back(off3[2 * k]);
+            st3_off.push_back(off3[2 * k + 1]);
+        }
+        hr.s31 = (int)st3_E.size();
+        hr.s20 = (int)st2_E.size();
+        for (int64_t k = 0; k < n2; ++k) {
+            for (int c = 0; c < 7; ++c) {
+                const int v = s2i->as<int32_t>()[7 * k + c];
+                if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: secondary stack %lld bad index", r, (long long)k));
+                st2_idx.push_back(p0 + v);
+            }
+            st2_r0.push_back(s2r->as<double>()[k]);
+            st2_E.push_back(s2E->as<double>()[k]);
+        }
+        hr.s21 = (int)st2_E.size();
+
+        // hydrogen bonds
+        const tis::Array *hE = need(s, "hb_E", r, TIS_F64);
+        const tis::Array *hv = need(s, "hba_valence", r, TIS_I32);
+        if (!hE || !hv) return bail(TIS_ERR_ARG);
+        const int64_t nh = hE->count(), na = hv->count();
+        const tis::Array *hi = need(s, "hb_idx", r, TIS_I32, 6 * nh), *hn = need(s, "hb_native", r, TIS_F64, 6 * nh);
+        const tis::Array *hd = need(s, "hb_dode", r, TIS_I32, nh), *hao = need(s, "hb_atom_off", r, TIS_I32, nh + 1);
+        const tis::Array *hco = need(s, "hba_cand_off", r, TIS_I32, na + 1);
+        if (!hi || !hn || !hd || !hao || !hco) return bail(TIS_ERR_ARG);
+        const tis::Array *hai = need(s, "hb_atom_idx", r, TIS_I32, hao->as<int32_t>()[nh]);
+        const tis::Array *hci = need(s, "hba_cand_idx", r, TIS_I32, hco->as<int32_t>()[na]);
+        if (!hai || !hci) return bail(TIS_ERR_ARG);
+        hr.hb0 = (int)hb_E.size();
+        hr.hba0 = (int)hba_val.size();
+        for (int64_t k = 0; k < nh; ++k) {
+            for (int c = 0; c < 6; ++c) {
+                const int v = hi->as<int32_t>()[6 * k + c];
+                if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond candidate %lld bad index", r, (long long)k));
+                hb_idx.push_back(p0 + v);
+                hb_nat.push_back(hn->as<double>()[6 * k + c]);
+            }
+            hb_E.push_back(hE->as<double>()[k]);
+            hb_dode.push_back(hd->as<int32_t>()[k]);
+            for (int u = hao->as<int32_t>()[k]; u < hao->as<int32_t>()[k + 1]; ++u) {
+                const int a = hai->as<int32_t>()[u];
+                if (a < 0 || a >= na) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond atom index out of range", r));
+                hb_aidx.push_back(hr.hba0 + a);
+            }
+            hb_aoff.push_back((int)hb_aidx.size());
+        }
+        hr.hb1 = (int)hb_E.size();
+        int maxk = 1;
+        R.ca0 = (int)ca_list.size();
+        for (int64_t a = 0; a < na; ++a) {
+            const int v = hv->as<int32_t>()[a];
+            hba_val.push_back(v);
+            const int cnt = hco->as<int32_t>()[a + 1] - hco->as<int32_t>()[a];
+            hba_n.push_back(cnt);
+            maxk = std::max(maxk, cnt);
+            for (int u = hco->as<int32_t>()[a]; u < hco->as<int32_t>()[a + 1]; ++u) {
+                const int k = hci->as<int32_t>()[u];
+                if (k < 0 || k >= nh) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond candidate index out of range", r));
+                hba_cidx.push_back(hr.hb0 + k);
+            }
+            hba_coff.push_back((int)hba_cidx.size());
+            if (cnt > v) ca_list.push_back(hr.hba0 + (int)a);  // only these can exceed their valence
+        }
+        R.ca1 = (int)ca_list.size();
+        hr.hba1 = (int)hba_val.size();
+        R.bt0 = hr.bt0; R.bt1 = hr.bt1; R.s30 = hr.s30; R.s31 = hr.s31; R.s20 = hr.s20; R.s21 = hr.s21;
+        R.hb0 = hr.hb0; R.hb1 = hr.hb1; R.hba0 = hr.hba0; R.hba1 = hr.hba1;
+        R.kscr0 = kscr;
+        R.maxk = maxk;
+        kscr += maxk;
+        h->rep.push_back(hr);
+        p0 += hr.npad;
+        c0 += hr.nc;
+    }
+    h->P = p0;
+    h->C = c0;
+    h->nblk = p0 / tis::kBlock;
+
+    // neighbour capacities: ten times the homogeneous expectation, at least 128 / 96
+    const double pi = 3.14159265358979323846;
+    double rmax_lr = 0;
+    for (auto &R : rp) rmax_lr = std::max(rmax_lr, sqrt(R.r2lr));
+    const double rsr = prm.sr + prm.skin;
+    int cap_sr = prm.cap_sr > 0 ? prm.cap_sr : std::max(128, round_up((int)(10 * max_rho * 4.0 / 3.0 * pi * rsr * rsr * rsr), 32));
+    int cap_lr = prm.cap_lr > 0 ? prm.cap_lr
+                                : std::max(96, round_up((int)(10 * max_rho_ch * 4.0 / 3.0 * pi * rmax_lr * rmax_lr * rmax_lr), 32));
+
+    tis::Dev &d = h->dev;
+    d.R = h->R;
+    d.P = h->P;
+    d.nblk = h->nblk;
+    d.C = h->C;
+    d.fp64 = prm.precision == TIS_PREC_FP64;
+    d.noise = prm.noise;
+    d.cap_sr = cap_sr;
+    d.cap_lr = cap_lr;
+    auto &O = h->owned;
+    int rc = TIS_OK;
+    std::vector<int4> q(h->P);
+    for (int i = 0; i < h->P; ++i) q[i] = make_int4(0, 0, 0, code[i]);
+    std::vector<tis::RepState> rs(h->R);
+    memset(rs.data(), 0, sizeof(tis::RepState) * h->R);
+    for (auto &s : rs) s.lr_now = 1;
+    tis::RepParams *d_rp = nullptr;
+    tis::RepState *d_rs = nullptr;
+    int *d_blk = nullptr, *d_rep = nullptr, *d_cellrep = nullptr;
+    int4 *d_q = nullptr;
+    if ((rc = dupload(O, &d_rp, rp)) || (rc = dupload(O, &d_rs, rs)) || (rc = dupload(O, &d_blk, blk_rep)) ||
+        (rc = dupload(O, &d_rep, rep_of)) || (rc = dupload(O, &d_cellrep, cell_rep)) || (rc = dupload(O, &d_q, q)))
+        return bail(rc);
+    d.rp = d_rp; d.rs = d_rs; d.blk_rep = d_blk; d.rep_of = d_rep; d.cell_rep = d_cellrep; d.q = d_q;
+    double **sd[9] = {&d.x, &d.y, &d.z, &d.xo, &d.yo, &d.zo, &d.vx, &d.vy, &d.vz};
+    for (int c = 0; c < 9; ++c)
+        if ((rc = dupload(O, sd[c], st[c]))) return bail(rc);
+    if ((rc = dalloc(O, &d.f, 3 * (size_t)h->P)) || (rc = dalloc(O, &d.flr, 3 * (size_t)h->P)) ||
+        (rc = dalloc(O, &d.gnoise, (size_t)h->R * tis::kNoise)) || (rc = dalloc(O, &d.cell_of, h->P)) ||
+        (rc = dalloc(O, &d.cell_count, h->C)) || (rc = dalloc(O, &d.cell_start, h->C)) ||
+        (rc = dalloc(O, &d.cell_fill, h->C)) || (rc = dalloc(O, &d.cell_list, h->P)) ||
+        (rc = dalloc(O, &d.n_sr, h->P)) || (rc = dalloc(O, &d.n_lr, h->P)) ||
+        (rc = dalloc(O, &d.nbr_sr, (size_t)cap_sr * h->P)) || (rc = dalloc(O, &d.nbr_lr, (size_t)cap_lr * h->P)) ||
+        (rc = dalloc(O, &d.eterm, (size_t)h->R * tis::kNE)) || (rc = dalloc(O, &d.shift, (size_t)h->R * 3)) ||
+        (rc = dalloc(O, &h->d_scalar, 4)))
+        return bail(rc);
+    int4 *d_bti = nullptr;
+    double2 *d_btp = nullptr;
+    int *i3 = nullptr, *o3 = nullptr, *i2 = nullptr, *ih = nullptr, *dh = nullptr, *ao = nullptr, *ai = nullptr;
+    int *hv = nullptr, *co = nullptr, *ci = nullptr, *hn = nullptr, *ca = nullptr;
+    double *n3 = nullptr, *e3 = nullptr, *r2 = nullptr, *e2 = nullptr, *nh = nullptr, *eh = nullptr;
+    if ((rc = dupload(O, &d_bti, bt_idx)) || (rc = dupload(O, &d_btp, bt_par)) || (rc = dupload(O, &i3, st3_idx)) ||
+        (rc = dupload(O, &n3, st3_nat)) || (rc = dupload(O, &e3, st3_E)) || (rc = dupload(O, &o3, st3_off)) ||
+        (rc = dupload(O, &i2, st2_idx)) || (rc = dupload(O, &r2, st2_r0)) || (rc = dupload(O, &e2, st2_E)) ||
+        (rc = dupload(O, &ih, hb_idx)) || (rc = dupload(O, &nh, hb_nat)) || (rc = dupload(O, &eh, hb_E)) ||
+        (rc = dupload(O, &dh, hb_dode)) || (rc = dupload(O, &ao, hb_aoff)) || (rc = dupload(O, &ai, hb_aidx)) ||
+        (rc = dupload(O, &hv, hba_val)) || (rc = dupload(O, &co, hba_coff)) || (rc = dupload(O, &ci, hba_cidx)) ||
+        (rc = dupload(O, &hn, hba_n)) || (rc = dupload(O, &ca, ca_list)))
+        return bail(rc);
+    d.bt_idx = d_bti; d.bt_par = d_btp;
+    d.st3_idx = i3; d.st3_nat = n3; d.st3_E = e3; d.st3_off = o3;
+    d.st2_idx = i2; d.st2_r0 = r2; d.st2_E = e2;
+    d.hb_idx = ih; d.hb_nat = nh; d.hb_E = eh; d.hb_dode = dh; d.hb_aoff = ao; d.hb_aidx = ai;
+    d.hba_val = hv; d.hba_coff = co; d.hba_cidx = ci; d.hba_n = hn; d.ca_list = ca;
+    const size_t nst2 = st2_E.size(), nst3 = st3_E.size(), nhb = hb_E.size(), nhba = hba_val.size();
+    if ((rc = dalloc(O, &d.st2_off_flag, nst2)) || (rc = dalloc(O, &d.st_energy, nst3)) ||
+        (rc = dalloc(O, &d.hb_status, nhb)) || (rc = dalloc(O, &d.hb_excess, nhba)) ||
+        (rc = dalloc(O, &d.excess, nhba)) || (rc = dalloc(O, &d.hb_active, nhb)) ||
+        (rc = dalloc(O, &d.hb_K, (size_t)kscr)) || (rc = dalloc(O, &d.hb_A, ca_list.size())) ||
+        (rc = dalloc(O, &d.hb_energy, nhb)) || (rc = dalloc(O, &d.hb_code, nhb)))
+        return bail(rc);
+    tis::launch_quantize(h->dev, h->stream);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess)
+        return bail(fail(TIS_ERR_CUDA, "quantisation kernel failed"));
+    *out = h;
+    return TIS_OK;
+}
+
+int tis_destroy(tis_handle *h)
+{
+    if (h) {
+        cudaSetDevice(h->prm.device);
+        cudaStreamSynchronize(h->stream);
+        delete h;
+    }
+    return TIS_OK;
+}
+
+int tis_set_state(tis_handle *h, int r, const double *x, const double *y, const double *z, const double *xo,
+                  const double *yo, const double *zo, const double *vx, const double *vy, const double *vz)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    const double *src[9] = {x, y, z, xo, yo, zo, vx, vy, vz};
+    double *dst[9] = {h->dev.x, h->dev.y, h->dev.z, h->dev.xo, h->dev.yo, h->dev.zo, h->dev.vx, h->dev.vy, h->dev.vz};
+    const RepHost &hr = h->rep[r];
+    for (int c = 0; c < 9; ++c) {
+        if (!src[c]) return fail(TIS_ERR_ARG, "tis_set_state: null array %d", c);
+        TIS_CUDA(cudaMemcpyAsync(dst[c] + hr.p0, src[c], sizeof(double) * hr.n, cudaMemcpyHostToDevice, h->stream));
+    }
+    tis::launch_quantize(h->dev, h->stream);
+    TIS_CUDA(cudaGetLastError());
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    h->lists_built = false;
+    return TIS_OK;
+}
+
+int tis_get_state(tis_handle *h, int r, double *x, double *y, double *z, double *xo, double *yo, double *zo,
+                  double *vx, double *vy, double *vz)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    double *dst[9] = {x, y, z, xo, yo, zo, vx, vy, vz};
+    double *src[9] = {h->dev.x, h->dev.y, h->dev.z, h->dev.xo, h->dev.yo, h->dev.zo, h->dev.vx, h->dev.vy, h->dev.vz};
+    const RepHost &hr = h->rep[r];
+    for (int c = 0; c < 9; ++c)
+        if (dst[c]) TIS_CUDA(cudaMemcpyAsync(dst[c], src[c] + hr.p0, sizeof(double) * hr.n, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return TIS_OK;
+}
+
+int tis_populate_lists(tis_handle *h)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    return populate(h);
+}
+
+int tis_get_cells(tis_handle *h, int r, int32_t *cell, int32_t *dims)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    const RepHost &hr = h->rep[r];
+    if (cell) TIS_CUDA(cudaMemcpyAsync(cell, h->dev.cell_of + hr.p0, sizeof(int) * hr.n, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    if (dims) for (int k = 0; k < 3; ++k) dims[k] = hr.mc[k];
+    return TIS_OK;
+}
+
+int tis_get_pairs(tis_handle *h, int r, int which, int32_t *pairs, int64_t cap, int64_t *n)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    const RepHost &hr = h->rep[r];
+    const int capl = which ? h->dev.cap_lr : h->dev.cap_sr;
+    const int *nbr = which ? h->dev.nbr_lr : h->dev.nbr_sr;
+    const int *cnt = which ? h->dev.n_lr : h->dev.n_sr;
+    std::vector<int> c(hr.npad), lst((size_t)capl * hr.npad);
+    TIS_CUDA(cudaMemcpyAsync(c.data(), cnt + hr.p0, sizeof(int) * hr.npad, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaMemcpy2DAsync(lst.data(), sizeof(int) * hr.npad, nbr + hr.p0, sizeof(int) * h->P, sizeof(int) * hr.npad,
+                               capl, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    std::vector<std::pair<int, int>> pr;
+    for (int i = 0; i < hr.n; ++i)
+        for (int k = 0; k < c[i]; ++k) {
+            const int j = lst[(size_t)k * hr.npad + i] - hr.p0;
+            if (i < j) pr.emplace_back(i, j);
+        }
+    std::sort(pr.begin(), pr.end());
+    if (n) *n = 2 * (int64_t)pr.size();
+    if (pairs)
+        for (int64_t t = 0; t < (int64_t)pr.size() && 2 * t + 1 < cap; ++t) {
+            pairs[2 * t] = pr[t].first;
+            pairs[2 * t + 1] = pr[t].second;
+        }
+    return TIS_OK;
+}
+
+int tis_get_hb_status(tis_handle *h, int r, int32_t *status, int32_t *excess)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    const RepHost &hr = h->rep[r];
+    if (status && hr.hb1 > hr.hb0)
+        TIS_CUDA(cudaMemcpyAsync(status, h->dev.hb_status + hr.hb0, sizeof(int) * (hr.hb1 - hr.hb0), cudaMemcpyDeviceToHost, h->stream));
+    if (excess && hr.hba1 > hr.hba0)
+        TIS_CUDA(cudaMemcpyAsync(excess, h->dev.hb_excess + hr.hba0, sizeof(int) * (hr.hba1 - hr.hba0), cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return TIS_OK;
+}
+
+int tis_compute_forces(tis_handle *h, int r, int mask, double *forces, double *energies)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    if (!h->lists_built && (rc = populate(h))) return rc;
+    if ((rc = clear_flags(h))) return rc;
+    const tis::Dev &d = h->dev;
+    TIS_CUDA(cudaMemsetAsync(d.eterm, 0, sizeof(double) * h->R * tis::kNE, h->stream));
+    if (mask & TIS_TERM_SR) tis::launch_pair_sr(d, h->stream, true);
+    else TIS_CUDA(cudaMemsetAsync(d.f, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
+    if (mask & TIS_TERM_LR) tis::launch_pair_lr(d, h->stream, true, true);
+    else TIS_CUDA(cudaMemsetAsync(d.flr, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
+    const int tmask = (mask & TIS_TERM_BONDED ? 4 : 0) | (mask & TIS_TERM_STACK ? 8 : 0) | (mask & TIS_TERM_HB ? 16 : 0);
+    if (tmask) tis::launch_topology(d, h->stream, tmask, true, false);
+    tis::launch_rg(d, h->stream, r, h->d_scalar);
+    TIS_CUDA(cudaGetLastError());
+    const RepHost &hr = h->rep[r];
+    std::vector<unsigned long long> f(3 * (size_t)hr.n), fl(3 * (size_t)hr.n);
+    for (int c = 0; c < 3; ++c) {
+        TIS_CUDA(cudaMemcpyAsync(f.data() + c * hr.n, d.f + (size_t)c * h->P + hr.p0, 8 * hr.n, cudaMemcpyDeviceToHost, h->stream));
+        TIS_CUDA(cudaMemcpyAsync(fl.data() + c * hr.n, d.flr + (size_t)c * h->P + hr.p0, 8 * hr.n, cudaMemcpyDeviceToHost, h->stream));
+    }
+    double et[tis::kNE], rg = 0;
+    tis::RepState st;
+    TIS_CUDA(cudaMemcpyAsync(et, d.eterm + r * tis::kNE, sizeof et, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaMemcpyAsync(&rg, h->d_scalar, sizeof rg, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaMemcpyAsync(&st, d.rs + r, sizeof st, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    if (forces)
+        for (int i = 0; i < hr.n; ++i)
+            for (int c = 0; c < 3; ++c) {
+                const size_t k = (size_t)c * hr.n + i;
+                double v;
+                if (d.fp64) {
+                    double a, b;
+                    memcpy(&a, &f[k], 8);
+                    memcpy(&b, &fl[k], 8);
+                    v = a + b;
+                } else {
+                    v = (double)(long long)(f[k] + fl[k]) / tis::kFixScale;
+                }
+                forces[3 * i + c] = v;
+            }
+    if (energies) {
+        for (int k = 0; k < tis::kNE; ++k) energies[k] = et[k];
+        energies[TIS_E_RG] = rg;
+    }
+    return check_flags(h);
+}
+
+int tis_deterministic_forces(tis_handle *h)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    int rc;
+    if (!h->lists_built && (rc = populate(h))) return rc;
+    tis::launch_pair_sr(h->dev, h->stream, false);
+    tis::launch_pair_lr(h->dev, h->stream, false, false);
+    tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, false);
+    TIS_CUDA(cudaGetLastError());
+    return TIS_OK;
+}
+
+int tis_full_forces(tis_handle *h)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    tis::launch_noise(h->dev, h->stream);
+    TIS_CUDA(cudaGetLastError());
+    return TIS_OK;
+}
+
+int tis_move_rigid_units(tis_handle *h)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    tis::launch_integrate(h->dev, h->stream);
+    TIS_CUDA(cudaGetLastError());
+    return TIS_OK;
+}
+
+int tis_check_shifts(tis_handle *h)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    tis::launch_control(h->dev, h->stream);
+    tis::launch_rebuild(h->dev, h->stream);
+    TIS_CUDA(cudaGetLastError());
+    return TIS_OK;
+}
+
+int tis_step(tis_handle *h, int64_t n)
+{
+    if (!h || n < 0) return fail(TIS_ERR_ARG, "tis_step: bad argument");
+    int rc;
+    if (!h->lists_built && (rc = populate(h))) return rc;
+    int64_t left = n;
+    if (h->prm.use_graph && n >= h->prm.graph_steps) {
+        if (!h->graph) {
+            cudaGraph_t g;
+            TIS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            for (int s = 0; s < h->prm.graph_steps; ++s) enqueue_step(h);
+            TIS_CUDA(cudaStreamEndCapture(h->stream, &g));
+            cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+            h->graph_steps = h->prm.graph_steps;
+        }
+        while (left >= h->graph_steps) {
+            TIS_CUDA(cudaGraphLaunch(h->graph, h->stream));
+            left -= h->graph_steps;
+        }
+    }
+    for (int64_t s = 0; s < left; ++s) enqueue_step(h);
+    TIS_CUDA(cudaGetLastError());
+    h->launches += n * tis::kernel_launches_per_step();
+    return TIS_OK;
+}
+
+int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
+{
+    if (!h || n < 1 || !ms) return fail(TIS_ERR_ARG, "tis_profile_stages: bad argument");
+    int rc;
+    if (!h->lists_built && (rc = populate(h))) return rc;
+    cudaEvent_t ev[7];
+    for (auto &e : ev) TIS_CUDA(cudaEventCreate(&e));
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t s = 0; s < n; ++s) {
+        TIS_CUDA(cudaEventRecord(ev[0], h->stream));
+        tis::launch_pair_sr(h->dev, h->stream, false);
+        TIS_CUDA(cudaEventRecord(ev[1], h->stream));
+        tis::launch_pair_lr(h->dev, h->stream, false, false);
+        TIS_CUDA(cudaEventRecord(ev[2], h->stream));
+        tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true);
+        TIS_CUDA(cudaEventRecord(ev[3], h->stream));
+        tis::launch_integrate(h->dev, h->stream);
+        TIS_CUDA(cudaEventRecord(ev[4], h->stream));
+        tis::launch_control(h->dev, h->stream);
+        TIS_CUDA(cudaEventRecord(ev[5], h->stream));
+        tis::launch_rebuild(h->dev, h->stream);
+        TIS_CUDA(cudaEventRecord(ev[6], h->stream));
+        TIS_CUDA(cudaEventSynchronize(ev[6]));
+        for (int k = 0; k < 6; ++k) {
+            float t = 0;
+            TIS_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+            acc[k] += t;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 6; ++k) ms[k] = acc[k] / (double)n;
+    h->launches += n * tis::kernel_launches_per_step();
+    return check_flags(h);
+}
+
+int tis_sync(tis_handle *h)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    return check_flags(h);
+}
+
+int tis_get_energies(tis_handle *h, int r, double *out5)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    if (!out5) return fail(TIS_ERR_ARG, "null output");
+    tis::RepState st;
+    double rg = 0;
+    tis::launch_rg(h->dev, h->stream, r, h->d_scalar);
+    TIS_CUDA(cudaMemcpyAsync(&st, h->dev.rs + r, sizeof st, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaMemcpyAsync(&rg, h->d_scalar, sizeof rg, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    out5[0] = st.e2hb;
+    out5[1] = st.e3hb;
+    out5[2] = st.e2st;
+    out5[3] = st.e3st;
+    out5[4] = rg;
+    return TIS_OK;
+}
+
+int tis_get_stack_energies(tis_handle *h, int r, double *out, int64_t cap, int64_t *n)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    const RepHost &hr = h->rep[r];
+    const int64_t m = hr.s31 - hr.s30;
+    if (n) *n = m;
+    if (out && m > 0)
+        TIS_CUDA(cudaMemcpyAsync(out, h->dev.st_energy + hr.s30, sizeof(double) * std::min(m, cap), cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return TIS_OK;
+}
+
+int tis_get_counters(tis_handle *h, int r, int64_t *klok, int64_t *rebuilds, int64_t *draws)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    tis::RepState st;
+    TIS_CUDA(cudaMemcpyAsync(&st, h->dev.rs + r, sizeof st, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    if (klok) *klok = st.klok;
+    if (rebuilds) *rebuilds = st.rebuilds;
+    if (draws) *draws = (int64_t)st.ctr;
+    return TIS_OK;
+}
+
+int tis_get_info(tis_handle *h, int *n_replicas, int *device, void **stream)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    if (n_replicas) *n_replicas = h->R;
+    if (device) *device = h->prm.device;
+    if (stream) *stream = (void *)h->stream;
+    return TIS_OK;
+}
+
+int tis_replica_size(tis_handle *h, int r, int *n_particles)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    if (n_particles) *n_particles = h->rep[r].n;
+    return TIS_OK;
+}
+
+int tis_get_launch_count(tis_handle *h, int64_t *n)
+{
+    if (!h || !n) return fail(TIS_ERR_ARG, "bad argument");
+    *n = h->launches;
+    return TIS_OK;
+}
+
+}  // extern "C"

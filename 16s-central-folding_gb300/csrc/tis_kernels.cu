@@ -1,0 +1,1197 @@
+// CUDA kernels of the TIS-RNA Langevin step for sm_103a.
+//
+// One step of every replica (E: = src/16SCD_Mg_Cl_K_COPY_fast.cpp):
+//   k_pair_sr     SR_interactions_lists      E:1783-1847   per particle, full neighbour list
+//   k_pair_lr     LR_interactions_lists      E:1851-1907   every lr_interval steps or after a rebuild
+//   k_topology    stacking_interactions      E:1911-2141   one block per replica:
+//                 hydrogen_bonds_interactions E:2145-2350  energies, valence-limited MC, forces
+//                 polymer_constraints        E:2354-2520
+//                 full_forces (the Gaussians) E:2590-2611
+//   k_integrate   full_forces (application) + move_rigid_units + leap_frog_move_atom + adjust_box
+//                                             E:2612-2732, E:570-642
+//   k_control     check_shifts               E:1741-1776
+//   rebuild       populate_lists + separate_in_cells E:1461-1737, gated per replica
+#include <cstdio>
+
+#include "tis_kernels.cuh"
+
+namespace tis {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// position and force accessors
+// ---------------------------------------------------------------------------
+template <bool D>
+struct Pos;
+
+template <>
+struct Pos<false> {  // exact int32 differences -> FP32
+    const int4 *q;
+    float sx, sy, sz;
+    __device__ V3<float> vec(int a, int b) const  // position(b) - position(a)
+    {
+        int4 qa = q[a], qb = q[b];
+        return {(float)(int)((unsigned)qb.x - (unsigned)qa.x) * sx, (float)(int)((unsigned)qb.y - (unsigned)qa.y) * sy,
+                (float)(int)((unsigned)qb.z - (unsigned)qa.z) * sz};
+    }
+};
+
+template <>
+struct Pos<true> {  // FP64 raw differences, no image (as the reference's bonded terms)
+    const double *x, *y, *z;
+    __device__ V3<double> vec(int a, int b) const { return {x[b] - x[a], y[b] - y[a], z[b] - z[a]}; }
+};
+
+template <bool D>
+struct Acc;
+
+template <>
+struct Acc<false> {
+    unsigned long long *f;
+    int P;
+    int err;
+    __device__ void add(int i, V3<float> v)
+    {
+        atomic_add_fix(f + i, to_fix(v.x, err));
+        atomic_add_fix(f + P + i, to_fix(v.y, err));
+        atomic_add_fix(f + 2 * P + i, to_fix(v.z, err));
+    }
+};
+
+template <>
+struct Acc<true> {
+    double *f;
+    int P;
+    int err;
+    __device__ void add(int i, V3<double> v)
+    {
+        atomicAdd(f + i, v.x);
+        atomicAdd(f + P + i, v.y);
+        atomicAdd(f + 2 * P + i, v.z);
+    }
+};
+
+template <bool D>
+using Real = typename std::conditional<D, double, float>::type;
+
+template <bool D>
+__device__ inline Pos<D> make_pos(const Dev &d, const RepParams *R);
+template <>
+__device__ inline Pos<false> make_pos<false>(const Dev &d, const RepParams *R)
+{
+    return Pos<false>{d.q, R->qstep[0], R->qstep[1], R->qstep[2]};
+}
+template <>
+__device__ inline Pos<true> make_pos<true>(const Dev &d, const RepParams *)
+{
+    return Pos<true>{d.x, d.y, d.z};
+}
+
+__device__ inline float acos_(float v) { return acosf(v); }
+__device__ inline double acos_(double v) { return acos(v); }
+__device__ inline float atan2_(float a, float b) { return atan2f(a, b); }
+__device__ inline double atan2_(double a, double b) { return atan2(a, b); }
+__device__ inline float exp_(float v) { return expf(v); }
+__device__ inline double exp_(double v) { return exp(v); }
+__device__ inline float sqrt_(float v) { return sqrtf(v); }
+__device__ inline double sqrt_(double v) { return sqrt(v); }
+
+// ---------------------------------------------------------------------------
+// geometry and restraint forces (E:924-1454)
+// ---------------------------------------------------------------------------
+// valence_angle (E:986-1027): angle at i2
+template <bool D>
+__device__ Real<D> angle_of(const Pos<D> &P, int i1, int i2, int i3)
+{
+    using R = Real<D>;
+    V3<R> a = P.vec(i2, i1), b = P.vec(i2, i3);
+    R c = dot(a, b) / sqrt_(dot(a, a) * dot(b, b));
+    if (!D) c = fminf(1.0f, fmaxf(-1.0f, (float)c));
+    return acos_(c);
+}
+
+// dihedral_angle (E:1255-1302)
+template <bool D>
+__device__ Real<D> dihedral_of(const Pos<D> &P, int i1, int i2, int i3, int i4)
+{
+    using R = Real<D>;
+    V3<R> v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
+    V3<R> m = cross(v1, v2), n = cross(v2, v3);
+    return atan2_(dot(v1, n) * sqrt_(dot(v2, v2)), dot(m, n));
+}
+
+// harmonic bond k0 (r0 - r)^2 (bead_bond_force / stacking_bond_force, E:924-982)
+template <bool D>
+__device__ void bond_force(const Pos<D> &P, Acc<D> &A, int i1, int i2, Real<D> k0, Real<D> r0)
+{
+    using R = Real<D>;
+    V3<R> v = P.vec(i1, i2);
+    R r = sqrt_(dot(v, v));
+    R t = R(2) * k0 * (r0 - r) / r;
+    V3<R> g = t * v;
+    A.add(i1, R(-1) * g);
+    A.add(i2, g);
+}
+
+// harmonic angle (bead_valence_force E:1031-1134; clamp = stacking_valence_force E:1138-1251)
+template <bool D>
+__device__ void angle_force(const Pos<D> &P, Acc<D> &A, int i1, int i2, int i3, Real<D> k0, Real<D> th0, bool clamp)
+{
+    using R = Real<D>;
+    V3<R> a = P.vec(i2, i1), b = P.vec(i2, i3);
+    R ia = R(1) / dot(a, a), ib = R(1) / dot(b, b);
+    R iab = sqrt_(ia * ib);
+    R c = dot(a, b) * iab;
+    if (clamp && c < R(-0.99995)) return;  // theta = pi, no force
+    if (!D) c = fminf(1.0f, fmaxf(-1.0f, (float)c));
+    R sn = sqrt_(R(1) - c * c);
+    if (sn == R(0)) return;
+    R th = acos_(c);
+    R s = R(-2) * k0 * (th0 - th) / sn;
+    R ca = c * ia, cb = c * ib;
+    V3<R> g1 = iab * b - ca * a;
+    V3<R> g3 = iab * a - cb * b;
+    V3<R> g2 = R(-1) * (g1 + g3);
+    A.add(i1, s * g1);
+    A.add(i2, s * g2);
+    A.add(i3, s * g3);
+}
+
+// harmonic dihedral (stacking_dihedral_force, E:1306-1454): s * d(cos psi)/dx
+template <bool D>
+__device__ void dihedral_force(const Pos<D> &P, Acc<D> &A, int i1, int i2, int i3, int i4, Real<D> k0,
+                               Real<D> psi0)
+{
+    using R = Real<D>;
+    V3<R> v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
+    V3<R> m = cross(v1, v2), n = cross(v2, v3);
+    R im = R(1) / dot(m, m), in = R(1) / dot(n, n);
+    R imn = sqrt_(im * in);
+    R l2 = sqrt_(dot(v2, v2));
+    R c = dot(m, n) * imn;
+    R sn = dot(v1, n) * l2 * imn;
+    if (sn == R(0)) return;
+    R psi = atan2_(sn, c);
+    R s = R(-2) * k0 * (psi0 - psi) / sn;
+    R cm = c * im, cn = c * in;
+    V3<R> G1 = imn * cross(v2, n) - cm * cross(v2, m);
+    V3<R> G2 = imn * (cross(n, v1) + cross(v3, m)) - cm * cross(m, v1) - cn * cross(v3, n);
+    V3<R> G3 = imn * cross(m, v2) - cn * cross(n, v2);
+    A.add(i1, R(-1) * s * G1);
+    A.add(i2, s * (G1 - G2));
+    A.add(i3, s * (G2 - G3));
+    A.add(i4, s * G3);
+}
+
+// native dihedral imaged to within pi of the current one (E:1999-2019): branch -1/0/+1
+template <class R>
+__device__ inline int psi_branch(R psi, R nat)
+{
+    const R pi = R(3.14159265358979323846);
+    if (fabs(psi - nat) <= pi) return 0;
+    return (psi - nat > pi) ? 1 : -1;
+}
+
+template <class R>
+__device__ inline R psi_shift(R nat, int br)
+{
+    return nat + R(2.0 * 3.14159265358979323846) * R(br);
+}
+
+// six-term native-geometry restraint (E:1983-2056, E:2177-2231, E:2319-2349)
+template <bool D>
+__device__ Real<D> six_q(const Pos<D> &P, const int *k, const double *nat, Real<D> rdev, Real<D> init, int &code)
+{
+    using R = Real<D>;
+    R t1 = angle_of<D>(P, k[0], k[1], k[4]);
+    R t2 = angle_of<D>(P, k[3], k[4], k[1]);
+    R p0 = dihedral_of<D>(P, k[0], k[1], k[4], k[3]);
+    R p1 = dihedral_of<D>(P, k[4], k[1], k[0], k[2]);
+    R p2 = dihedral_of<D>(P, k[1], k[4], k[3], k[5]);
+    int b0 = psi_branch<R>(p0, (R)nat[3]), b1 = psi_branch<R>(p1, (R)nat[4]), b2 = psi_branch<R>(p2, (R)nat[5]);
+    code = (b0 + 1) + 3 * (b1 + 1) + 9 * (b2 + 1);
+    R d0 = p0 - psi_shift<R>((R)nat[3], b0), d1 = p1 - psi_shift<R>((R)nat[4], b1), d2 = p2 - psi_shift<R>((R)nat[5], b2);
+    R q = init + R(5) * rdev * rdev;
+    q += R(1.5) * (t1 - (R)nat[1]) * (t1 - (R)nat[1]);
+    q += R(1.5) * (t2 - (R)nat[2]) * (t2 - (R)nat[2]);
+    q += R(0.15) * d0 * d0;
+    q += R(0.15) * d1 * d1;
+    q += R(0.15) * d2 * d2;
+    return q;
+}
+
+template <bool D>
+__device__ void six_force(const Pos<D> &P, Acc<D> &A, const int *k, const double *nat, int code, Real<D> w)
+{
+    using R = Real<D>;
+    int b0 = code % 3 - 1, b1 = (code / 3) % 3 - 1, b2 = code / 9 - 1;
+    bond_force<D>(P, A, k[1], k[4], R(5) * w, (R)nat[0]);
+    angle_force<D>(P, A, k[0], k[1], k[4], R(1.5) * w, (R)nat[1], true);
+    angle_force<D>(P, A, k[3], k[4], k[1], R(1.5) * w, (R)nat[2], true);
+    dihedral_force<D>(P, A, k[0], k[1], k[4], k[3], R(0.15) * w, psi_shift<R>((R)nat[3], b0));
+    dihedral_force<D>(P, A, k[4], k[1], k[0], k[2], R(0.15) * w, psi_shift<R>((R)nat[4], b1));
+    dihedral_force<D>(P, A, k[1], k[4], k[3], k[5], R(0.15) * w, psi_shift<R>((R)nat[5], b2));
+}
+
+template <bool D>
+__device__ inline Real<D> distance(const Pos<D> &P, int a, int b)
+{
+    V3<Real<D>> v = P.vec(a, b);
+    return sqrt_(dot(v, v));
+}
+
+// ---------------------------------------------------------------------------
+// exact FP64 pair distance with the reference's image rule (CC_vector, E:674-683)
+// ---------------------------------------------------------------------------
+__device__ inline double exact_r2(const Dev &d, const RepParams *R, int i, int j)
+{
+    double a = __dsub_rn(d.x[i], d.x[j]);
+    double b = __dsub_rn(d.y[i], d.y[j]);
+    double c = __dsub_rn(d.z[i], d.z[j]);
+    if (a > R->hbox[0]) a = __dsub_rn(a, R->box[0]);
+    if (a < -R->hbox[0]) a = __dadd_rn(a, R->box[0]);
+    if (b > R->hbox[1]) b = __dsub_rn(b, R->box[1]);
+    if (b < -R->hbox[1]) b = __dadd_rn(b, R->box[1]);
+    if (c > R->hbox[2]) c = __dsub_rn(c, R->box[2]);
+    if (c < -R->hbox[2]) c = __dadd_rn(c, R->box[2]);
+    return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+}
+
+__device__ inline void exact_vec(const Dev &d, const RepParams *R, int i, int j, double v[3])
+{
+    v[0] = d.x[i] - d.x[j];
+    v[1] = d.y[i] - d.y[j];
+    v[2] = d.z[i] - d.z[j];
+    for (int k = 0; k < 3; ++k) {
+        if (v[k] > R->hbox[k]) v[k] = v[k] - R->box[k];
+        if (v[k] < -R->hbox[k]) v[k] = v[k] + R->box[k];
+    }
+}
+
+__device__ inline bool is_charged(int kind) { return kind != 1 && kind != 2; }
+
+// Relative half-width of the band around a threshold inside which the FP32
+// squared distance cannot decide a comparison and the exact FP64 one is used.
+constexpr float kBand = 1.0e-5f;
+
+// ---------------------------------------------------------------------------
+// quantisation: fixed-point copy of the FP64 positions
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_quantize(Dev d)
+{
+    int p = blockIdx.x * kBlock + threadIdx.x;
+    const RepParams *R = d.rp + d.blk_rep[blockIdx.x];
+    int4 q = d.q[p];
+    q.x = (int)(unsigned)(long long)floor(d.x[p] * R->qinv[0]);
+    q.y = (int)(unsigned)(long long)floor(d.y[p] * R->qinv[1]);
+    q.z = (int)(unsigned)(long long)floor(d.z[p] * R->qinv[2]);
+    d.q[p] = q;
+}
+
+// ---------------------------------------------------------------------------
+// pair forces over the full (both-direction) neighbour lists
+// ---------------------------------------------------------------------------
+template <bool D, bool LR, bool EN>
+__global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
+{
+    const int r = d.blk_rep[blockIdx.x];
+    const RepParams *R = d.rp + r;
+    if (LR && !force_all && !d.rs[r].lr_now) return;
+    __shared__ float s_dlj2[46], s_dm[46], s_flj[46], s_qclb[46];
+    if (!D) {
+        for (int t = threadIdx.x; t < 46; t += kBlock) {
+            s_dlj2[t] = R->dlj2[t];
+            s_dm[t] = R->dm[t];
+            s_flj[t] = R->flj[t];
+            s_qclb[t] = R->qclb[t];
+        }
+        __syncthreads();
+    }
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int P = d.P;
+    const int4 qp = d.q[p];
+    const int tp = qp.w & 0xff, kp = (qp.w >> 8) & 0xff, act = (qp.w >> 16) & 1;
+    const bool chp = is_charged(kp);
+    const int cnt = act ? (LR ? d.n_lr[p] : d.n_sr[p]) : 0;
+    const int *nbr = LR ? d.nbr_lr : d.nbr_sr;
+    int err = 0;
+    double e_lj = 0, e_c = 0;
+    if (!D) {
+        long long ax = 0, ay = 0, az = 0;
+        const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
+        const float rc2 = R->rc2f, lo = rc2 * (1.0f - kBand), hi = rc2 * (1.0f + kBand);
+        for (int k = 0; k < cnt; ++k) {
+            const int j = __ldg(nbr + (size_t)k * P + p);
+            const int4 qj = __ldg(d.q + j);
+            const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
+            const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
+            const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const int tj = qj.w & 0xff, kj = (qj.w >> 8) & 0xff;
+            const int J = jn12(tp, tj);
+            float F = 0.0f;
+            if (!LR && r2 <= s_dlj2[J]) {  // LJ_FORCE (E:801-821)
+                const float rr = sqrtf(r2);
+                const float dr = rr - s_dm[J];
+                const float s = 1.5852f / dr;
+                const float s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+                F = s_flj[J] * (s14 - s8) * dr / rr;
+                if (EN) {
+                    double e;
+                    if ((double)r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
+                    else {
+                        const float s6 = s4 * s2, s12 = s6 * s6;
+                        e = (double)(R->elj[J] * (s12 - 2.0f * s6 + 1.0f));
+                    }
+                    e_lj += 0.5 * e;
+                }
+            }
+            if ((LR || (chp && is_charged(kj))) && r2 <= hi) {  // COULOMB_TRUNCATED_FORCE (E:841-855)
+                bool in = r2 <= lo || exact_r2(d, R, p, j) <= R->rc2;
+                if (in) {
+                    const float rr = sqrtf(r2);
+                    F += s_qclb[J] / (r2 * rr);
+                    if (EN) e_c += 0.5 * (double)(s_qclb[J] / rr);
+                }
+            }
+            if (F != 0.0f) {
+                ax += to_fix(F * dx, err);
+                ay += to_fix(F * dy, err);
+                az += to_fix(F * dz, err);
+            }
+        }
+        unsigned long long *out = LR ? d.flr : d.f;
+        out[p] = (unsigned long long)ax;
+        out[P + p] = (unsigned long long)ay;
+        out[2 * P + p] = (unsigned long long)az;
+    } else {
+        double ax = 0, ay = 0, az = 0;
+        for (int k = 0; k < cnt; ++k) {
+            const int j = __ldg(nbr + (size_t)k * P + p);
+            const int tj = d.q[j].w & 0xff, kj = (d.q[j].w >> 8) & 0xff;
+            const int J = jn12(tp, tj);
+            double v[3];
+            exact_vec(d, R, p, j, v);
+            const double r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+            double F = 0.0;
+            if (!LR && r2 <= R->dlj2_d[J]) {
+                const double rr = sqrt(r2);
+                const double dr = rr + kSig0 - R->dlj_d[J];
+                const double s = kSig0 / dr;
+                const double s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+                F = R->flj_d[J] * (s14 - s8) * dr / rr;
+                if (EN) {
+                    double e;
+                    if (r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
+                    else {
+                        const double s6 = s4 * s2, s12 = s6 * s6;
+                        e = R->elj_d[J] * (s12 - 2.0 * s6 + 1.0);
+                    }
+                    e_lj += 0.5 * e;
+                }
+            }
+            if ((LR || (chp && is_charged(kj))) && r2 <= R->rc2) {
+                const double rr = sqrt(r2);
+                F += R->qclb_d[J] / (rr * r2);
+                if (EN) e_c += 0.5 * R->qclb_d[J] / rr;
+            }
+            ax += v[0] * F;
+            ay += v[1] * F;
+            az += v[2] * F;
+        }
+        double *out = (double *)(LR ? d.flr : d.f);
+        out[p] = ax;
+        out[P + p] = ay;
+        out[2 * P + p] = az;
+    }
+    if (EN) {
+        if (!LR) atomicAdd(d.eterm + r * kNE + 0, e_lj);
+        atomicAdd(d.eterm + r * kNE + (LR ? 2 : 1), e_c);
+    }
+    if (err) atomicOr(&d.rs[r].err, err);
+}
+
+// ---------------------------------------------------------------------------
+// block reductions
+// ---------------------------------------------------------------------------
+template <int NV>
+__device__ void block_sum(double (&v)[NV], double *smem /* NV * 32 */)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+        for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_down_sync(kFull, v[i], o);
+    __syncthreads();
+    if (lane == 0)
+        for (int i = 0; i < NV; ++i) smem[i * 32 + w] = v[i];
+    __syncthreads();
+    if (w == 0) {
+        for (int i = 0; i < NV; ++i) {
+            double t = lane < nw ? smem[i * 32 + lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(kFull, t, o);
+            v[i] = t;
+        }
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// integrator: noise application, leap-frog, recentring, ion wrap, skin check
+// ---------------------------------------------------------------------------
+template <bool D>
+__device__ inline double total_force(const Dev &d, int p, int c)
+{
+    if (D) {
+        const double *f = (const double *)d.f, *fl = (const double *)d.flr;
+        return __ldcg(f + c * d.P + p) + __ldcg(fl + c * d.P + p);
+    }
+    const long long t = (long long)(__ldcg(d.f + c * d.P + p) + __ldcg(d.flr + c * d.P + p));
+    return (double)t * (1.0 / kFixScale);
+}
+
+// leap_frog_move_atom (E:570-642) with the noise of full_forces (E:2612-2622)
+template <bool D>
+__device__ inline void leap_frog(const Dev &d, const RepParams *R, int r, int p, double xn[3], double vn[3])
+{
+    const int t = d.q[p].w & 0xff;
+    double f[3] = {total_force<D>(d, p, 0), total_force<D>(d, p, 1), total_force<D>(d, p, 2)};
+    if (d.noise == 0) {
+        const int k = (p - R->p0 + 1) % 1000;
+        const float *g = d.gnoise + r * kNoise;
+        const double sg = R->sigma[t];
+        f[0] = f[0] + (double)g[k] * sg;
+        f[1] = f[1] + (double)g[k + 1000] * sg;
+        f[2] = f[2] + (double)g[k + 2000] * sg;
+    }
+    const double v0[3] = {d.vx[p], d.vy[p], d.vz[p]};
+    const double x0[3] = {d.x[p], d.y[p], d.z[p]};
+    const double o0[3] = {d.xo[p], d.yo[p], d.zo[p]};
+    for (int c = 0; c < 3; ++c) vn[c] = __dadd_rn(__dmul_rn(R->k1[t], v0[c]), __dmul_rn(R->k2[t], f[c]));
+    double vsq = __dmul_rn(R->mass[t], __dadd_rn(__dadd_rn(__dmul_rn(vn[0], vn[0]), __dmul_rn(vn[1], vn[1])),
+                                                  __dmul_rn(vn[2], vn[2])));
+    vsq = vsq / (300.0 * R->T);
+    if (vsq > 1.0) {
+        vsq = 1.0 / sqrt(vsq);
+        for (int c = 0; c < 3; ++c) vn[c] *= vsq;
+    }
+    for (int c = 0; c < 3; ++c)
+        xn[c] = __dadd_rn(__dsub_rn(__dmul_rn(2.0, x0[c]), o0[c]), __dmul_rn(__dsub_rn(vn[c], v0[c]), R->h));
+}
+
+// full_forces' Gaussians (E:2594-2606) for one replica, then the recentring
+// shift of adjust_box (E:2632-2656) from the centre bead's new position.  Runs
+// in one block after every force on the replica is final.
+template <bool D>
+__device__ void noise_and_shift(const Dev &d, int r, unsigned long long &s_ctr)
+{
+    const RepParams *R = d.rp + r;
+    __syncthreads();
+    const unsigned long long c0 = s_ctr;
+    if (d.noise == 0) {
+        for (int t = threadIdx.x; t < kNoise / 2; t += blockDim.x) {
+            const uint32_t v1 = rand_value(R->seed, c0 + 2 * t);
+            const uint32_t v2 = rand_value(R->seed, c0 + 2 * t + 1);
+            const float a = bm_radius(v1);
+            float sn, cs;
+            sincospif(2.0f * ((float)v2 * (1.0f / 2147483647.0f)), &sn, &cs);
+            d.gnoise[r * kNoise + 2 * t] = a * cs;
+            d.gnoise[r * kNoise + 2 * t + 1] = a * sn;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_ctr = c0 + kNoise;  // the reference draws them even when the noise amplitude is zero
+        double xn[3], vn[3];
+        leap_frog<D>(d, R, r, R->center, xn, vn);
+        for (int c = 0; c < 3; ++c) d.shift[3 * r + c] = R->hbox[c] - xn[c];
+    }
+}
+
+template <bool D>
+__global__ void k_noise(Dev d)
+{
+    __shared__ unsigned long long s_ctr;
+    const int r = blockIdx.x;
+    if (threadIdx.x == 0) s_ctr = d.rs[r].ctr;
+    noise_and_shift<D>(d, r, s_ctr);
+    if (threadIdx.x == 0) d.rs[r].ctr = s_ctr;
+}
+
+// ---------------------------------------------------------------------------
+// topology terms of one replica per block: bonded, stacking, hydrogen bonds
+// with the valence-limited Monte Carlo, and this step's Gaussians
+// ---------------------------------------------------------------------------
+constexpr int kTopoThreads = 256;
+
+template <bool D, bool EN>
+__global__ void __launch_bounds__(kTopoThreads) k_topology(Dev d, int mask, int make_noise)
+{
+    using Rl = Real<D>;
+    const int r = blockIdx.x;
+    const RepParams *R = d.rp + r;
+    RepState *S = d.rs + r;
+    const Pos<D> P = make_pos<D>(d, R);
+    Acc<D> A;
+    A.f = (decltype(A.f))d.f;
+    A.P = d.P;
+    A.err = 0;
+    __shared__ unsigned long long s_ctr;
+    __shared__ double s_red[8 * 32];
+    if (threadIdx.x == 0) s_ctr = S->ctr;
+    double e_bond = 0, e_angle = 0, e_excl = 0, e2st = 0, e3st = 0, e2hb = 0, e3hb = 0;
+
+    // ---- polymer_constraints (E:2354-2520) ----
+    if (mask & 4) {
+        for (int t = R->bt0 + threadIdx.x; t < R->bt1; t += blockDim.x) {
+            const int4 id = d.bt_idx[t];
+            const double2 par = d.bt_par[t];
+            const int ex = id.w == 0 ? id.y : id.z;  // excluded pair partner of id.x
+            if (id.w == 0) bond_force<D>(P, A, id.x, id.y, (Rl)par.x, (Rl)par.y);
+            else angle_force<D>(P, A, id.x, id.y, id.z, (Rl)par.x, (Rl)par.y, false);
+            // subtract the LJ force of the excluded pair (reduce_forces, E:880-897)
+            const int ta = d.q[id.x].w & 0xff, tb = d.q[ex].w & 0xff;
+            const int J = jn12(ta, tb);
+            V3<Rl> v = P.vec(ex, id.x);  // x_a - x_ex, minimum image
+            if (D) {
+                double w[3];
+                exact_vec(d, R, id.x, ex, w);
+                v = V3<Rl>{(Rl)w[0], (Rl)w[1], (Rl)w[2]};
+            }
+            const Rl r2 = dot(v, v);
+            Rl F = 0;
+            if (r2 <= (Rl)(D ? R->dlj2_d[J] : R->dlj2[J])) {
+                const Rl rr = sqrt_(r2);
+                const Rl dr = D ? (Rl)(rr + kSig0 - R->dlj_d[J]) : (Rl)(rr - R->dm[J]);
+                const Rl s = Rl(1.5852) / dr;
+                const Rl s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+                F = (Rl)(D ? R->flj_d[J] : R->flj[J]) * (s14 - s8) * dr / rr;
+                if (EN) {
+                    double e;
+                    if ((double)r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
+                    else {
+                        const Rl s6 = s4 * s2, s12 = s6 * s6;
+                        e = (double)((Rl)(D ? R->elj_d[J] : R->elj[J]) * (s12 - Rl(2) * s6 + Rl(1)));
+                    }
+                    e_excl -= e;
+                }
+            }
+            if (F != Rl(0)) {
+                const V3<Rl> g = (Rl(-1) * F) * v;
+                A.add(id.x, g);
+                A.add(ex, Rl(-1) * g);
+            }
+            if (EN) {
+                if (id.w == 0) {
+                    const Rl rr = distance<D>(P, id.x, id.y);
+                    e_bond += (double)((Rl)par.x * (rr - (Rl)par.y) * (rr - (Rl)par.y));
+                } else {
+                    const Rl th = angle_of<D>(P, id.x, id.y, id.z);
+                    e_angle += (double)((Rl)par.x * (th - (Rl)par.y) * (th - (Rl)par.y));
+                }
+            }
+        }
+    }
+
+    // ---- stacking_interactions (E:1911-2141) ----
+    if (mask & 8) {
+        for (int k = R->s20 + threadIdx.x; k < R->s21; k += blockDim.x) d.st2_off_flag[k] = 0;
+        __syncthreads();
+        for (int k = R->s30 + threadIdx.x; k < R->s31; k += blockDim.x) {
+            const int *id = d.st3_idx + 6 * k;
+            if (distance<D>(P, id[1], id[4]) - (Rl)d.st3_nat[6 * k] < Rl(10)) {
+                for (int s = 0; s < 2; ++s) {
+                    const int t = d.st3_off[2 * k + s];
+                    if (t >= 0) d.st2_off_flag[R->s20 + t] = 1;
+                }
+            }
+        }
+        __syncthreads();
+        for (int k = R->s30 + threadIdx.x; k < R->s31; k += blockDim.x) {
+            const int *id = d.st3_idx + 6 * k;
+            const double *nat = d.st3_nat + 6 * k;
+            const Rl rdev = distance<D>(P, id[1], id[4]) - (Rl)nat[0];
+            int code;
+            const Rl Dn = six_q<D>(P, id, nat, rdev, Rl(1), code);
+            const Rl E = (Rl)d.st3_E[k] / Dn;
+            six_force<D>(P, A, id, nat, code, -E / Dn);
+            e3st += (double)E;
+            d.st_energy[k] = (double)E;
+        }
+        for (int k = R->s20 + threadIdx.x; k < R->s21; k += blockDim.x) {
+            if (d.st2_off_flag[k]) continue;
+            const int *id = d.st2_idx + 7 * k;  // k_10 k00 k01 k10 k20 k21 k30
+            const Rl rr = distance<D>(P, id[2], id[5]);
+            const Rl p1 = dihedral_of<D>(P, id[0], id[1], id[3], id[4]);
+            const Rl p2 = dihedral_of<D>(P, id[6], id[4], id[3], id[1]);
+            const Rl p10 = psi_shift<Rl>(Rl(-2.58684), psi_branch<Rl>(p1, Rl(-2.58684)));
+            const Rl p20 = psi_shift<Rl>(Rl(3.07135), psi_branch<Rl>(p2, Rl(3.07135)));
+            const Rl r0 = (Rl)d.st2_r0[k];
+            Rl Dn = Rl(1) + Rl(1.4) * (rr - r0) * (rr - r0);
+            Dn += Rl(4) * (p1 - p10) * (p1 - p10);
+            Dn += Rl(4) * (p2 - p20) * (p2 - p20);
+            const Rl E = (Rl)d.st2_E[k] / Dn;
+            const Rl w = -E / Dn;
+            bond_force<D>(P, A, id[2], id[5], Rl(1.4) * w, r0);
+            dihedral_force<D>(P, A, id[0], id[1], id[3], id[4], Rl(4) * w, p10);
+            dihedral_force<D>(P, A, id[6], id[4], id[3], id[1], Rl(4) * w, p20);
+            e2st += (double)E;
+        }
+    }
+
+    // ---- hydrogen_bonds_interactions (E:2145-2350) ----
+    if (mask & 16) {
+        for (int a = R->hba0 + threadIdx.x; a < R->hba1; a += blockDim.x) d.excess[a] = d.hb_excess[a];
+        __syncthreads();
+        const int nact = S->n_active;
+        for (int t = threadIdx.x; t < nact; t += blockDim.x) {
+            const int k = d.hb_active[R->hb0 + t];
+            const int *id = d.hb_idx + 6 * k;
+            const double *nat = d.hb_nat + 6 * k;
+            const Rl rr = distance<D>(P, id[1], id[4]);
+            if (fabs((double)(rr - (Rl)nat[0])) > 2.0) {
+                d.hb_status[k] = 1;
+                for (int u = d.hb_aoff[k]; u < d.hb_aoff[k + 1]; ++u) atomicSub(d.excess + d.hb_aidx[u], 1);
+                d.hb_energy[k] = 0.0;
+                continue;
+            }
+            int code;
+            const Rl q = six_q<D>(P, id, nat, rr - (Rl)nat[0], Rl(0), code);
+            d.hb_energy[k] = (double)((Rl)d.hb_E[k] * exp_(-q));
+            d.hb_code[k] = code;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {  // valence-limited Monte Carlo (E:2239-2315), one warp
+            const int lane = threadIdx.x;
+            const unsigned lt = (1u << lane) - 1u;
+            unsigned long long ctr = s_ctr;
+            const int ca0 = R->ca0, nca = R->ca1 - R->ca0;
+            const double T = R->T;
+            int guard = nact + 2;
+            while (guard-- > 0) {
+                int nA = 0;
+                for (int base = 0; base < nca; base += 32) {
+                    const int i = base + lane;
+                    const int a = i < nca ? d.ca_list[ca0 + i] : -1;
+                    const bool pos = a >= 0 && d.excess[a] > 0;
+                    const unsigned m = __ballot_sync(kFull, pos);
+                    if (pos) d.hb_A[ca0 + nA + __popc(m & lt)] = a;
+                    nA += __popc(m);
+                }
+                __syncwarp();
+                if (nA == 0) break;
+                int bad = 0;
+                if (lane == 0) {
+                    double u = rand_uniform(R->seed, ctr++);
+                    int j = (int)ceil(u * nA);
+                    if (j == nA + 1) j = nA;
+                    if (j == 0) j = 1;
+                    const int atom = d.hb_A[ca0 + j - 1];
+                    int *K = d.hb_K + R->kscr0;
+                    int nK = 0;
+                    for (int t = d.hba_coff[atom]; t < d.hba_coff[atom + 1]; ++t) {
+                        const int k = d.hba_cidx[t];
+                        if (d.hb_status[k] == 0 && nK < R->maxk) K[nK++] = k;
+                    }
+                    if (nK == 0) bad = 1;
+                    else {
+                        for (int i = 1; i <= nK; ++i) {
+                            u = rand_uniform(R->seed, ctr++);
+                            j = (int)ceil(u * nK);
+                            if (j == nK + 1) j = nK;
+                            if (j == 0) j = 1;
+                            const int tmp = K[i - 1];
+                            K[i - 1] = K[j - 1];
+                            K[j - 1] = tmp;
+                        }
+                        int k = K[0];
+                        for (int i = 2; i <= nK; ++i) {
+                            const int c = K[i - 1];
+                            const double acc = exp((d.hb_energy[c] - d.hb_energy[k]) / T);
+                            u = rand_uniform(R->seed, ctr++);
+                            if (u < acc) k = c;
+                        }
+                        d.hb_status[k] = 1;
+                        for (int t = d.hb_aoff[k]; t < d.hb_aoff[k + 1]; ++t) d.excess[d.hb_aidx[t]] -= 1;
+                    }
+                }
+                bad = __shfl_sync(kFull, bad, 0);
+                __syncwarp();
+                if (bad) {
+                    A.err |= kErrRange;
+                    break;
+                }
+            }
+            if (lane == 0) s_ctr = ctr;
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < nact; t += blockDim.x) {
+            const int k = d.hb_active[R->hb0 + t];
+            if (d.hb_status[k] == 1) {
+                d.hb_status[k] = 0;
+                continue;
+            }
+            const Rl w = -(Rl)d.hb_energy[k];
+            if (d.hb_dode[k]) e3hb -= (double)w;
+            else e2hb -= (double)w;
+            six_force<D>(P, A, d.hb_idx + 6 * k, d.hb_nat + 6 * k, d.hb_code[k], w);
+        }
+    }
+
+    // ---- full_forces: the step's Gaussians, then the recentring shift ----
+    if (make_noise) noise_and_shift<D>(d, r, s_ctr);
+
+    double v[7] = {e2hb, e3hb, e2st, e3st, e_bond, e_angle, e_excl};
+    block_sum<7>(v, s_red);
+    if (threadIdx.x == 0) {
+        S->ctr = s_ctr;
+        if (mask & 16) { S->e2hb = v[0]; S->e3hb = v[1]; }
+        if (mask & 8) { S->e2st = v[2]; S->e3st = v[3]; }
+        if (EN) {
+            double *e = d.eterm + r * kNE;
+            e[3] += v[4]; e[4] += v[5]; e[5] += v[6];
+            e[6] += v[2]; e[7] += v[3]; e[8] += v[0]; e[9] += v[1];
+        }
+    }
+    if (A.err) atomicOr(&S->err, A.err);
+}
+
+template <bool D>
+__global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
+{
+    const int r = d.blk_rep[blockIdx.x];
+    const RepParams *R = d.rp + r;
+    __shared__ unsigned long long s_max;
+    if (threadIdx.x == 0) s_max = 0ull;
+    __syncthreads();
+    const double s_shift[3] = {d.shift[3 * r], d.shift[3 * r + 1], d.shift[3 * r + 2]};
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int4 qp = d.q[p];
+    double d2 = 0.0;
+    int err = 0;
+    if ((qp.w >> 16) & 1) {
+        double xn[3], vn[3];
+        leap_frog<D>(d, R, r, p, xn, vn);
+        double xo[3] = {d.x[p], d.y[p], d.z[p]};
+        for (int c = 0; c < 3; ++c) {
+            xn[c] = xn[c] + s_shift[c];
+            xo[c] = xo[c] + s_shift[c];
+        }
+        if (p - R->p0 >= R->nrna) {  // periodic wrap of the ions (E:2676-2731)
+            for (int c = 0; c < 3; ++c) {
+                if (xn[c] < 0) { xn[c] += R->box[c]; xo[c] += R->box[c]; }
+                if (xn[c] > R->box[c]) { xn[c] -= R->box[c]; xo[c] -= R->box[c]; }
+            }
+        }
+        for (int c = 0; c < 3; ++c) {
+            const double e = xn[c] - xo[c];
+            d2 += e * e;
+            if (!(fabs(xn[c]) < 1.0e6) || !(fabs(vn[c]) < 1.0e6)) err |= kErrNonFinite;
+        }
+        d.x[p] = xn[0]; d.y[p] = xn[1]; d.z[p] = xn[2];
+        d.xo[p] = xo[0]; d.yo[p] = xo[1]; d.zo[p] = xo[2];
+        d.vx[p] = vn[0]; d.vy[p] = vn[1]; d.vz[p] = vn[2];
+        int4 q = qp;
+        q.x = (int)(unsigned)(long long)floor(xn[0] * R->qinv[0]);
+        q.y = (int)(unsigned)(long long)floor(xn[1] * R->qinv[1]);
+        q.z = (int)(unsigned)(long long)floor(xn[2] * R->qinv[2]);
+        d.q[p] = q;
+    }
+    // check_shifts (E:1745-1762): max |x - x_old|^2; non-negative doubles order as integers
+    unsigned long long bits = (unsigned long long)__double_as_longlong(d2);
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long b = __shfl_down_sync(kFull, bits, o);
+        bits = b > bits ? b : bits;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(&s_max, bits);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(&d.rs[r].maxd2, s_max);
+    if (err) atomicOr(&d.rs[r].err, err);
+}
+
+// check_shifts (E:1741-1776) and the LR gate of deterministic_forces_MPI (E:2550)
+__global__ void k_control(Dev d)
+{
+    const int r = blockIdx.x;
+    const RepParams *R = d.rp + r;
+    RepState *S = d.rs + r;
+    __shared__ int s_reb;
+    if (threadIdx.x == 0) {
+        const double d2 = __longlong_as_double((long long)S->maxd2);
+        S->maxd2 = 0ull;
+        const double sh = sqrt(d2);
+        S->progress += (sh + sh);
+        S->klok += 1;
+        int reb = S->progress > R->skin;
+        if (reb) S->progress = 0.0;
+        S->rebuild = reb;
+        const long long kn = S->klok + 1;
+        S->lr_now = (R->lr_interval <= 1) || (kn % R->lr_interval == 1) || (S->progress == 0.0);
+        s_reb = reb;
+    }
+    __syncthreads();
+    if (s_reb)
+        for (int c = threadIdx.x; c < R->nc; c += blockDim.x) d.cell_count[R->c0 + c] = 0;
+}
+
+__global__ void k_force_rebuild(Dev d)
+{
+    const int r = blockIdx.x;
+    const RepParams *R = d.rp + r;
+    RepState *S = d.rs + r;
+    if (threadIdx.x == 0) {
+        S->rebuild = 1;
+        S->progress = 0.0;
+        S->lr_now = 1;
+        S->maxd2 = 0ull;
+    }
+    for (int c = threadIdx.x; c < R->nc; c += blockDim.x) d.cell_count[R->c0 + c] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// list rebuild (populate_lists, E:1546-1737)
+// ---------------------------------------------------------------------------
+// separate_in_cells (E:1461-1542): single periodic wrap then ceil(tmp / l)
+__device__ inline int cell_axis(double v, double side, double l)
+{
+    double t = v;
+    if (t < 0) t = __dadd_rn(t, side);
+    else if (t > side) t = __dsub_rn(t, side);
+    return (int)ceil(__ddiv_rn(t, l));
+}
+
+__global__ void __launch_bounds__(kBlock) k_cell_assign(Dev d)
+{
+    const int r = d.blk_rep[blockIdx.x];
+    if (!d.rs[r].rebuild) return;
+    const RepParams *R = d.rp + r;
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    if (!((d.q[p].w >> 16) & 1)) {
+        d.cell_of[p] = -1;
+        return;
+    }
+    const int i1 = cell_axis(d.x[p], R->box[0], R->lcell[0]);
+    const int i2 = cell_axis(d.y[p], R->box[1], R->lcell[1]);
+    const int i3 = cell_axis(d.z[p], R->box[2], R->lcell[2]);
+    if (i1 < 1 || i1 > R->mc[0] || i2 < 1 || i2 > R->mc[1] || i3 < 1 || i3 > R->mc[2]) {
+        d.cell_of[p] = -1;
+        atomicOr(&d.rs[r].err, kErrRange);
+        return;
+    }
+    const int c = (i1 - 1) * R->mc[1] * R->mc[2] + (i2 - 1) * R->mc[2] + (i3 - 1);
+    d.cell_of[p] = c;
+    atomicAdd(d.cell_count + R->c0 + c, 1);
+}
+
+__global__ void k_cell_scan(Dev d)
+{
+    const int r = blockIdx.x;
+    if (!d.rs[r].rebuild) return;
+    const RepParams *R = d.rp + r;
+    __shared__ int s_warp[32];
+    __shared__ int s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int base = 0; base < R->nc; base += blockDim.x) {
+        const int c = base + threadIdx.x;
+        const int v = c < R->nc ? d.cell_count[R->c0 + c] : 0;
+        int incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) s_warp[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            int t = lane < nw ? s_warp[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(kFull, t, o);
+                if (lane >= o) t += u;
+            }
+            if (lane < nw) s_warp[lane] = t;
+        }
+        __syncthreads();
+        const int excl = s_carry + (w > 0 ? s_warp[w - 1] : 0) + incl - v;
+        if (c < R->nc) {
+            d.cell_start[R->c0 + c] = excl;
+            d.cell_fill[R->c0 + c] = 0;
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) s_carry = excl + v;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_cell_fill(Dev d)
+{
+    const int r = d.blk_rep[blockIdx.x];
+    if (!d.rs[r].rebuild) return;
+    const RepParams *R = d.rp + r;
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int c = d.cell_of[p];
+    if (c < 0) return;
+    const int slot = atomicAdd(d.cell_fill + R->c0 + c, 1);
+    d.cell_list[R->p0 + d.cell_start[R->c0 + c] + slot] = p;
+}
+
+// particles of a cell in index order, as the reference appends them (E:1536-1540)
+__global__ void k_cell_sort(Dev d)
+{
+    const int cg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cg >= d.C) return;
+    const int r = d.cell_rep[cg];
+    if (!d.rs[r].rebuild) return;
+    const RepParams *R = d.rp + r;
+    int *seg = d.cell_list + R->p0 + d.cell_start[cg];
+    const int n = d.cell_count[cg];
+    for (int i = 1; i < n; ++i) {
+        const int v = seg[i];
+        int j = i - 1;
+        while (j >= 0 && seg[j] > v) {
+            seg[j + 1] = seg[j];
+            --j;
+        }
+        seg[j + 1] = v;
+    }
+}
+
+// distinct periodic neighbours of cell index i (1..m) along one axis
+__device__ inline int axis_neighbours(int i, int m, int out[3])
+{
+    int n = 0;
+    for (int dd = -1; dd <= 1; ++dd) {
+        int v = i + dd;
+        if (v < 1) v += m;
+        if (v > m) v -= m;
+        bool dup = false;
+        for (int t = 0; t < n; ++t) dup |= (out[t] == v);
+        if (!dup) out[n++] = v;
+    }
+    return n;
+}
+
+// SR and LR neighbour lists (E:1576-1694).  A pair is SR when r^2 <= (sr+skin)^2,
+// else LR when r^2 <= (rc+skin)^2 and neither bead is a sugar or a base.  The FP32
+// distance from the exact integer differences decides outside a narrow band
+// around each threshold; inside it the FP64 distance with the reference's
+// rounding and image rule decides, so the lists are the reference's sets.
+template <bool D>
+__global__ void __launch_bounds__(kBlock) k_pair_search(Dev d)
+{
+    const int r = d.blk_rep[blockIdx.x];
+    if (!d.rs[r].rebuild) return;
+    const RepParams *R = d.rp + r;
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int P = d.P;
+    const int c = d.cell_of[p];
+    if (c < 0) {
+        d.n_sr[p] = 0;
+        d.n_lr[p] = 0;
+        return;
+    }
+    const int4 qp = d.q[p];
+    const bool chp = is_charged((qp.w >> 8) & 0xff);
+    const int i1 = c / (R->mc[1] * R->mc[2]) + 1, i2 = (c / R->mc[2]) % R->mc[1] + 1, i3 = c % R->mc[2] + 1;
+    int n1[3], n2[3], n3[3];
+    const int m1 = axis_neighbours(i1, R->mc[0], n1);
+    const int m2 = axis_neighbours(i2, R->mc[1], n2);
+    const int m3 = axis_neighbours(i3, R->mc[2], n3);
+    const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
+    const float sr_lo = R->r2srf * (1.0f - kBand), sr_hi = R->r2srf * (1.0f + kBand);
+    const float lr_lo = R->r2lrf * (1.0f - kBand), lr_hi = R->r2lrf * (1.0f + kBand);
+    int nsr = 0, nlr = 0;
+    for (int a = 0; a < m1; ++a)
+        for (int b = 0; b < m2; ++b)
+            for (int e = 0; e < m3; ++e) {
+                const int cc = (n1[a] - 1) * R->mc[1] * R->mc[2] + (n2[b] - 1) * R->mc[2] + (n3[e] - 1);
+                const int start = R->p0 + d.cell_start[R->c0 + cc];
+                const int cnt = d.cell_count[R->c0 + cc];
+                for (int t = 0; t < cnt; ++t) {
+                    const int j = d.cell_list[start + t];
+                    if (j == p) continue;
+                    const int4 qj = d.q[j];
+                    const bool ch = chp && is_charged((qj.w >> 8) & 0xff);
+                    int cls;  // 0 none, 1 SR, 2 LR
+                    if (D) {
+                        const double r2 = exact_r2(d, R, p, j);
+                        cls = r2 <= R->r2sr ? 1 : ((ch && r2 <= R->r2lr) ? 2 : 0);
+                    } else {
+                        const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
+                        const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
+                        const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        if (r2 < sr_lo) cls = 1;
+                        else if (r2 > sr_hi && (!ch || r2 > lr_hi)) cls = 0;
+                        else if (r2 > sr_hi && r2 < lr_lo) cls = 2;
+                        else {
+                            const double e2 = exact_r2(d, R, p, j);
+                            cls = e2 <= R->r2sr ? 1 : ((ch && e2 <= R->r2lr) ? 2 : 0);
+                        }
+                    }
+                    if (cls == 1) {
+                        if (nsr < d.cap_sr) d.nbr_sr[(size_t)nsr * P + p] = j;
+                        ++nsr;
+                    } else if (cls == 2) {
+                        if (nlr < d.cap_lr) d.nbr_lr[(size_t)nlr * P + p] = j;
+                        ++nlr;
+                    }
+                }
+            }
+    if (nsr > d.cap_sr || nlr > d.cap_lr) atomicOr(&d.rs[r].err, kErrCapacity);
+    d.n_sr[p] = min(nsr, d.cap_sr);
+    d.n_lr[p] = min(nlr, d.cap_lr);
+}
+
+// hydrogen-bond candidate status and HB_EXCESS (E:1698-1736): a candidate is live
+// (0) when its central pair is in the SR list, i.e. within the SR radius.
+__global__ void k_hb_rebuild(Dev d)
+{
+    const int r = blockIdx.x;
+    RepState *S = d.rs + r;
+    if (!S->rebuild) return;
+    const RepParams *R = d.rp + r;
+    for (int a = R->hba0 + threadIdx.x; a < R->hba1; a += blockDim.x)
+        d.hb_excess[a] = d.hba_n[a] - d.hba_val[a];
+    __syncthreads();
+    for (int k = R->hb0 + threadIdx.x; k < R->hb1; k += blockDim.x) {
+        const int a = d.hb_idx[6 * k + 1], b = d.hb_idx[6 * k + 4];
+        const int st = (a != b && exact_r2(d, R, a, b) <= R->r2sr) ? 0 : -1;
+        d.hb_status[k] = st;
+        if (st != 0)
+            for (int u = d.hb_aoff[k]; u < d.hb_aoff[k + 1]; ++u) atomicSub(d.hb_excess + d.hb_aidx[u], 1);
+    }
+    __syncthreads();
+    // ordered compaction of the live candidates
+    __shared__ int s_warp[32];
+    __shared__ int s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nh = R->hb1 - R->hb0;
+    for (int base = 0; base < nh; base += blockDim.x) {
+        const int k = R->hb0 + base + threadIdx.x;
+        const bool live = (base + threadIdx.x < nh) && d.hb_status[k] == 0;
+        const unsigned m = __ballot_sync(kFull, live);
+        if (lane == 0) s_warp[w] = __popc(m);
+        __syncthreads();
+        int off = s_carry;
+        for (int t = 0; t < w; ++t) off += s_warp[t];
+        if (live) d.hb_active[R->hb0 + off + __popc(m & ((1u << lane) - 1u))] = k;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int t = 0; t < (int)(blockDim.x >> 5); ++t) tot += s_warp[t];
+            s_carry += tot;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        S->n_active = s_carry;
+        S->rebuild = 0;
+        S->rebuilds += 1;
+    }
+}
+
+// radius_of_gyration (E:2844-2876) of the RNA beads of one replica
+__global__ void k_rg(Dev d, int r, double *out)
+{
+    const RepParams *R = d.rp + r;
+    __shared__ double s_red[3 * 32];
+    double c[3] = {0, 0, 0};
+    for (int i = threadIdx.x; i < R->nrna; i += blockDim.x) {
+        c[0] += d.x[R->p0 + i];
+        c[1] += d.y[R->p0 + i];
+        c[2] += d.z[R->p0 + i];
+    }
+    block_sum<3>(c, s_red);
+    __shared__ double s_c[3];
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; ++k) s_c[k] = c[k] / R->nrna;
+    __syncthreads();
+    double s[1] = {0};
+    for (int i = threadIdx.x; i < R->nrna; i += blockDim.x) {
+        const double a = d.x[R->p0 + i] - s_c[0], b = d.y[R->p0 + i] - s_c[1], e = d.z[R->p0 + i] - s_c[2];
+        s[0] += a * a + b * b + e * e;
+    }
+    block_sum<1>(s, s_red);
+    if (threadIdx.x == 0) *out = sqrt(s[0] / R->nrna);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_quantize(const Dev &d, cudaStream_t s) { k_quantize<<<d.nblk, kBlock, 0, s>>>(d); }
+
+void launch_pair_sr(const Dev &d, cudaStream_t s, bool en)
+{
+    if (d.fp64) {
+        if (en) k_pair<true, false, true><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        else k_pair<true, false, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
+    } else {
+        if (en) k_pair<false, false, true><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        else k_pair<false, false, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
+    }
+}
+
+void launch_pair_lr(const Dev &d, cudaStream_t s, bool en, bool force_all)
+{
+    const int fa = force_all ? 1 : 0;
+    if (d.fp64) {
+        if (en) k_pair<true, true, true><<<d.nblk, kBlock, 0, s>>>(d, fa);
+        else k_pair<true, true, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
+    } else {
+        if (en) k_pair<false, true, true><<<d.nblk, kBlock, 0, s>>>(d, fa);
+        else k_pair<false, true, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
+    }
+}
+
+void launch_topology(const Dev &d, cudaStream_t s, int mask, bool en, bool make_noise)
+{
+    const int mn = make_noise ? 1 : 0;
+    if (d.fp64) {
+        if (en) k_topology<true, true><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn);
+        else k_topology<true, false><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn);
+    } else {
+        if (en) k_topology<false, true><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn);
+        else k_topology<false, false><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn);
+    }
+}
+
+void launch_noise(const Dev &d, cudaStream_t s)
+{
+    if (d.fp64) k_noise<true><<<d.R, kTopoThreads, 0, s>>>(d);
+    else k_noise<false><<<d.R, kTopoThreads, 0, s>>>(d);
+}
+
+void launch_integrate(const Dev &d, cudaStream_t s)
+{
+    if (d.fp64) k_integrate<true><<<d.nblk, kBlock, 0, s>>>(d);
+    else k_integrate<false><<<d.nblk, kBlock, 0, s>>>(d);
+}
+
+void launch_control(const Dev &d, cudaStream_t s) { k_control<<<d.R, 128, 0, s>>>(d); }
+
+void launch_rebuild(const Dev &d, cudaStream_t s)
+{
+    k_cell_assign<<<d.nblk, kBlock, 0, s>>>(d);
+    k_cell_scan<<<d.R, 256, 0, s>>>(d);
+    k_cell_fill<<<d.nblk, kBlock, 0, s>>>(d);
+    k_cell_sort<<<(d.C + 127) / 128, 128, 0, s>>>(d);
+    if (d.fp64) k_pair_search<true><<<d.nblk, kBlock, 0, s>>>(d);
+    else k_pair_search<false><<<d.nblk, kBlock, 0, s>>>(d);
+    k_hb_rebuild<<<d.R, 256, 0, s>>>(d);
+}
+
+void launch_force_all_rebuild(const Dev &d, cudaStream_t s) { k_force_rebuild<<<d.R, 128, 0, s>>>(d); }
+
+void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out) { k_rg<<<1, 256, 0, s>>>(d, replica, out); }
+
+// pair SR, pair LR, topology, integrate, control, 6 rebuild kernels
+int kernel_launches_per_step() { return 11; }
+
+}  // namespace tis

@@ -1,0 +1,59 @@
+// Kernel interface of the TIS engine: device pointer bundle and launchers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "tis_device.cuh"
+
+namespace tis {
+
+// Device pointers of one handle (all replicas packed; see tis_engine.cu).
+struct Dev {
+    int R, P, nblk, C;          // replicas, padded particles, particle blocks, cells
+    int fp64;                   // 1: FP64 mode
+    int noise;                  // tis_noise
+    const RepParams *rp;
+    RepState *rs;
+    const int *blk_rep;         // replica of every particle block
+    const int *rep_of;          // replica of every particle (padded slots included)
+    double *x, *y, *z, *xo, *yo, *zo, *vx, *vy, *vz;
+    int4 *q;                    // fixed-point position + (type | kind << 8 | active << 16)
+    unsigned long long *f, *flr;  // 3P each: int64 fixed point (mixed) or double (FP64)
+    float *gnoise;              // R x kNoise
+    // cells
+    int *cell_of, *cell_count, *cell_start, *cell_fill, *cell_list;
+    // neighbour lists, column-major: nbr[k * P + p]
+    int *nbr_sr, *n_sr, *nbr_lr, *n_lr;
+    int cap_sr, cap_lr;
+    // topology (global particle indices)
+    const int4 *bt_idx;         // a, b, c, kind
+    const double2 *bt_par;      // k0, x0
+    const int *st3_idx; const double *st3_nat, *st3_E; const int *st3_off;
+    const int *st2_idx; const double *st2_r0, *st2_E;
+    int *st2_off_flag;
+    double *st_energy;          // tertiary energies of the last step (for the Contacts file)
+    const int *hb_idx; const double *hb_nat, *hb_E; const int *hb_dode;
+    const int *hb_aoff, *hb_aidx;   // atoms of every candidate (CSR, global ids)
+    const int *hba_val, *hba_coff, *hba_cidx, *hba_n;
+    const int *ca_list;             // atoms whose candidate count exceeds their valence
+    int *hb_status, *hb_excess, *excess, *hb_active, *hb_K, *hb_A;
+    double *hb_energy;
+    int *hb_code;               // imaging branch of the three native dihedrals
+    double *eterm;              // R x kNE (per-term energies, compute_forces only)
+    double *shift;              // R x 3, recentring shift of the current step (adjust_box)
+    const int *cell_rep;        // replica of every cell
+};
+
+// Launchers (stream-ordered; gated per replica on device flags where noted).
+void launch_quantize(const Dev &d, cudaStream_t s);
+void launch_pair_sr(const Dev &d, cudaStream_t s, bool energies);
+void launch_pair_lr(const Dev &d, cudaStream_t s, bool energies, bool force_all);
+void launch_topology(const Dev &d, cudaStream_t s, int mask, bool energies, bool make_noise);
+void launch_noise(const Dev &d, cudaStream_t s);  // Gaussians + recentring shift only
+void launch_integrate(const Dev &d, cudaStream_t s);
+void launch_control(const Dev &d, cudaStream_t s);
+void launch_rebuild(const Dev &d, cudaStream_t s);  // gated on RepState::rebuild
+void launch_force_all_rebuild(const Dev &d, cudaStream_t s);
+void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out);
+int kernel_launches_per_step();
+
+}  // namespace tis

@@ -1,0 +1,323 @@
+"""ctypes binding of the C ABI in include/tis_gpu.h (libtis_gpu.so).
+
+The product path is the CUDA library; nothing here computes physics.  Loading
+fails loudly when the library is missing."""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+F64, I32, I64 = 0, 1, 2
+_NP = {F64: np.float64, I32: np.int32, I64: np.int64}
+STATE_NAMES = ["x", "y", "z", "ox", "oy", "oz", "vx", "vy", "vz"]
+ENERGY_NAMES = ["E_lj", "E_coul_sr", "E_coul_lr", "E_bond", "E_angle", "E_excl",
+                "E2_STACK", "E3_STACK", "E2_HB", "E3_HB", "Rg"]
+TERM_SR, TERM_LR, TERM_BONDED, TERM_STACK, TERM_HB = 1, 2, 4, 8, 16
+PREC_MIXED, PREC_FP64 = 0, 1
+NOISE_REFERENCE, NOISE_OFF = 0, 1
+
+
+class TisError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"tis error {code}: {msg}")
+        self.code = code
+
+
+class LoadParams(C.Structure):
+    _fields_ = [("pdb", C.c_char_p), ("bonds", C.c_char_p), ("stacks", C.c_char_p), ("maxikey", C.c_char_p),
+                ("T", C.c_double), ("ss_D", C.c_double), ("hs_D", C.c_double), ("st_D", C.c_double),
+                ("seed", C.c_int32), ("box", C.c_double), ("rc", C.c_double), ("c_mg", C.c_double),
+                ("c_k", C.c_double), ("n_mg", C.c_int32), ("n_cl", C.c_int32), ("n_k", C.c_int32),
+                ("center", C.c_int32), ("rng", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class RunParams(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("noise", C.c_int32), ("sr", C.c_double), ("skin", C.c_double),
+                ("lr_interval", C.c_int32), ("cap_sr", C.c_int32), ("cap_lr", C.c_int32), ("device", C.c_int32),
+                ("use_graph", C.c_int32), ("graph_steps", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
+_lib = None
+
+
+def lib(build_if_missing=True):
+    """The loaded libtis_gpu.so (built in-tree on first use)."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if build_if_missing:
+            _build.build()  # no-op when the library is newer than its sources
+        if not os.path.exists(path):
+            raise OSError(f"{path} is missing; run the build first")
+        _lib = C.CDLL(path)
+        _declare(_lib)
+    return _lib
+
+
+def _declare(L):
+    vp, i32, i64, dp, ip, cp = C.c_void_p, C.c_int, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_char_p
+    sig = {
+        "tis_last_error": [cp, C.c_size_t],
+        "tis_load_params_default": [C.POINTER(LoadParams)],
+        "tis_system_load": [C.POINTER(LoadParams), C.POINTER(vp)],
+        "tis_system_new": [C.POINTER(vp)],
+        "tis_system_set": [vp, cp, i32, vp, i64],
+        "tis_system_get": [vp, cp, C.POINTER(C.c_int), C.POINTER(vp), C.POINTER(C.c_int64)],
+        "tis_system_count": [vp, C.POINTER(C.c_int)],
+        "tis_system_name": [vp, i32, C.POINTER(C.c_char_p)],
+        "tis_system_destroy": [vp],
+        "tis_run_params_default": [C.POINTER(RunParams)],
+        "tis_create": [C.POINTER(vp), i32, C.POINTER(RunParams), C.POINTER(vp)],
+        "tis_destroy": [vp],
+        "tis_set_state": [vp, i32] + [dp] * 9,
+        "tis_get_state": [vp, i32] + [dp] * 9,
+        "tis_populate_lists": [vp],
+        "tis_get_cells": [vp, i32, ip, ip],
+        "tis_get_pairs": [vp, i32, i32, ip, i64, C.POINTER(C.c_int64)],
+        "tis_get_hb_status": [vp, i32, ip, ip],
+        "tis_compute_forces": [vp, i32, i32, dp, dp],
+        "tis_deterministic_forces": [vp],
+        "tis_full_forces": [vp],
+        "tis_move_rigid_units": [vp],
+        "tis_check_shifts": [vp],
+        "tis_step": [vp, i64],
+        "tis_sync": [vp],
+        "tis_get_energies": [vp, i32, dp],
+        "tis_get_stack_energies": [vp, i32, dp, i64, C.POINTER(C.c_int64)],
+        "tis_get_counters": [vp, i32, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+        "tis_get_info": [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(vp)],
+        "tis_replica_size": [vp, i32, C.POINTER(C.c_int)],
+        "tis_get_launch_count": [vp, C.POINTER(C.c_int64)],
+        "tis_rand_stream": [C.c_uint64, C.c_uint64, i64, ip],
+        "tis_profile_stages": [vp, i64, dp],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+
+
+EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis_system_new", "tis_system_set",
+            "tis_system_get", "tis_system_count", "tis_system_name", "tis_system_destroy", "tis_run_params_default",
+            "tis_create", "tis_destroy", "tis_set_state", "tis_get_state", "tis_populate_lists", "tis_get_cells",
+            "tis_get_pairs", "tis_get_hb_status", "tis_compute_forces", "tis_deterministic_forces", "tis_full_forces",
+            "tis_move_rigid_units", "tis_check_shifts", "tis_step", "tis_sync", "tis_get_energies",
+            "tis_get_stack_energies", "tis_get_counters", "tis_get_info", "tis_replica_size", "tis_get_launch_count",
+            "tis_rand_stream", "tis_profile_stages"]
+
+
+def rand_stream(seed, first, n):
+    """Draws of the Philox rand() stream (values in [1, 2^31-1])."""
+    out = np.zeros(max(n, 1), dtype=np.int32)
+    _check(lib().tis_rand_stream(seed, first, n, _ip(out)))
+    return out[:n]
+
+
+def _check(rc):
+    if rc != 0:
+        buf = C.create_string_buffer(1024)
+        lib().tis_last_error(buf, 1024)
+        raise TisError(rc, buf.value.decode(errors="replace"))
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class System:
+    """One replica's topology and state (a tis_system)."""
+
+    def __init__(self, handle):
+        self.h = C.c_void_p(handle)
+
+    @classmethod
+    def load(cls, pdb, bonds, stacks, maxikey, **kw):
+        p = LoadParams()
+        lib().tis_load_params_default(C.byref(p))
+        p.pdb, p.bonds, p.stacks, p.maxikey = (os.fsencode(v) for v in (pdb, bonds, stacks, maxikey))
+        for k, v in kw.items():
+            setattr(p, k, v)
+        out = C.c_void_p()
+        _check(lib().tis_system_load(C.byref(p), C.byref(out)))
+        return cls(out.value)
+
+    @classmethod
+    def from_arrays(cls, arrays):
+        out = C.c_void_p()
+        _check(lib().tis_system_new(C.byref(out)))
+        s = cls(out.value)
+        for k, v in arrays.items():
+            s[k] = v
+        return s
+
+    def __setitem__(self, name, arr):
+        arr = np.ascontiguousarray(arr)
+        if arr.dtype == np.float64:
+            dt = F64
+        elif arr.dtype == np.int32:
+            dt = I32
+        elif arr.dtype == np.int64:
+            dt = I64
+        else:
+            raise TypeError(f"{name}: dtype {arr.dtype} not supported")
+        _check(lib().tis_system_set(self.h, name.encode(), dt, arr.ctypes.data_as(C.c_void_p), arr.size))
+
+    def __getitem__(self, name):
+        dt, ptr, n = C.c_int(), C.c_void_p(), C.c_int64()
+        _check(lib().tis_system_get(self.h, name.encode(), C.byref(dt), C.byref(ptr), C.byref(n)))
+        npdt = _NP[dt.value]
+        if n.value == 0:
+            return np.zeros(0, dtype=npdt)
+        buf = (C.c_char * (n.value * np.dtype(npdt).itemsize)).from_address(ptr.value)
+        return np.frombuffer(buf, dtype=npdt).copy()
+
+    def names(self):
+        n = C.c_int()
+        _check(lib().tis_system_count(self.h, C.byref(n)))
+        out = []
+        for i in range(n.value):
+            nm = C.c_char_p()
+            _check(lib().tis_system_name(self.h, i, C.byref(nm)))
+            out.append(nm.value.decode())
+        return out
+
+    def to_dict(self):
+        return {k: self[k] for k in self.names()}
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().tis_system_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def run_params(**kw):
+    p = RunParams()
+    lib().tis_run_params_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Engine:
+    """A batch of replicas advanced together on one GPU (a tis_handle)."""
+
+    def __init__(self, systems, **params):
+        self.systems = list(systems)
+        arr = (C.c_void_p * len(self.systems))(*[s.h.value for s in self.systems])
+        self.params = run_params(**params)
+        out = C.c_void_p()
+        _check(lib().tis_create(arr, len(self.systems), C.byref(self.params), C.byref(out)))
+        self.h = out
+        self.n = []
+        for r in range(len(self.systems)):
+            n = C.c_int()
+            _check(lib().tis_replica_size(self.h, r, C.byref(n)))
+            self.n.append(n.value)
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().tis_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, r, st):
+        arrs = [np.ascontiguousarray(st[k], dtype=np.float64) for k in STATE_NAMES]
+        _check(lib().tis_set_state(self.h, r, *[_dp(a) for a in arrs]))
+
+    def get_state(self, r):
+        arrs = [np.zeros(self.n[r]) for _ in STATE_NAMES]
+        _check(lib().tis_get_state(self.h, r, *[_dp(a) for a in arrs]))
+        return dict(zip(STATE_NAMES, arrs))
+
+    def populate_lists(self):
+        _check(lib().tis_populate_lists(self.h))
+
+    def cells(self, r):
+        c = np.zeros(self.n[r], dtype=np.int32)
+        dims = np.zeros(3, dtype=np.int32)
+        _check(lib().tis_get_cells(self.h, r, _ip(c), _ip(dims)))
+        return c, dims
+
+    def pairs(self, r, which):
+        n = C.c_int64()
+        _check(lib().tis_get_pairs(self.h, r, which, None, 0, C.byref(n)))
+        out = np.zeros(max(n.value, 2), dtype=np.int32)
+        _check(lib().tis_get_pairs(self.h, r, which, _ip(out), out.size, C.byref(n)))
+        return out[: n.value].reshape(-1, 2)
+
+    def hb_status(self, r, n_hb, n_hba):
+        st = np.zeros(max(n_hb, 1), dtype=np.int32)
+        ex = np.zeros(max(n_hba, 1), dtype=np.int32)
+        _check(lib().tis_get_hb_status(self.h, r, _ip(st), _ip(ex)))
+        return st[:n_hb], ex[:n_hba]
+
+    def forces(self, r, mask):
+        f = np.zeros(3 * self.n[r])
+        e = np.zeros(len(ENERGY_NAMES))
+        _check(lib().tis_compute_forces(self.h, r, mask, _dp(f), _dp(e)))
+        return f, dict(zip(ENERGY_NAMES, e))
+
+    def step(self, n):
+        _check(lib().tis_step(self.h, n))
+
+    def sync(self):
+        _check(lib().tis_sync(self.h))
+
+    def deterministic_forces(self):
+        _check(lib().tis_deterministic_forces(self.h))
+
+    def full_forces(self):
+        _check(lib().tis_full_forces(self.h))
+
+    def move_rigid_units(self):
+        _check(lib().tis_move_rigid_units(self.h))
+
+    def check_shifts(self):
+        _check(lib().tis_check_shifts(self.h))
+
+    def energies(self, r):
+        e = np.zeros(5)
+        _check(lib().tis_get_energies(self.h, r, _dp(e)))
+        return e
+
+    def stack_energies(self, r):
+        n = C.c_int64()
+        _check(lib().tis_get_stack_energies(self.h, r, None, 0, C.byref(n)))
+        out = np.zeros(max(n.value, 1))
+        _check(lib().tis_get_stack_energies(self.h, r, _dp(out), n.value, C.byref(n)))
+        return out[: n.value]
+
+    def counters(self, r):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().tis_get_counters(self.h, r, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def profile_stages(self, n):
+        """Mean ms per step of: pair_sr, pair_lr, topology, integrate, control, rebuild."""
+        ms = np.zeros(6)
+        _check(lib().tis_profile_stages(self.h, n, _dp(ms)))
+        return dict(zip(["pair_sr", "pair_lr", "topology", "integrate", "control", "rebuild"], ms))
+
+    def launches(self):
+        n = C.c_int64()
+        _check(lib().tis_get_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(lib().tis_get_info(self.h, None, None, C.byref(s)))
+        return s.value

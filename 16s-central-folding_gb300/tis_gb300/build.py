@@ -1,0 +1,44 @@
+"""Builds libtis_gpu.so in-tree (16s-central-folding_gb300/_build/) with nvcc for sm_103a."""
+import os
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(PKG, "csrc")
+OUT = os.path.join(PKG, "_build")
+LIB = os.path.join(OUT, "libtis_gpu.so")
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = ["tis_kernels.cu", "tis_engine.cu", "tis_system.cpp", "tis_loader.cpp"]
+
+
+def _flags():
+    return ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-ffp-contract=off",
+            "-I", os.path.join(PKG, "..", "include")]
+
+
+def _compile(src):
+    obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
+    inp = os.path.join(CSRC, src)
+    lang = ["-x", "cu"] if src.endswith(".cu") else ["-x", "c++"]
+    cmd = [NVCC, *_flags(), *lang, "-c", inp, "-o", obj]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return obj
+
+
+def build(verbose=False, force=False):
+    os.makedirs(OUT, exist_ok=True)
+    srcs = [os.path.join(CSRC, s) for s in SOURCES] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    srcs.append(os.path.join(PKG, "..", "include", "tis_gpu.h"))
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > max(os.path.getmtime(s) for s in srcs):
+        return LIB
+    try:
+        with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+            objs = list(ex.map(_compile, SOURCES))
+        cmd = [NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+    except subprocess.CalledProcessError as e:
+        raise RuntimeError(f"building libtis_gpu.so failed:\n{' '.join(e.cmd)}\n{e.stdout}\n{e.stderr}") from None
+    if verbose:
+        print("built", LIB)
+    return LIB

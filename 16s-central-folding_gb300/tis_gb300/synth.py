@@ -188,7 +188,6 @@ def generate(out_dir, name, n_nt, seed, n_hb_pairs, n_tertiary=None, density=400
                 x, y, z = pos[bid]
                 f.write(f"ATOM {serial:6d} {an:<4s} {seq[t]:>3s} A {rn:5d}    {x:.3f} {y:.3f} {z:.3f}  1.00  0.00 {el}\n")
                 serial += 1
-        f.write("END\n")
 
     B = np.asarray([pos[ids[t][2]] for t in range(n_nt)])
     comp = set(_PAIR_ATOMS.keys())
@@ -198,10 +197,11 @@ def generate(out_dir, name, n_nt, seed, n_hb_pairs, n_tertiary=None, density=400
 
     bonds = os.path.join(out_dir, f"{name}_bonds.dat")
     pairs = _pick_close_pairs(rng, B, hb_ok, n_hb_pairs) if n_hb_pairs > 0 else []
-    with open(bonds, "w") as f:
-        for i, j in pairs:
-            atoms = _PAIR_ATOMS[(seq[i], seq[j])]
-            f.write(f"CAN11 {resnum(i + 1)} {resnum(j + 1)} {' '.join(atoms)} TER\n")
+    lines = [f"CAN11 {resnum(i + 1)} {resnum(j + 1)} {' '.join(_PAIR_ATOMS[(seq[i], seq[j])])} TER" for i, j in pairs]
+    if not lines:
+        raise ValueError("the reference's bonds reader needs at least one record")
+    with open(bonds, "w") as f:  # no newline after the last TER: the reference's reader loops on feof()
+        f.write("\n".join(lines))
 
     if n_tertiary is None:
         n_tertiary = max(1, n_nt // 8)

@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Throughput benchmark: aggregate Langevin steps/s of batched replicas.
+
+Workload (the batched configuration of the benchmark description): 64 replicas of
+a seeded 346-nt synthetic TIS chain (1037 beads) in a 350 A box, Mg2+ swept
+0..20 mM in 64 linear steps at 76 mM KCl (ion numbers by the reference's rule,
+4.6k-6.2k particles per replica), T = 298 K (0.59219 kcal/mol), h = 0.05,
+Coulomb cutoff 30 A, SR list radius 12+3 A, LR refresh every 10 steps,
+independent seeds.  Mixed precision (FP32 pair/bonded math, int64 fixed-point
+forces, FP64 integration), all replicas advanced together by one CUDA graph.
+
+A "step" advances every replica by one Langevin step; value = replica-steps/s
+over all GPUs.  Inputs (the systems) are synthetic and generated here.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+--impl reference times the reference's own CPU engine (oracle/_ref/tis_ref, built
+from the reference sources; else the C oracle port) on the host cores, one
+replica per core, on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "16s-central-folding_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+N_REPLICAS = 64
+N_NT = 346
+BOX = 350.0
+RC = 30.0
+T_298 = 0.59219
+GEN_SEED = 2000
+METRIC = "aggregate Langevin steps/s, batched mixed-prec vs plain GPU, force rel-err <=1e-5"
+UNIT = "replica-steps/s"
+GRAPH_STEPS = 20
+
+
+def replica_specs(n=N_REPLICAS):
+    from tis_gb300 import synth
+    ions = synth.batch_mg_sweep(n_replicas=n, mg_max_mm=20.0, kcl_mm=76.0, box=BOX, n_nt=N_NT)
+    return [dict(n_mg=m, n_cl=c, n_k=k, seed=1000 + r) for r, (m, c, k) in enumerate(ions)]
+
+
+def make_inputs(tmp):
+    from tis_gb300 import synth
+    return synth.generate(tmp, "central", N_NT, seed=GEN_SEED, n_hb_pairs=120)
+
+
+def load_systems(files, specs):
+    from tis_gb300 import System
+
+    def one(sp):
+        return System.load(files["pdb"], files["bonds"], files["stacks"], files["maxikey"], T=T_298, box=BOX, rc=RC,
+                           center=500, rng=1, **sp)
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        return list(ex.map(one, specs))
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.rows, self.proc, self.device = [], None, device
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([v.strip() for v in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        import statistics
+        sm = [float(r[0]) for r in self.rows if len(r) >= 8 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 8 and r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 8:
+                for n, v in zip(names, r[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# algorithmic bytes per particle-step of each stage (FP64 state, int64 fixed-point forces)
+#   integrator: read x, x_old, v (72 B) + SR and LR force accumulators (48 B) + code (16 B,
+#   the packed position it also rewrites), write x, x_old, v (72 B) + packed position (16 B)
+ALG_BYTES = {"integrate": 72 + 48 + 16 + 72 + 16,
+             #   SR pair stage: packed positions of the particle (16 B) + write of its force (24 B)
+             "pair_sr": 16 + 24}
+
+
+def cpu_sample(files, specs, steps, workers):
+    """Reference CPU engine on `workers` replicas in parallel, `steps` steps each."""
+    import build_ref
+    exe = build_ref.build()
+    kind = "reference" if exe else "port"
+    sample = specs[:: max(1, len(specs) // workers)][:workers]
+
+    def run_ref(sp):
+        args = [exe, "--pdb", files["pdb"], "--bonds", files["bonds"], "--stacks", files["stacks"],
+                "--maxikey", files["maxikey"], "--box", str(BOX), "--rc", str(RC), "--T", str(T_298),
+                "--nMg", str(sp["n_mg"]), "--nCl", str(sp["n_cl"]), "--nK", str(sp["n_k"]),
+                "--seed", str(sp["seed"]), "--center", "500", "--rng", "philox", "--steps", str(steps), "--time"]
+        out = subprocess.run(args, check=True, capture_output=True, text=True).stdout
+        return json.loads(out.strip().splitlines()[-1])["seconds"]
+
+    def run_port(sp):
+        from oracle_bridge import Oracle
+        from tis_gb300 import System
+        s = System.load(files["pdb"], files["bonds"], files["stacks"], files["maxikey"], T=T_298, box=BOX, rc=RC,
+                        center=500, rng=1, **sp)
+        o = Oracle(s.to_dict(), seed=sp["seed"])
+        o.populate_lists()
+        t0 = time.perf_counter()
+        o.step(steps)
+        return time.perf_counter() - t0
+
+    fn = run_ref if kind == "reference" else run_port
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        secs = list(ex.map(fn, sample))
+    value = len(sample) * steps / max(secs)
+    return {"value": value, "unit": UNIT, "cores": len(sample), "kind": kind,
+            "sample": f"{len(sample)} of the {len(specs)} replicas ({steps} steps each, one per host core, "
+                      f"concurrently; setup excluded)"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as tmp:
+        files = make_inputs(tmp)
+        specs = replica_specs()
+        workers = min(len(specs), os.cpu_count() or 1)
+        cpu = cpu_sample(files, specs, max(200, args.steps), workers)
+    cpu_line = dict(cpu)
+    line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * N_REPLICAS / cpu["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "64 replicas x 346-nt TIS chain + Mg 0-20 mM sweep, 76 mM KCl, 350 A box",
+                       "replicas": N_REPLICAS},
+            "cpu_baseline": cpu_line,
+            "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def gpu_arm(args):
+    import numpy as np
+    import torch
+
+    from tis_gb300 import PREC_FP64, PREC_MIXED, Engine
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    with tempfile.TemporaryDirectory() as tmp:
+        files = make_inputs(tmp)
+        specs = replica_specs()
+        # replicas only: every rank runs its own full batch of independent replicas
+        for sp in specs:
+            sp["seed"] += 100000 * rank
+        systems = load_systems(files, specs)
+        eng = Engine(systems, precision=PREC_MIXED, device=local, use_graph=1, graph_steps=GRAPH_STEPS)
+        eng.populate_lists()
+        stream = torch.cuda.ExternalStream(eng.stream())
+        flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+        K = max(1, args.steps)
+        W = max(3, args.warmup)
+        eng.step(W)                # W warm-up steps (direct launches) ...
+        eng.step(GRAPH_STEPS)      # ... and one graph replay, so capture happens before timing
+        eng.sync()
+        chunks = [GRAPH_STEPS] * (K // GRAPH_STEPS) + ([K % GRAPH_STEPS] if K % GRAPH_STEPS else [])
+        iters = len(chunks)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(iters)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            for i in range(iters):
+                with torch.cuda.stream(stream):
+                    flush.zero_()  # L2 flush between timed iterations (256 MB > 129 MB L2)
+                    ev[i][0].record(stream)
+                eng.step(chunks[i])
+                with torch.cuda.stream(stream):
+                    ev[i][1].record(stream)
+            eng.sync()
+            torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        if world > 1:
+            t = torch.tensor([ms], device=f"cuda:{local}")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+            torch.distributed.barrier()
+        ms_per_step = ms / K
+        value = world * N_REPLICAS * K / (ms / 1000.0)
+        launches = K * 11
+
+        # end to end through the C ABI with host buffers: every 100 steps a state
+        # upload from pinned host memory and a frame (positions + energies) read back
+        e2e = None
+        if rank == 0:
+            E2E_STEPS = 100
+            n_it = max(1, min(10, K // E2E_STEPS))
+            states = [eng.get_state(r) for r in range(N_REPLICAS)]
+            pinned = []
+            for st in states:
+                pinned.append({k: torch.from_numpy(v).pin_memory().numpy() for k, v in st.items()})
+            h2d = sum(v.nbytes for st in pinned for v in st.values())
+            t0 = time.perf_counter()
+            d2h = 0
+            for _ in range(n_it):
+                for r in range(N_REPLICAS):
+                    eng.set_state(r, pinned[r])
+                eng.populate_lists()
+                eng.step(E2E_STEPS)
+                for r in range(N_REPLICAS):
+                    st = eng.get_state(r)
+                    en = eng.energies(r)
+                    d2h += 3 * st["x"].nbytes + en.nbytes
+            eng.sync()
+            dt = time.perf_counter() - t0
+            e2e = {"value": N_REPLICAS * E2E_STEPS * n_it / dt, "unit": UNIT,
+                   "h2d_bytes_per_step": h2d // E2E_STEPS, "d2h_bytes_per_step": d2h // (E2E_STEPS * n_it),
+                   "frame_every_steps": E2E_STEPS}
+
+        # per-stage device time (CUDA events between the stage launches)
+        stages = eng.profile_stages(50)
+        dom = max(stages, key=stages.get)
+        peak, peak_kind = measured_peaks()
+        n_part = sum(eng.n)
+        alg = ALG_BYTES.get(dom)
+        roofline = None
+        if alg is not None:
+            achieved = alg * n_part / (stages[dom] * 1e-3) / 1e9
+            roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                        "alg_bytes_per_launch": alg * n_part}
+        else:
+            roofline = {"bound": "hbm", "kernel": dom, "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
+                        "peak_source": peak_kind, "traffic": None}
+
+        # the plain single-replica FP64 GPU path (the denominator of the batching target)
+        plain = Engine([systems[len(systems) // 2]], precision=PREC_FP64, device=local, use_graph=0)
+        plain.populate_lists()
+        plain.step(50)
+        plain.sync()
+        t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pstream = torch.cuda.ExternalStream(plain.stream())
+        NP = 500
+        with torch.cuda.stream(pstream):
+            t0e.record(pstream)
+        plain.step(NP)
+        with torch.cuda.stream(pstream):
+            t1e.record(pstream)
+        plain.sync()
+        torch.cuda.synchronize()
+        plain_sps = NP / (t0e.elapsed_time(t1e) / 1000.0)
+
+    if rank != 0:
+        return
+    cpu = cpu_sample(files_for_cpu(), replica_specs(), 2000, min(N_REPLICAS, os.cpu_count() or 1)) \
+        if args.cpu_baseline else None
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+i64+f64", "data": "synthetic",
+            "config": {"workload": "64 replicas x 346-nt TIS chain (1037 beads) + Mg 0-20 mM sweep, 76 mM KCl, "
+                                   "350 A box, T 298 K, rc 30 A",
+                       "replicas_per_gpu": N_REPLICAS, "particles_per_gpu": n_part, "precision": "mixed",
+                       "graph_steps": GRAPH_STEPS, "l2": "flushed (256 MB write) between timed iterations of "
+                                                         f"{GRAPH_STEPS} steps", "parallelism": f"replicas x{world}"},
+            "plain_fp64_single_replica_steps_per_s": plain_sps,
+            "batched_vs_plain": value / world / plain_sps,
+            "stage_ms_per_step": stages,
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def files_for_cpu():
+    d = tempfile.mkdtemp()
+    return make_inputs(d)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

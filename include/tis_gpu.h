@@ -1,0 +1,208 @@
+/* tis_gpu.h — C ABI of the GB300 (sm_103a) TIS-RNA Langevin engine.
+ *
+ * The reference (naotohori/16S-central-folding, src/16SCD_Mg_Cl_K_COPY_fast.cpp,
+ * cited as E:) has no library interface: its hot path is the call sequence
+ *     populate_lists();                                   E:6237 (and from check_shifts)
+ *     for (klok ...) { deterministic_forces_MPI();        E:6380  (E:2524-2586)
+ *                      full_forces();                     E:6382  (E:2590-2625)
+ *                      move_rigid_units();                E:6384  (E:2660-2732)
+ *                      check_shifts(); }                  E:6386  (E:1741-1776)
+ * acting on 1-based FP64 global arrays set up by read_maxi_key / read_PDB /
+ * initialize_* / set_box / add_crowder (E:6111-6179).  Each entry point below
+ * names the reference routine it replaces.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *   - Every function returns 0 (TIS_OK) or a positive TIS_ERR_* code; the text
+ *     of the last error of the calling thread is available from tis_last_error.
+ *   - Particle indices are 0-based (reference index minus one).
+ *   - A handle owns device memory for n_replicas independent replicas that are
+ *     advanced together; calls on one handle are serialised on its CUDA stream;
+ *     a handle is not thread-safe; distinct handles may be used concurrently.
+ *   - Host buffers passed in are copied; the library never retains them.
+ */
+#ifndef TIS_GPU_H
+#define TIS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TIS_ABI_VERSION 1
+
+enum tis_status {
+    TIS_OK = 0,
+    TIS_ERR_ARG = 1,        /* bad argument or missing system array */
+    TIS_ERR_IO = 2,         /* input file cannot be opened or read */
+    TIS_ERR_FORMAT = 3,     /* input file content not understood */
+    TIS_ERR_CUDA = 4,       /* CUDA runtime error (no device, launch failure ...) */
+    TIS_ERR_CAPACITY = 5,   /* a neighbour list overflowed its per-particle capacity */
+    TIS_ERR_NONFINITE = 6,  /* non-finite force, position or velocity */
+    TIS_ERR_RANGE = 7,      /* a particle left the range the cell grid covers */
+    TIS_ERR_STATE = 8,      /* call out of order (e.g. forces before lists) */
+    TIS_ERR_NOMEM = 9,      /* host or device allocation failed */
+    TIS_ERR_SETUP = 10      /* ion placement did not converge */
+};
+
+/* array element types of tis_system arrays */
+enum tis_dtype { TIS_F64 = 0, TIS_I32 = 1, TIS_I64 = 2 };
+
+/* Text of the last error raised on the calling thread (empty if none). */
+int tis_last_error(char *buf, size_t n);
+
+/* ------------------------------------------------------------------------ */
+/* Systems: host-side topology + initial state of one replica.               */
+/* ------------------------------------------------------------------------ */
+typedef struct tis_system tis_system;
+
+typedef struct tis_load_params {
+    const char *pdb;          /* coordinates (read_PDB, E:3137) */
+    const char *bonds;        /* hydrogen-bond candidates (initialize_unprocessed_bonds, E:3733) */
+    const char *stacks;       /* tertiary stacks (initialize_unprocessed_stacks, E:4232) */
+    const char *maxikey;      /* 9-type parameter table (read_maxi_key, E:2883) */
+    double T;                 /* -T, temperature in kcal/mol (E:6090) */
+    double ss_D, hs_D, st_D;  /* -D -E -d force-field adjustments (E:6086-6089) */
+    int32_t seed;             /* -s; seeds srand(T*1000*seed) (E:6105) and the Philox stream */
+    double box;               /* cubic box side, A (E:6076: 350) */
+    double rc;                /* Coulomb cutoff, A (E:348: 50) */
+    double c_mg, c_k;         /* -c -f bulk concentrations, M (E:6092-6094) */
+    int32_t n_mg, n_cl, n_k;  /* explicit ion numbers; all < 0 selects the rule of E:6167-6171 */
+    int32_t center;           /* 1-based recentring bead (E:2670, E:4542: 500) */
+    int32_t rng;              /* 0: glibc rand() for set-up draws, 1: Philox stream */
+    int32_t reserved[7];
+} tis_load_params;
+
+/* Fills p with the reference's defaults (src/run_sample.sh and E:6076, E:348). */
+int tis_load_params_default(tis_load_params *p);
+
+/* Reads the four input files and runs the reference's set-up sequence
+ * (read_maxi_key, read_PDB, initialize_HB_atoms, initialize_unprocessed_bonds,
+ * initialize_unprocessed_stacks, set_box, add_crowder; E:6111-6179). */
+int tis_system_load(const tis_load_params *p, tis_system **out);
+
+/* An empty system to be filled array by array (names of the TISB system export). */
+int tis_system_new(tis_system **out);
+int tis_system_set(tis_system *s, const char *name, int dtype, const void *data, int64_t count);
+/* Borrowed view of an array; valid until the array is replaced or s destroyed. */
+int tis_system_get(const tis_system *s, const char *name, int *dtype, const void **data, int64_t *count);
+/* Number of arrays and the name of array i (for enumeration). */
+int tis_system_count(const tis_system *s, int *n);
+int tis_system_name(const tis_system *s, int i, const char **name);
+int tis_system_destroy(tis_system *s);
+
+/* ------------------------------------------------------------------------ */
+/* Engine                                                                    */
+/* ------------------------------------------------------------------------ */
+typedef struct tis_handle tis_handle;
+
+enum tis_precision {
+    TIS_PREC_MIXED = 0, /* FP32 pair/bonded math, int64 fixed-point forces, FP64 integration */
+    TIS_PREC_FP64 = 1   /* FP64 throughout (the plain GPU path) */
+};
+
+enum tis_noise { TIS_NOISE_REFERENCE = 0, TIS_NOISE_OFF = 1 };
+
+typedef struct tis_run_params {
+    int32_t precision;     /* tis_precision */
+    int32_t noise;         /* tis_noise: REFERENCE = 3000 shared Gaussians per step (E:2590-2625) */
+    double sr;             /* SR list radius minus skin (E:6229: 12) */
+    double skin;           /* Verlet skin dr1 (E:6227: 3) */
+    int32_t lr_interval;   /* LR Coulomb refresh period (E:2550: 10) */
+    int32_t cap_sr;        /* SR neighbours per particle (0: default) */
+    int32_t cap_lr;        /* LR neighbours per particle (0: default) */
+    int32_t device;        /* CUDA device ordinal */
+    int32_t use_graph;     /* 1: tis_step replays a captured CUDA graph */
+    int32_t graph_steps;   /* steps per captured graph (0: default) */
+    int32_t reserved[6];
+} tis_run_params;
+
+int tis_run_params_default(tis_run_params *p);
+
+/* Uploads n_replicas systems (each with its own size, ions, T and seed) and
+ * allocates the device state.  Replaces the reference's globals set-up. */
+int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_params *p, tis_handle **out);
+int tis_destroy(tis_handle *h);
+
+/* State of one replica: positions, previous positions (x_old) and velocities,
+ * FP64, length n each (the reference's x,y,z,x_old,..,vz, E:155-165). */
+int tis_set_state(tis_handle *h, int replica, const double *x, const double *y, const double *z,
+                  const double *xo, const double *yo, const double *zo,
+                  const double *vx, const double *vy, const double *vz);
+int tis_get_state(tis_handle *h, int replica, double *x, double *y, double *z,
+                  double *xo, double *yo, double *zo, double *vx, double *vy, double *vz);
+
+/* populate_lists (E:1546-1737) for every replica: cell binning, SR/LR neighbour
+ * lists, hydrogen-bond candidate status; resets PROGRESS (E:6238). */
+int tis_populate_lists(tis_handle *h);
+
+/* Cell of every particle (0-based linear index of E:1536) and the grid dims. */
+int tis_get_cells(tis_handle *h, int replica, int32_t *cell, int32_t *dims);
+/* Unordered pair set of list `which` (0: SR, 1: LR) as (i<j) pairs, 2 ints each;
+ * *n receives the number of ints; at most cap ints are written. */
+int tis_get_pairs(tis_handle *h, int replica, int which, int32_t *pairs, int64_t cap, int64_t *n);
+/* Hydrogen-bond candidate status (-1/0) and HB_EXCESS after the last list build. */
+int tis_get_hb_status(tis_handle *h, int replica, int32_t *status, int32_t *excess);
+
+/* Force terms, for per-term parity on the current state of one replica.
+ * term_mask bits: */
+enum tis_term {
+    TIS_TERM_SR = 1,      /* SR_interactions_lists  E:1783 (LJ + Coulomb inside 15 A) */
+    TIS_TERM_LR = 2,      /* LR_interactions_lists  E:1851 (Coulomb 15 A .. rc+3 A) */
+    TIS_TERM_BONDED = 4,  /* polymer_constraints    E:2354 (bonds, angles, LJ exclusions) */
+    TIS_TERM_STACK = 8,   /* stacking_interactions  E:1911 */
+    TIS_TERM_HB = 16      /* hydrogen_bonds_interactions E:2145 (consumes MC draws) */
+};
+/* energies[TIS_N_ENERGIES] (may be NULL) */
+enum tis_energy_index {
+    TIS_E_LJ = 0, TIS_E_COUL_SR, TIS_E_COUL_LR, TIS_E_BOND, TIS_E_ANGLE, TIS_E_EXCL,
+    TIS_E2_STACK, TIS_E3_STACK, TIS_E2_HB, TIS_E3_HB, TIS_E_RG, TIS_N_ENERGIES
+};
+/* Sum of the selected terms into forces[3n] (x,y,z interleaved, FP64). */
+int tis_compute_forces(tis_handle *h, int replica, int term_mask, double *forces, double *energies);
+
+/* One reference step per call of each, in the reference's order, for every
+ * replica (drop-in replacements of the four routines of the run loop). */
+int tis_deterministic_forces(tis_handle *h); /* deterministic_forces_MPI  E:2524 */
+int tis_full_forces(tis_handle *h);          /* full_forces               E:2590 */
+int tis_move_rigid_units(tis_handle *h);     /* move_rigid_units          E:2660 */
+int tis_check_shifts(tis_handle *h);         /* check_shifts              E:1741 */
+
+/* n steps of the whole sequence for every replica (CUDA-graph replay when
+ * use_graph is set); asynchronous: returns after enqueueing. */
+int tis_step(tis_handle *h, int64_t n);
+/* Waits for the handle's stream; reports device-side error flags. */
+int tis_sync(tis_handle *h);
+
+/* E2_HB, E3_HB, E2_STACK, E3_STACK of the last step and Rg of the RNA
+ * (the five columns of the Energies file, E:6312). */
+int tis_get_energies(tis_handle *h, int replica, double *out5);
+/* Energies of the tertiary stacks of the last step (the Contacts file, E:6290). */
+int tis_get_stack_energies(tis_handle *h, int replica, double *out, int64_t cap, int64_t *n);
+/* Step counter (klok), rebuild count and rand() draws consumed by one replica. */
+int tis_get_counters(tis_handle *h, int replica, int64_t *klok, int64_t *rebuilds, int64_t *draws);
+
+/* Number of replicas, particles of one replica, and the CUDA stream (cudaStream_t). */
+int tis_get_info(tis_handle *h, int *n_replicas, int *device, void **stream);
+int tis_replica_size(tis_handle *h, int replica, int *n_particles);
+
+/* Runs n steps with direct launches and CUDA events between the stages, on the
+ * handle's stream; ms[6] receives the mean duration per step of: SR pair forces,
+ * LR pair forces, topology terms (bonded/stacking/H-bond + noise), integrator,
+ * skin check, list rebuild (all six rebuild kernels). */
+int tis_profile_stages(tis_handle *h, int64_t n, double *ms);
+
+/* Kernel launches enqueued by tis_step since the handle was created. */
+int tis_get_launch_count(tis_handle *h, int64_t *n);
+
+/* Draws first .. first+n-1 of the rand() stream that replaces glibc rand() for
+ * a replica with this seed: Philox-4x32-10 (Salmon et al. 2011), values in
+ * [1, 2^31-1].  The hydrogen-bond Monte Carlo (E:2251-2300) and full_forces
+ * (E:2594-2606) consume it in the reference's order. */
+int tis_rand_stream(uint64_t seed, uint64_t first, int64_t n, int32_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

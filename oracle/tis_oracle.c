@@ -886,3 +886,11 @@ void tis_o_last_forces(const tis_o *o, double *f3n) { copy_f(o, o->fx, o->fy, o-
 uint64_t tis_o_draws(const tis_o *o) { return o->ctr; }
 int64_t tis_o_rebuilds(const tis_o *o) { return o->rebuilds; }
 int64_t tis_o_klok(const tis_o *o) { return o->klok; }
+
+/* one Philox-4x32-10 output word (for known-answer tests of the shared stream) */
+uint32_t tis_o_philox_word(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, int lane)
+{
+    uint32_t c[4] = { c0, c1, c2, c3 };
+    tis_o_philox4x32_10(c, k0, k1);
+    return c[lane & 3];
+}

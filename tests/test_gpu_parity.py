@@ -1,0 +1,189 @@
+"""GPU parity through the C ABI against the FP64 CPU oracle, on the same systems
+(loaded once by the product loader, whose output is pinned to the reference).
+
+Tolerances, stated per check:
+  * cell assignments, SR/LR pair sets, H-bond candidate status: bit-exact;
+  * per-term forces, mixed precision: ||F_gpu - F_oracle|| / ||F_oracle|| <= 1e-5
+    and max_i |F_gpu,i - F_oracle,i| <= 1e-5 * max_i |F_oracle,i|;
+  * per-term forces, FP64 mode: relative error <= 1e-10;
+  * energies: relative 1e-5 (mixed), 1e-10 (FP64).
+"""
+import numpy as np
+import pytest
+
+from oracle_bridge import Oracle
+from systems import CASES, golden_inputs, load, pair_set, rel_err
+from tis_gb300 import (PREC_FP64, PREC_MIXED, NOISE_OFF, NOISE_REFERENCE, TERM_BONDED, TERM_HB, TERM_LR, TERM_SR,
+                       TERM_STACK, Engine, TisError)
+
+pytestmark = pytest.mark.gpu
+
+TERMS = [("F_sr", TERM_SR), ("F_lr", TERM_LR), ("F_bonded", TERM_BONDED), ("F_stack", TERM_STACK), ("F_hb", TERM_HB)]
+E_TERM = {"F_sr": ["E_lj", "E_coul_sr"], "F_lr": ["E_coul_lr"], "F_bonded": ["E_bond", "E_angle", "E_excl"],
+          "F_stack": ["E2_STACK", "E3_STACK"], "F_hb": ["E2_HB", "E3_HB"]}
+PRECS = [("mixed", PREC_MIXED, 1e-5), ("fp64", PREC_FP64, 1e-10)]
+
+
+@pytest.fixture(scope="module")
+def systems(synth_dir):
+    return {"small": load(golden_inputs(), "small"), "central": load(synth_dir["central"], "central")}
+
+
+def _oracle(sysobj, noise=True, seed=3):
+    return Oracle(sysobj.to_dict(), seed=seed, noise=noise)
+
+
+@pytest.mark.parametrize("prec_name,prec,tol", PRECS)
+@pytest.mark.parametrize("case", ["small", "central"])
+def test_lists_bit_exact(systems, case, prec_name, prec, tol):
+    s = systems[case]
+    o = _oracle(s)
+    o.populate_lists()
+    e = Engine([s], precision=prec)
+    e.populate_lists()
+    c, dims = e.cells(0)
+    oc, od = o.cells()
+    assert np.array_equal(dims, od)
+    assert np.array_equal(c, oc)
+    for which in (0, 1):
+        assert np.array_equal(e.pairs(0, which), pair_set(o.pairs(which))), f"list {which}"
+    st, ex = e.hb_status(0, o.n_hb, o.n_hba)
+    ost, oex = o.hb()
+    assert np.array_equal(st, ost)
+    assert np.array_equal(ex, oex)
+
+
+@pytest.mark.parametrize("prec_name,prec,tol", PRECS)
+@pytest.mark.parametrize("case", ["small", "central"])
+def test_term_forces_and_energies(systems, case, prec_name, prec, tol):
+    s = systems[case]
+    o = _oracle(s)
+    o.populate_lists()
+    ref = o.terms()
+    for name, mask in TERMS:
+        e = Engine([s], precision=prec)  # fresh: the H-bond term consumes Monte Carlo draws
+        e.populate_lists()
+        f, en = e.forces(0, mask)
+        want = ref[name]
+        if np.linalg.norm(want) == 0:
+            assert np.abs(f).max() < 1e-12, name
+            continue
+        assert rel_err(f, want) <= tol, (name, rel_err(f, want))
+        assert np.abs(f - want).max() <= tol * np.abs(want).max(), name
+        for k in E_TERM[name]:
+            assert en[k] == pytest.approx(ref[k], rel=tol, abs=tol * max(1.0, abs(ref[k]))), (name, k)
+    e = Engine([s], precision=prec)
+    e.populate_lists()
+    f, en = e.forces(0, TERM_SR | TERM_LR | TERM_BONDED | TERM_STACK | TERM_HB)
+    total = sum(ref[n] for n, _ in TERMS)
+    assert rel_err(f, total) <= tol
+    assert en["Rg"] == pytest.approx(ref["Rg"], rel=1e-12)
+
+
+def _positions(st):
+    return np.stack([st["x"], st["y"], st["z"]], 1)
+
+
+@pytest.mark.parametrize("prec_name,prec,tol_pos", [("fp64", PREC_FP64, 1e-7), ("mixed", PREC_MIXED, 1e-3)])
+def test_noise_free_trajectory_tracks_oracle(systems, prec_name, prec, tol_pos):
+    """1000 noise-free steps of the small system (H-bond Monte Carlo on the shared
+    stream): max position deviation from the FP64 oracle stays below tol_pos A."""
+    s = systems["small"]
+    o = _oracle(s, noise=False)
+    o.populate_lists()
+    e = Engine([s], precision=prec, noise=NOISE_OFF)
+    e.populate_lists()
+    dev = []
+    for k in range(10):
+        o.step(100)
+        e.step(100)
+        e.sync()
+        d = np.abs(_positions(e.get_state(0)) - _positions(o.get_state())).max()
+        dev.append(d)
+    print(f"{prec_name} max |dx| every 100 steps:", " ".join(f"{d:.2e}" for d in dev))
+    assert max(dev) < tol_pos
+    assert e.counters(0)[2] == o.draws()
+
+
+@pytest.mark.parametrize("prec_name,prec,tol_pos", [("fp64", PREC_FP64, 1e-7), ("mixed", PREC_MIXED, 1e-3)])
+def test_stochastic_trajectory_tracks_oracle(systems, prec_name, prec, tol_pos):
+    """Langevin noise and Monte Carlo from the shared Philox stream: 200 steps."""
+    s = systems["small"]
+    o = _oracle(s, noise=True)
+    o.populate_lists()
+    e = Engine([s], precision=prec, noise=NOISE_REFERENCE)
+    e.populate_lists()
+    o.step(200)
+    e.step(200)
+    e.sync()
+    d = np.abs(_positions(e.get_state(0)) - _positions(o.get_state())).max()
+    print(f"{prec_name} stochastic 200 steps max |dx| = {d:.2e}")
+    assert d < tol_pos
+    assert e.counters(0)[2] == o.draws()
+    np.testing.assert_allclose(e.energies(0), o.last_energies(), rtol=1e-3 if prec == PREC_MIXED else 1e-8, atol=1e-3)
+
+
+def test_batch_equals_single_bitwise(synth_dir):
+    """Replicas with different ion numbers, temperatures and seeds advance in one
+    batch exactly as each does alone (fixed-point sums are order-independent)."""
+    f = synth_dir["small"]
+    specs = [dict(seed=3), dict(seed=5, n_mg=20, n_cl=281, n_k=317, T=0.62), dict(seed=9, n_mg=0, n_cl=241, n_k=317)]
+    sys_ = [load(f, "small", **sp) for sp in specs]
+    batch = Engine(sys_)
+    batch.populate_lists()
+    batch.step(300)
+    batch.sync()
+    for r, s in enumerate(sys_):
+        one = Engine([s])
+        one.populate_lists()
+        one.step(300)
+        one.sync()
+        a, b = batch.get_state(r), one.get_state(0)
+        for k in a:
+            assert np.array_equal(a[k], b[k]), (r, k)
+        assert batch.counters(r) == one.counters(0)
+
+
+def test_split_calls_and_graph_equal_fused_step(systems):
+    """The four drop-in calls (deterministic_forces, full_forces, move_rigid_units,
+    check_shifts), the fused step and the captured graph give identical states."""
+    s = systems["small"]
+    runs = []
+    for mode in ["split", "direct", "graph"]:
+        e = Engine([s], use_graph=1 if mode == "graph" else 0, graph_steps=20)
+        e.populate_lists()
+        if mode == "split":
+            for _ in range(100):
+                e.deterministic_forces()
+                e.full_forces()
+                e.move_rigid_units()
+                e.check_shifts()
+        else:
+            e.step(100)
+        e.sync()
+        runs.append(e.get_state(0))
+    for k in runs[0]:
+        assert np.array_equal(runs[0][k], runs[1][k]), k
+        assert np.array_equal(runs[1][k], runs[2][k]), k
+
+
+def test_nonfinite_state_is_reported(systems):
+    s = systems["small"]
+    e = Engine([s])
+    st = e.get_state(0)
+    st["vx"][5] = np.inf
+    e.set_state(0, st)
+    e.populate_lists()
+    e.step(2)
+    with pytest.raises(TisError) as err:
+        e.sync()
+    assert err.value.code == 6
+
+
+def test_small_capacity_grows_at_list_build(systems):
+    s = systems["central"]
+    e = Engine([s], cap_sr=8, cap_lr=8)
+    e.populate_lists()  # overflows, grows, rebuilds
+    o = _oracle(s)
+    o.populate_lists()
+    assert np.array_equal(e.pairs(0, 0), pair_set(o.pairs(0)))
