@@ -134,14 +134,15 @@ def grow_chain(seq, rng, r_conf, min_sep=3.6, tries=400):
         sid_prev = ids[-1][1]
         prev_bond = (s_prev - p_prev) if p_prev is not None else (s_prev - pos[ids[-1][2]])
         theta = _BETA2 if p_prev is not None else _ALPHA1[seq[t - 1]]
-        excl = {sid_prev, ids[-1][2]} | ({ids[-1][0]} if ids[-1][0] >= 0 else set())
-        p = place(s_prev, _R_SP, prev_bond, theta, excl)
+        # only the bonded origin is exempt from the overlap test: 1-3 partners must
+        # also stay apart, or the bond angle collapses onto its neighbour
+        p = place(s_prev, _R_SP, prev_bond, theta, {sid_prev})
         pid = len(pos)
         pos.append(p)
-        s = place(p, _R_PS, p - s_prev, _BETA1, {pid, sid_prev})
+        s = place(p, _R_PS, p - s_prev, _BETA1, {pid})
         sid = len(pos)
         pos.append(s)
-        bpos = place(s, _R_SB[b], s - p, _ALPHA2[b], {sid, pid})
+        bpos = place(s, _R_SB[b], s - p, _ALPHA2[b], {sid})
         pos.append(bpos)
         ids.append((pid, sid, sid + 1))
         s_prev, p_prev = s, p
