@@ -98,19 +98,21 @@ __device__ inline float exp_(float v) { return expf(v); }
 __device__ inline double exp_(double v) { return exp(v); }
 __device__ inline float sqrt_(float v) { return sqrtf(v); }
 __device__ inline double sqrt_(double v) { return sqrt(v); }
+__device__ inline float rsqrt_(float v) { return 1.0f / sqrtf(v); }
+__device__ inline double rsqrt_(double v) { return 1.0 / sqrt(v); }
 
 // ---------------------------------------------------------------------------
 // geometry and restraint forces (E:924-1454)
 // ---------------------------------------------------------------------------
-// valence_angle (E:986-1027): angle at i2
+// valence_angle (E:986-1027): the angle at i2, as atan2(|a x b|, a.b), which
+// equals the reference's acos(a.b / |a||b|) and stays accurate near 0 and pi.
 template <bool D>
 __device__ Real<D> angle_of(const Pos<D> &P, int i1, int i2, int i3)
 {
     using R = Real<D>;
     V3<R> a = P.vec(i2, i1), b = P.vec(i2, i3);
-    R c = dot(a, b) / sqrt_(dot(a, a) * dot(b, b));
-    if (!D) c = fminf(1.0f, fmaxf(-1.0f, (float)c));
-    return acos_(c);
+    V3<R> w = cross(a, b);
+    return atan2_(sqrt_(dot(w, w)), dot(a, b));
 }
 
 // dihedral_angle (E:1255-1302)
@@ -136,54 +138,57 @@ __device__ void bond_force(const Pos<D> &P, Acc<D> &A, int i1, int i2, Real<D> k
     A.add(i2, g);
 }
 
-// harmonic angle (bead_valence_force E:1031-1134; clamp = stacking_valence_force E:1138-1251)
+// harmonic angle k0 (theta0 - theta)^2 at i2 (bead_valence_force E:1031-1134;
+// clamp = stacking_valence_force E:1138-1251, no force once cos theta < -0.99995).
+// The reference writes the force as s d(cos theta)/dx with s = -2 k0 (theta0 -
+// theta) / sin theta; this is the same vector, 2 k0 (theta0 - theta) d theta/dx,
+// with d theta/dx1 = a x w / (|a|^2 |w|), d theta/dx3 = -b x w / (|b|^2 |w|),
+// w = a x b, which keeps FP32 accurate where sin theta is small.
 template <bool D>
 __device__ void angle_force(const Pos<D> &P, Acc<D> &A, int i1, int i2, int i3, Real<D> k0, Real<D> th0, bool clamp)
 {
     using R = Real<D>;
     V3<R> a = P.vec(i2, i1), b = P.vec(i2, i3);
-    R ia = R(1) / dot(a, a), ib = R(1) / dot(b, b);
-    R iab = sqrt_(ia * ib);
-    R c = dot(a, b) * iab;
-    if (clamp && c < R(-0.99995)) return;  // theta = pi, no force
-    if (!D) c = fminf(1.0f, fmaxf(-1.0f, (float)c));
-    R sn = sqrt_(R(1) - c * c);
-    if (sn == R(0)) return;
-    R th = acos_(c);
-    R s = R(-2) * k0 * (th0 - th) / sn;
-    R ca = c * ia, cb = c * ib;
-    V3<R> g1 = iab * b - ca * a;
-    V3<R> g3 = iab * a - cb * b;
-    V3<R> g2 = R(-1) * (g1 + g3);
-    A.add(i1, s * g1);
-    A.add(i2, s * g2);
-    A.add(i3, s * g3);
+    const R aa = dot(a, a), bb = dot(b, b), ab = dot(a, b);
+    if (clamp && ab * rsqrt_(aa * bb) < R(-0.99995)) return;  // theta = pi, no force
+    const V3<R> w = cross(a, b);
+    const R ww = sqrt_(dot(w, w));
+    if (ww == R(0)) return;
+    const R th = atan2_(ww, ab);
+    const R s = R(2) * k0 * (th0 - th) / ww;
+    const V3<R> g1 = (s / aa) * cross(a, w);
+    const V3<R> g3 = (-s / bb) * cross(b, w);
+    A.add(i1, g1);
+    A.add(i2, R(-1) * (g1 + g3));
+    A.add(i3, g3);
 }
 
-// harmonic dihedral (stacking_dihedral_force, E:1306-1454): s * d(cos psi)/dx
+// harmonic dihedral k0 (psi0 - psi)^2 (stacking_dihedral_force, E:1306-1454).
+// The reference's s d(cos psi)/dx with s = -2 k0 (psi0 - psi) / sin psi equals
+// 2 k0 (psi0 - psi) d psi/dx; here d psi/dx uses the cross-product form
+// d psi/dx1 = -|v2| m / |m|^2, d psi/dx4 = |v2| n / |n|^2,
+// d psi/dx2 = -(1 + v1.v2/|v2|^2) d psi/dx1 + (v3.v2/|v2|^2) d psi/dx4,
+// which has no 1/sin psi and so no FP32 cancellation at planar (psi ~ 0, pi) geometry.
 template <bool D>
 __device__ void dihedral_force(const Pos<D> &P, Acc<D> &A, int i1, int i2, int i3, int i4, Real<D> k0,
                                Real<D> psi0)
 {
     using R = Real<D>;
-    V3<R> v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
-    V3<R> m = cross(v1, v2), n = cross(v2, v3);
-    R im = R(1) / dot(m, m), in = R(1) / dot(n, n);
-    R imn = sqrt_(im * in);
-    R l2 = sqrt_(dot(v2, v2));
-    R c = dot(m, n) * imn;
-    R sn = dot(v1, n) * l2 * imn;
-    if (sn == R(0)) return;
-    R psi = atan2_(sn, c);
-    R s = R(-2) * k0 * (psi0 - psi) / sn;
-    R cm = c * im, cn = c * in;
-    V3<R> G1 = imn * cross(v2, n) - cm * cross(v2, m);
-    V3<R> G2 = imn * (cross(n, v1) + cross(v3, m)) - cm * cross(m, v1) - cn * cross(v3, n);
-    V3<R> G3 = imn * cross(m, v2) - cn * cross(n, v2);
-    A.add(i1, R(-1) * s * G1);
-    A.add(i2, s * (G1 - G2));
-    A.add(i3, s * (G2 - G3));
-    A.add(i4, s * G3);
+    const V3<R> v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
+    const V3<R> m = cross(v1, v2), n = cross(v2, v3);
+    const R mm = dot(m, m), nn = dot(n, n), v22 = dot(v2, v2);
+    if (mm == R(0) || nn == R(0)) return;
+    const R l2 = sqrt_(v22);
+    const R psi = atan2_(dot(v1, n) * l2, dot(m, n));
+    const R c = R(2) * k0 * (psi0 - psi);
+    const V3<R> g1 = (-c * l2 / mm) * m;
+    const V3<R> g4 = (c * l2 / nn) * n;
+    const R p = dot(v1, v2) / v22, q = dot(v3, v2) / v22;
+    const V3<R> g2 = (R(-1) - p) * g1 + q * g4;
+    A.add(i1, g1);
+    A.add(i2, g2);
+    A.add(i3, R(-1) * (g1 + g2 + g4));
+    A.add(i4, g4);
 }
 
 // native dihedral imaged to within pi of the current one (E:1999-2019): branch -1/0/+1
@@ -460,11 +465,11 @@ __device__ inline void leap_frog(const Dev &d, const RepParams *R, int r, int p,
     double f[3] = {total_force<D>(d, p, 0), total_force<D>(d, p, 1), total_force<D>(d, p, 2)};
     if (d.noise == 0) {
         const int k = (p - R->p0 + 1) % 1000;
-        const float *g = d.gnoise + r * kNoise;
+        const double *g = d.gnoise + r * kNoise;
         const double sg = R->sigma[t];
-        f[0] = f[0] + (double)g[k] * sg;
-        f[1] = f[1] + (double)g[k + 1000] * sg;
-        f[2] = f[2] + (double)g[k + 2000] * sg;
+        f[0] = __dadd_rn(f[0], __dmul_rn(g[k], sg));
+        f[1] = __dadd_rn(f[1], __dmul_rn(g[k + 1000], sg));
+        f[2] = __dadd_rn(f[2], __dmul_rn(g[k + 2000], sg));
     }
     const double v0[3] = {d.vx[p], d.vy[p], d.vz[p]};
     const double x0[3] = {d.x[p], d.y[p], d.z[p]};
@@ -494,11 +499,20 @@ __device__ void noise_and_shift(const Dev &d, int r, unsigned long long &s_ctr)
         for (int t = threadIdx.x; t < kNoise / 2; t += blockDim.x) {
             const uint32_t v1 = rand_value(R->seed, c0 + 2 * t);
             const uint32_t v2 = rand_value(R->seed, c0 + 2 * t + 1);
-            const float a = bm_radius(v1);
-            float sn, cs;
-            sincospif(2.0f * ((float)v2 * (1.0f / 2147483647.0f)), &sn, &cs);
-            d.gnoise[r * kNoise + 2 * t] = a * cs;
-            d.gnoise[r * kNoise + 2 * t + 1] = a * sn;
+            if (D) {  // Box-Muller as the reference forms it (E:2598-2606), in FP64
+                const double a = sqrt(-2.0 * log((double)v1 / 2147483647.0));
+                const double b = 2.0 * 3.14159265358979323846 * ((double)v2 / 2147483647.0);
+                double sn, cs;
+                sincos(b, &sn, &cs);
+                d.gnoise[r * kNoise + 2 * t] = a * cs;
+                d.gnoise[r * kNoise + 2 * t + 1] = a * sn;
+            } else {  // FP32 Box-Muller, radius accurate over the whole uniform range
+                const float a = bm_radius(v1);
+                float sn, cs;
+                sincospif(2.0f * ((float)v2 * (1.0f / 2147483647.0f)), &sn, &cs);
+                d.gnoise[r * kNoise + 2 * t] = (double)(a * cs);
+                d.gnoise[r * kNoise + 2 * t + 1] = (double)(a * sn);
+            }
         }
     }
     __syncthreads();

@@ -18,7 +18,7 @@ struct Dev {
     double *x, *y, *z, *xo, *yo, *zo, *vx, *vy, *vz;
     int4 *q;                    // fixed-point position + (type | kind << 8 | active << 16)
     unsigned long long *f, *flr;  // 3P each: int64 fixed point (mixed) or double (FP64)
-    float *gnoise;              // R x kNoise
+    double *gnoise;             // R x kNoise
     // cells
     int *cell_of, *cell_count, *cell_start, *cell_fill, *cell_list;
     // neighbour lists, column-major: nbr[k * P + p]
