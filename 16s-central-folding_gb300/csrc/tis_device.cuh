@@ -21,6 +21,9 @@ constexpr double kSig0 = 1.5852;     // LJ length scale (E:749-821)
 constexpr double kFixScale = 4294967296.0;   // 2^32 fixed-point units per kcal/mol/A
 constexpr float kFixScaleF = 4294967296.0f;
 constexpr float kFixLimit = 1.0e9f;  // |contribution| clamp (int64 range / 2^32 with margin)
+constexpr int kExcl = 8;             // bonded (1-2, 1-3) partners stored per particle
+constexpr int kExclShift = 30;       // SR list entry: partner | (exclusion multiplicity << 30)
+constexpr int kIdxMask = (1 << kExclShift) - 1;
 
 enum ErrBits : int { kErrCapacity = 1, kErrNonFinite = 2, kErrRange = 4 };
 

@@ -187,9 +187,9 @@ int populate(tis_handle *h)
 
 void enqueue_step(tis_handle *h)
 {
-    tis::launch_pair_sr(h->dev, h->stream, false);
+    tis::launch_pair_sr(h->dev, h->stream, false, true);
     tis::launch_pair_lr(h->dev, h->stream, false, false);
-    tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true);
+    tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true, true);
     tis::launch_integrate(h->dev, h->stream);
     tis::launch_control(h->dev, h->stream);
     tis::launch_rebuild(h->dev, h->stream);
@@ -255,6 +255,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     std::vector<int> st3_idx, st3_off, st2_idx, hb_idx, hb_dode, hb_aoff{0}, hb_aidx, hba_val, hba_coff{0}, hba_cidx,
         hba_n, ca_list;
     std::vector<double> st3_nat, st3_E, st2_r0, st2_E, hb_nat, hb_E;
+    std::vector<std::vector<int>> excl_of;
     int p0 = 0, c0 = 0, kscr = 0;
     double max_rho = 0, max_rho_ch = 0;
     const char *snames[9] = {"x", "y", "z", "ox", "oy", "oz", "vx", "vy", "vz"};
@@ -273,6 +274,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
         const tis::Array *sv[9];
         for (int k = 0; k < 9; ++k)
             if (!(sv[k] = need(s, snames[k], r, TIS_F64, n))) return bail(TIS_ERR_ARG);
+        excl_of.resize((size_t)p0 + round_up(n, tis::kBlock));
         const int center = (int)scalar_i64(s, "center", 499);
         if (center < 0 || center >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: centre bead %d outside the RNA", r, center));
 
@@ -392,6 +394,19 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
             bt_par.push_back(make_double2(btk0->as<double>()[t], btx0->as<double>()[t]));
         }
         hr.bt1 = (int)bt_idx.size();
+        // bonded partners whose LJ the reference adds in the SR loop and subtracts in
+        // polymer_constraints (E:948, E:1132): one entry per subtraction
+        for (int64_t t = 0; t < nbt; ++t) {
+            const int kd = btk->as<int32_t>()[t];
+            const int a = p0 + bta->as<int32_t>()[t];
+            const int b = p0 + (kd == 1 ? btc->as<int32_t>()[t] : btb->as<int32_t>()[t]);
+            for (int side = 0; side < 2; ++side) {
+                const int self = side ? b : a, other = side ? a : b;
+                if ((int)excl_of[self].size() >= tis::kExcl)
+                    return bail(fail(TIS_ERR_ARG, "replica %d: particle %d has more than %d bonded partners", r, self - p0, tis::kExcl));
+                excl_of[self].push_back(other);
+            }
+        }
 
         // stacks
         const tis::Array *s3E = need(s, "st3_E", r, TIS_F64), *s2E = need(s, "st2_E", r, TIS_F64);
@@ -536,6 +551,18 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
         (rc = dupload(O, &d_rep, rep_of)) || (rc = dupload(O, &d_cellrep, cell_rep)) || (rc = dupload(O, &d_q, q)))
         return bail(rc);
     d.rp = d_rp; d.rs = d_rs; d.blk_rep = d_blk; d.rep_of = d_rep; d.cell_rep = d_cellrep; d.q = d_q;
+    {
+        excl_of.resize(h->P);
+        std::vector<int> ex((size_t)tis::kExcl * h->P, -1), nex(h->P, 0);
+        for (int p = 0; p < h->P; ++p) {
+            nex[p] = (int)excl_of[p].size();
+            for (int k = 0; k < nex[p]; ++k) ex[(size_t)k * h->P + p] = excl_of[p][k];
+        }
+        int *d_ex = nullptr, *d_nex = nullptr;
+        if ((rc = dupload(O, &d_ex, ex)) || (rc = dupload(O, &d_nex, nex))) return bail(rc);
+        d.excl = d_ex;
+        d.n_excl = d_nex;
+    }
     double **sd[9] = {&d.x, &d.y, &d.z, &d.xo, &d.yo, &d.zo, &d.vx, &d.vy, &d.vz};
     for (int c = 0; c < 9; ++c)
         if ((rc = dupload(O, sd[c], st[c]))) return bail(rc);
@@ -656,7 +683,7 @@ int tis_get_pairs(tis_handle *h, int r, int which, int32_t *pairs, int64_t cap, 
     std::vector<std::pair<int, int>> pr;
     for (int i = 0; i < hr.n; ++i)
         for (int k = 0; k < c[i]; ++k) {
-            const int j = lst[(size_t)k * hr.npad + i] - hr.p0;
+            const int j = (lst[(size_t)k * hr.npad + i] & tis::kIdxMask) - hr.p0;
             if (i < j) pr.emplace_back(i, j);
         }
     std::sort(pr.begin(), pr.end());
@@ -690,12 +717,12 @@ int tis_compute_forces(tis_handle *h, int r, int mask, double *forces, double *e
     if ((rc = clear_flags(h))) return rc;
     const tis::Dev &d = h->dev;
     TIS_CUDA(cudaMemsetAsync(d.eterm, 0, sizeof(double) * h->R * tis::kNE, h->stream));
-    if (mask & TIS_TERM_SR) tis::launch_pair_sr(d, h->stream, true);
+    if (mask & TIS_TERM_SR) tis::launch_pair_sr(d, h->stream, true, false);
     else TIS_CUDA(cudaMemsetAsync(d.f, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
     if (mask & TIS_TERM_LR) tis::launch_pair_lr(d, h->stream, true, true);
     else TIS_CUDA(cudaMemsetAsync(d.flr, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
     const int tmask = (mask & TIS_TERM_BONDED ? 4 : 0) | (mask & TIS_TERM_STACK ? 8 : 0) | (mask & TIS_TERM_HB ? 16 : 0);
-    if (tmask) tis::launch_topology(d, h->stream, tmask, true, false);
+    if (tmask) tis::launch_topology(d, h->stream, tmask, true, false, false);
     tis::launch_rg(d, h->stream, r, h->d_scalar);
     TIS_CUDA(cudaGetLastError());
     const RepHost &hr = h->rep[r];
@@ -737,11 +764,39 @@ int tis_deterministic_forces(tis_handle *h)
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     int rc;
     if (!h->lists_built && (rc = populate(h))) return rc;
-    tis::launch_pair_sr(h->dev, h->stream, false);
+    tis::launch_pair_sr(h->dev, h->stream, false, true);
     tis::launch_pair_lr(h->dev, h->stream, false, false);
-    tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, false);
+    tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, false, true);
     TIS_CUDA(cudaGetLastError());
     return TIS_OK;
+}
+
+int tis_get_forces(tis_handle *h, int r, double *forces)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    if (!forces) return fail(TIS_ERR_ARG, "null output");
+    const RepHost &hr = h->rep[r];
+    const tis::Dev &d = h->dev;
+    std::vector<unsigned long long> f(3 * (size_t)hr.n), fl(3 * (size_t)hr.n);
+    for (int c = 0; c < 3; ++c) {
+        TIS_CUDA(cudaMemcpyAsync(f.data() + c * hr.n, d.f + (size_t)c * h->P + hr.p0, 8 * hr.n, cudaMemcpyDeviceToHost, h->stream));
+        TIS_CUDA(cudaMemcpyAsync(fl.data() + c * hr.n, d.flr + (size_t)c * h->P + hr.p0, 8 * hr.n, cudaMemcpyDeviceToHost, h->stream));
+    }
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < hr.n; ++i)
+        for (int c = 0; c < 3; ++c) {
+            const size_t k = (size_t)c * hr.n + i;
+            if (d.fp64) {
+                double a, b;
+                memcpy(&a, &f[k], 8);
+                memcpy(&b, &fl[k], 8);
+                forces[3 * i + c] = a + b;
+            } else {
+                forces[3 * i + c] = (double)(long long)(f[k] + fl[k]) / tis::kFixScale;
+            }
+        }
+    return check_flags(h);
 }
 
 int tis_full_forces(tis_handle *h)
@@ -807,11 +862,11 @@ int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int64_t s = 0; s < n; ++s) {
         TIS_CUDA(cudaEventRecord(ev[0], h->stream));
-        tis::launch_pair_sr(h->dev, h->stream, false);
+        tis::launch_pair_sr(h->dev, h->stream, false, true);
         TIS_CUDA(cudaEventRecord(ev[1], h->stream));
         tis::launch_pair_lr(h->dev, h->stream, false, false);
         TIS_CUDA(cudaEventRecord(ev[2], h->stream));
-        tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true);
+        tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true, true);
         TIS_CUDA(cudaEventRecord(ev[3], h->stream));
         tis::launch_integrate(h->dev, h->stream);
         TIS_CUDA(cudaEventRecord(ev[4], h->stream));

@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(kBlock) k_quantize(Dev d)
 // ---------------------------------------------------------------------------
 // pair forces over the full (both-direction) neighbour lists
 // ---------------------------------------------------------------------------
-template <bool D, bool LR, bool EN>
+template <bool D, bool LR, bool EN, bool EX>
 __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
 {
     const int r = d.blk_rep[blockIdx.x];
@@ -329,7 +329,9 @@ __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
         const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
         const float rc2 = R->rc2f, lo = rc2 * (1.0f - kBand), hi = rc2 * (1.0f + kBand);
         for (int k = 0; k < cnt; ++k) {
-            const int j = __ldg(nbr + (size_t)k * P + p);
+            const int raw = __ldg(nbr + (size_t)k * P + p);
+            const int j = raw & kIdxMask;
+            const float ljw = EX ? (float)(1 - (raw >> kExclShift)) : 1.0f;
             const int4 qj = __ldg(d.q + j);
             const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
             const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
@@ -338,12 +340,12 @@ __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
             const int tj = qj.w & 0xff, kj = (qj.w >> 8) & 0xff;
             const int J = jn12(tp, tj);
             float F = 0.0f;
-            if (!LR && r2 <= s_dlj2[J]) {  // LJ_FORCE (E:801-821)
+            if (!LR && ljw != 0.0f && r2 <= s_dlj2[J]) {  // LJ_FORCE (E:801-821)
                 const float rr = sqrtf(r2);
                 const float dr = rr - s_dm[J];
                 const float s = 1.5852f / dr;
                 const float s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
-                F = s_flj[J] * (s14 - s8) * dr / rr;
+                F = ljw * (s_flj[J] * (s14 - s8) * dr / rr);
                 if (EN) {
                     double e;
                     if ((double)r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
                         const float s6 = s4 * s2, s12 = s6 * s6;
                         e = (double)(R->elj[J] * (s12 - 2.0f * s6 + 1.0f));
                     }
-                    e_lj += 0.5 * e;
+                    e_lj += 0.5 * (double)ljw * e;
                 }
             }
             if ((LR || (chp && is_charged(kj))) && r2 <= hi) {  // COULOMB_TRUNCATED_FORCE (E:841-855)
@@ -375,19 +377,21 @@ __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
     } else {
         double ax = 0, ay = 0, az = 0;
         for (int k = 0; k < cnt; ++k) {
-            const int j = __ldg(nbr + (size_t)k * P + p);
+            const int raw = __ldg(nbr + (size_t)k * P + p);
+            const int j = raw & kIdxMask;
+            const double ljw = EX ? (double)(1 - (raw >> kExclShift)) : 1.0;
             const int tj = d.q[j].w & 0xff, kj = (d.q[j].w >> 8) & 0xff;
             const int J = jn12(tp, tj);
             double v[3];
             exact_vec(d, R, p, j, v);
             const double r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
             double F = 0.0;
-            if (!LR && r2 <= R->dlj2_d[J]) {
+            if (!LR && ljw != 0.0 && r2 <= R->dlj2_d[J]) {
                 const double rr = sqrt(r2);
                 const double dr = rr + kSig0 - R->dlj_d[J];
                 const double s = kSig0 / dr;
                 const double s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
-                F = R->flj_d[J] * (s14 - s8) * dr / rr;
+                F = ljw * (R->flj_d[J] * (s14 - s8) * dr / rr);
                 if (EN) {
                     double e;
                     if (r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
@@ -395,7 +399,7 @@ __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
                         const double s6 = s4 * s2, s12 = s6 * s6;
                         e = R->elj_d[J] * (s12 - 2.0 * s6 + 1.0);
                     }
-                    e_lj += 0.5 * e;
+                    e_lj += 0.5 * ljw * e;
                 }
             }
             if ((LR || (chp && is_charged(kj))) && r2 <= R->rc2) {
@@ -541,7 +545,7 @@ __global__ void k_noise(Dev d)
 constexpr int kTopoThreads = 256;
 
 template <bool D, bool EN>
-__global__ void __launch_bounds__(kTopoThreads) k_topology(Dev d, int mask, int make_noise)
+__global__ void __launch_bounds__(kTopoThreads) k_topology(Dev d, int mask, int make_noise, int excl_in_list)
 {
     using Rl = Real<D>;
     const int r = blockIdx.x;
@@ -565,6 +569,7 @@ __global__ void __launch_bounds__(kTopoThreads) k_topology(Dev d, int mask, int 
             const int ex = id.w == 0 ? id.y : id.z;  // excluded pair partner of id.x
             if (id.w == 0) bond_force<D>(P, A, id.x, id.y, (Rl)par.x, (Rl)par.y);
             else angle_force<D>(P, A, id.x, id.y, id.z, (Rl)par.x, (Rl)par.y, false);
+            if (excl_in_list && !EN) continue;  // the SR kernel already left this pair's LJ out
             // subtract the LJ force of the excluded pair (reduce_forces, E:880-897)
             const int ta = d.q[id.x].w & 0xff, tb = d.q[ex].w & 0xff;
             const int J = jn12(ta, tb);
@@ -1016,6 +1021,9 @@ __global__ void __launch_bounds__(kBlock) k_pair_search(Dev d)
     const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
     const float sr_lo = R->r2srf * (1.0f - kBand), sr_hi = R->r2srf * (1.0f + kBand);
     const float lr_lo = R->r2lrf * (1.0f - kBand), lr_hi = R->r2lrf * (1.0f + kBand);
+    int exl[kExcl];
+    const int nex = d.n_excl[p];
+    for (int t2 = 0; t2 < kExcl; ++t2) exl[t2] = t2 < nex ? d.excl[(size_t)t2 * P + p] : -1;
     int nsr = 0, nlr = 0;
     for (int a = 0; a < m1; ++a)
         for (int b = 0; b < m2; ++b)
@@ -1046,7 +1054,9 @@ __global__ void __launch_bounds__(kBlock) k_pair_search(Dev d)
                         }
                     }
                     if (cls == 1) {
-                        if (nsr < d.cap_sr) d.nbr_sr[(size_t)nsr * P + p] = j;
+                        int m = 0;  // how often the reference subtracts this pair's LJ again
+                        for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
+                        if (nsr < d.cap_sr) d.nbr_sr[(size_t)nsr * P + p] = j | (m << kExclShift);
                         ++nsr;
                     } else if (cls == 2) {
                         if (nlr < d.cap_lr) d.nbr_lr[(size_t)nlr * P + p] = j;
@@ -1141,14 +1151,16 @@ __global__ void k_rg(Dev d, int r, double *out)
 // ---------------------------------------------------------------------------
 void launch_quantize(const Dev &d, cudaStream_t s) { k_quantize<<<d.nblk, kBlock, 0, s>>>(d); }
 
-void launch_pair_sr(const Dev &d, cudaStream_t s, bool en)
+void launch_pair_sr(const Dev &d, cudaStream_t s, bool en, bool ex)
 {
     if (d.fp64) {
-        if (en) k_pair<true, false, true><<<d.nblk, kBlock, 0, s>>>(d, 1);
-        else k_pair<true, false, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        if (en) k_pair<true, false, true, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        else if (ex) k_pair<true, false, false, true><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        else k_pair<true, false, false, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
     } else {
-        if (en) k_pair<false, false, true><<<d.nblk, kBlock, 0, s>>>(d, 1);
-        else k_pair<false, false, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        if (en) k_pair<false, false, true, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        else if (ex) k_pair<false, false, false, true><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        else k_pair<false, false, false, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
     }
 }
 
@@ -1156,23 +1168,23 @@ void launch_pair_lr(const Dev &d, cudaStream_t s, bool en, bool force_all)
 {
     const int fa = force_all ? 1 : 0;
     if (d.fp64) {
-        if (en) k_pair<true, true, true><<<d.nblk, kBlock, 0, s>>>(d, fa);
-        else k_pair<true, true, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
+        if (en) k_pair<true, true, true, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
+        else k_pair<true, true, false, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
     } else {
-        if (en) k_pair<false, true, true><<<d.nblk, kBlock, 0, s>>>(d, fa);
-        else k_pair<false, true, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
+        if (en) k_pair<false, true, true, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
+        else k_pair<false, true, false, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
     }
 }
 
-void launch_topology(const Dev &d, cudaStream_t s, int mask, bool en, bool make_noise)
+void launch_topology(const Dev &d, cudaStream_t s, int mask, bool en, bool make_noise, bool ex)
 {
-    const int mn = make_noise ? 1 : 0;
+    const int mn = make_noise ? 1 : 0, xl = ex ? 1 : 0;
     if (d.fp64) {
-        if (en) k_topology<true, true><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn);
-        else k_topology<true, false><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn);
+        if (en) k_topology<true, true><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn, xl);
+        else k_topology<true, false><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn, xl);
     } else {
-        if (en) k_topology<false, true><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn);
-        else k_topology<false, false><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn);
+        if (en) k_topology<false, true><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn, xl);
+        else k_topology<false, false><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn, xl);
     }
 }
 

@@ -24,6 +24,9 @@ struct Dev {
     // neighbour lists, column-major: nbr[k * P + p]
     int *nbr_sr, *n_sr, *nbr_lr, *n_lr;
     int cap_sr, cap_lr;
+    // bonded partners whose LJ the reference subtracts again (reduce_forces, E:880-897),
+    // column-major excl[k * P + p], k < n_excl[p] <= kExcl
+    const int *excl, *n_excl;
     // topology (global particle indices)
     const int4 *bt_idx;         // a, b, c, kind
     const double2 *bt_par;      // k0, x0
@@ -45,9 +48,13 @@ struct Dev {
 
 // Launchers (stream-ordered; gated per replica on device flags where noted).
 void launch_quantize(const Dev &d, cudaStream_t s);
-void launch_pair_sr(const Dev &d, cudaStream_t s, bool energies);
+// excl_in_list: the hot path skips the LJ of bonded pairs in the SR kernel and
+// does not subtract it in the bonded kernel (the reference's net force, without
+// the cancellation of two large equal terms); false gives the reference's
+// per-term split (tis_compute_forces).
+void launch_pair_sr(const Dev &d, cudaStream_t s, bool energies, bool excl_in_list);
 void launch_pair_lr(const Dev &d, cudaStream_t s, bool energies, bool force_all);
-void launch_topology(const Dev &d, cudaStream_t s, int mask, bool energies, bool make_noise);
+void launch_topology(const Dev &d, cudaStream_t s, int mask, bool energies, bool make_noise, bool excl_in_list);
 void launch_noise(const Dev &d, cudaStream_t s);  // Gaussians + recentring shift only
 void launch_integrate(const Dev &d, cudaStream_t s);
 void launch_control(const Dev &d, cudaStream_t s);

@@ -92,6 +92,7 @@ def _declare(L):
         "tis_get_launch_count": [vp, C.POINTER(C.c_int64)],
         "tis_rand_stream": [C.c_uint64, C.c_uint64, i64, ip],
         "tis_profile_stages": [vp, i64, dp],
+        "tis_get_forces": [vp, i32, dp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -105,7 +106,7 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_pairs", "tis_get_hb_status", "tis_compute_forces", "tis_deterministic_forces", "tis_full_forces",
             "tis_move_rigid_units", "tis_check_shifts", "tis_step", "tis_sync", "tis_get_energies",
             "tis_get_stack_energies", "tis_get_counters", "tis_get_info", "tis_replica_size", "tis_get_launch_count",
-            "tis_rand_stream", "tis_profile_stages"]
+            "tis_rand_stream", "tis_profile_stages", "tis_get_forces"]
 
 
 def rand_stream(seed, first, n):
@@ -279,6 +280,12 @@ class Engine:
 
     def deterministic_forces(self):
         _check(lib().tis_deterministic_forces(self.h))
+
+    def current_forces(self, r):
+        """The force array as it stands (after deterministic_forces: the total deterministic force)."""
+        f = np.zeros(3 * self.n[r])
+        _check(lib().tis_get_forces(self.h, r, _dp(f)))
+        return f
 
     def full_forces(self):
         _check(lib().tis_full_forces(self.h))

@@ -168,6 +168,9 @@ int tis_deterministic_forces(tis_handle *h); /* deterministic_forces_MPI  E:2524
 int tis_full_forces(tis_handle *h);          /* full_forces               E:2590 */
 int tis_move_rigid_units(tis_handle *h);     /* move_rigid_units          E:2660 */
 int tis_check_shifts(tis_handle *h);         /* check_shifts              E:1741 */
+/* The force array of one replica as it stands (after tis_deterministic_forces:
+ * the reference's fx,fy,fz after the Allreduce, E:2576-2585), x,y,z interleaved. */
+int tis_get_forces(tis_handle *h, int replica, double *forces);
 
 /* n steps of the whole sequence for every replica (CUDA-graph replay when
  * use_graph is set); asynchronous: returns after enqueueing. */

