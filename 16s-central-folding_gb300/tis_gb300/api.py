@@ -93,6 +93,7 @@ def _declare(L):
         "tis_rand_stream": [C.c_uint64, C.c_uint64, i64, ip],
         "tis_profile_stages": [vp, i64, dp],
         "tis_get_forces": [vp, i32, dp],
+        "tis_pair_lists_noalloc": [vp, vp, vp, vp, C.c_int32, dp, C.c_double, C.c_double, vp, i64, vp, i64, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -106,7 +107,15 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_pairs", "tis_get_hb_status", "tis_compute_forces", "tis_deterministic_forces", "tis_full_forces",
             "tis_move_rigid_units", "tis_check_shifts", "tis_step", "tis_sync", "tis_get_energies",
             "tis_get_stack_energies", "tis_get_counters", "tis_get_info", "tis_replica_size", "tis_get_launch_count",
-            "tis_rand_stream", "tis_profile_stages", "tis_get_forces"]
+            "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc"]
+
+
+def pair_lists_noalloc(d_x, d_y, d_z, d_kind, n, box, sr_radius, lr_radius, d_sr, sr_cap, d_lr, lr_cap, d_counts,
+                       stream=None):
+    """Allocation-free list build on caller-owned device buffers (addresses as ints)."""
+    b = np.ascontiguousarray(box, dtype=np.float64)
+    _check(lib().tis_pair_lists_noalloc(d_x, d_y, d_z, d_kind, n, _dp(b), sr_radius, lr_radius, d_sr, sr_cap,
+                                        d_lr, lr_cap, d_counts, stream))
 
 
 def rand_stream(seed, first, n):

@@ -205,6 +205,33 @@ int tis_get_launch_count(tis_handle *h, int64_t *n);
  * (E:2594-2606) consume it in the reference's order. */
 int tis_rand_stream(uint64_t seed, uint64_t first, int64_t n, int32_t *out);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free list build                                                 */
+/* ------------------------------------------------------------------------ */
+/* No counterpart in the reference: an addition for callers that cannot allocate
+ * device memory where they need a neighbour list - a host recording its CUDA work
+ * into a graph (cudaMalloc cannot be captured), a time step that must not
+ * synchronise the device (cudaFree does), or an engine running under a fixed,
+ * pre-reserved memory budget.  It bins one configuration into cells and returns
+ * the SR and LR pair sets with populate_lists' rule (E:1461-1694): SR when
+ * r^2 <= sr_radius^2, otherwise LR when r^2 <= lr_radius^2 and neither bead is a
+ * sugar or a base (kind 1 or 2); cells of side >= lr_radius; minimum image.
+ * All pointers d_* are device memory owned by the caller: positions (FP64, n
+ * each), kinds (n), pair outputs (2 ints per pair, i < j, unordered, at most
+ * *_cap pairs written) and d_counts[3] = {SR pairs, LR pairs, particles outside
+ * the grid's single periodic wrap}, all written on `stream` (cudaStream_t; NULL
+ * = default stream); counts above the capacities mean the outputs were cut.
+ * Allocates nothing: its scratch is a fixed device array of 896 KiB that every
+ * GPU loading the library keeps until exit, which limits a call to 65,536
+ * particles and 32,768 cells (larger calls fail with TIS_ERR_ARG).  Every call
+ * reuses that one array, so calls that overlap on the GPU race: order them.  The
+ * first call on a device looks up the array's address; make it before any stream
+ * capture starts. */
+int tis_pair_lists_noalloc(const double *d_x, const double *d_y, const double *d_z, const int32_t *d_kind,
+                           int32_t n, const double *box, double sr_radius, double lr_radius,
+                           int32_t *d_sr_pairs, int64_t sr_cap, int32_t *d_lr_pairs, int64_t lr_cap,
+                           uint64_t *d_counts, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
