@@ -536,6 +536,11 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     d.noise = prm.noise;
     d.cap_sr = cap_sr;
     d.cap_lr = cap_lr;
+    {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, prm.device);
+        d.search_warps = std::max(4, sms * 8 * 4);  // 8 blocks of 4 warps per SM
+    }
     auto &O = h->owned;
     int rc = TIS_OK;
     std::vector<int4> q(h->P);
@@ -569,7 +574,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     if ((rc = dalloc(O, &d.f, 3 * (size_t)h->P)) || (rc = dalloc(O, &d.flr, 3 * (size_t)h->P)) ||
         (rc = dalloc(O, &d.gnoise, (size_t)h->R * tis::kNoise)) || (rc = dalloc(O, &d.cell_of, h->P)) ||
         (rc = dalloc(O, &d.cell_count, h->C)) || (rc = dalloc(O, &d.cell_start, h->C)) ||
-        (rc = dalloc(O, &d.cell_fill, h->C)) || (rc = dalloc(O, &d.cell_list, h->P)) ||
+        (rc = dalloc(O, &d.cell_fill, h->C)) || (rc = dalloc(O, &d.cell_list, h->P)) || (rc = dalloc(O, &d.qs, h->P)) ||
         (rc = dalloc(O, &d.n_sr, h->P)) || (rc = dalloc(O, &d.n_lr, h->P)) ||
         (rc = dalloc(O, &d.nbr_sr, (size_t)cap_sr * h->P)) || (rc = dalloc(O, &d.nbr_lr, (size_t)cap_lr * h->P)) ||
         (rc = dalloc(O, &d.eterm, (size_t)h->R * tis::kNE)) || (rc = dalloc(O, &d.shift, (size_t)h->R * 3)) ||

@@ -956,25 +956,48 @@ __global__ void __launch_bounds__(kBlock) k_cell_fill(Dev d)
     d.cell_list[R->p0 + d.cell_start[R->c0 + c] + slot] = p;
 }
 
-// particles of a cell in index order, as the reference appends them (E:1536-1540)
-__global__ void k_cell_sort(Dev d)
+// One warp per cell: in FP64 mode the cell's particles are put in index order,
+// as the reference appends them (E:1536-1540), so that list order and hence
+// FP64 summation order are reproducible; mixed-precision sums are exact in fixed
+// point and need no order.  Then the packed positions are copied in cell order
+// so the pair search reads each cell's candidates contiguously.
+template <bool D>
+__global__ void k_cell_order(Dev d)
 {
-    const int cg = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cg >= d.C) return;
-    const int r = d.cell_rep[cg];
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= d.C) return;
+    const int r = d.cell_rep[warp];
     if (!d.rs[r].rebuild) return;
     const RepParams *R = d.rp + r;
-    int *seg = d.cell_list + R->p0 + d.cell_start[cg];
-    const int n = d.cell_count[cg];
-    for (int i = 1; i < n; ++i) {
-        const int v = seg[i];
-        int j = i - 1;
-        while (j >= 0 && seg[j] > v) {
-            seg[j + 1] = seg[j];
-            --j;
+    const int base = R->p0 + d.cell_start[warp];
+    const int n = d.cell_count[warp];
+    int *seg = d.cell_list + base;
+    if (D && n > 1 && n <= 256) {  // rank sort, at most 8 particles per lane held in registers
+        int v[8], rk[8];
+        int m = 0;
+        for (int i = lane; i < n; i += 32, ++m) {
+            v[m] = seg[i];
+            int c = 0;
+            for (int k = 0; k < n; ++k) c += seg[k] < v[m];
+            rk[m] = c;
         }
-        seg[j + 1] = v;
+        __syncwarp();
+        for (int t = 0; t < m; ++t) seg[rk[t]] = v[t];
+        __syncwarp();
+    } else if (D && n > 256) {  // very full cell: insertion sort by one lane
+        if (lane == 0)
+            for (int i = 1; i < n; ++i) {
+                const int v = seg[i];
+                int j = i - 1;
+                while (j >= 0 && seg[j] > v) {
+                    seg[j + 1] = seg[j];
+                    --j;
+                }
+                seg[j + 1] = v;
+            }
+        __syncwarp();
     }
+    for (int i = lane; i < n; i += 32) d.qs[base + i] = d.q[seg[i]];
 }
 
 // distinct periodic neighbours of cell index i (1..m) along one axis
@@ -997,76 +1020,92 @@ __device__ inline int axis_neighbours(int i, int m, int out[3])
 // distance from the exact integer differences decides outside a narrow band
 // around each threshold; inside it the FP64 distance with the reference's
 // rounding and image rule decides, so the lists are the reference's sets.
+// One warp per particle: the lanes scan a neighbour cell's candidates together
+// (contiguous in cell order) and append hits in candidate order by ballot.  The
+// warps stride over the particles of the replicas that rebuild this step.
 template <bool D>
-__global__ void __launch_bounds__(kBlock) k_pair_search(Dev d)
+__global__ void __launch_bounds__(128) k_pair_search(Dev d)
 {
-    const int r = d.blk_rep[blockIdx.x];
-    if (!d.rs[r].rebuild) return;
-    const RepParams *R = d.rp + r;
-    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int P = d.P;
-    const int c = d.cell_of[p];
-    if (c < 0) {
-        d.n_sr[p] = 0;
-        d.n_lr[p] = 0;
-        return;
-    }
-    const int4 qp = d.q[p];
-    const bool chp = is_charged((qp.w >> 8) & 0xff);
-    const int i1 = c / (R->mc[1] * R->mc[2]) + 1, i2 = (c / R->mc[2]) % R->mc[1] + 1, i3 = c % R->mc[2] + 1;
-    int n1[3], n2[3], n3[3];
-    const int m1 = axis_neighbours(i1, R->mc[0], n1);
-    const int m2 = axis_neighbours(i2, R->mc[1], n2);
-    const int m3 = axis_neighbours(i3, R->mc[2], n3);
-    const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
-    const float sr_lo = R->r2srf * (1.0f - kBand), sr_hi = R->r2srf * (1.0f + kBand);
-    const float lr_lo = R->r2lrf * (1.0f - kBand), lr_hi = R->r2lrf * (1.0f + kBand);
-    int exl[kExcl];
-    const int nex = d.n_excl[p];
-    for (int t2 = 0; t2 < kExcl; ++t2) exl[t2] = t2 < nex ? d.excl[(size_t)t2 * P + p] : -1;
-    int nsr = 0, nlr = 0;
-    for (int a = 0; a < m1; ++a)
-        for (int b = 0; b < m2; ++b)
-            for (int e = 0; e < m3; ++e) {
-                const int cc = (n1[a] - 1) * R->mc[1] * R->mc[2] + (n2[b] - 1) * R->mc[2] + (n3[e] - 1);
-                const int start = R->p0 + d.cell_start[R->c0 + cc];
-                const int cnt = d.cell_count[R->c0 + cc];
-                for (int t = 0; t < cnt; ++t) {
-                    const int j = d.cell_list[start + t];
-                    if (j == p) continue;
-                    const int4 qj = d.q[j];
-                    const bool ch = chp && is_charged((qj.w >> 8) & 0xff);
-                    int cls;  // 0 none, 1 SR, 2 LR
-                    if (D) {
-                        const double r2 = exact_r2(d, R, p, j);
-                        cls = r2 <= R->r2sr ? 1 : ((ch && r2 <= R->r2lr) ? 2 : 0);
-                    } else {
-                        const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
-                        const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
-                        const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
-                        if (r2 < sr_lo) cls = 1;
-                        else if (r2 > sr_hi && (!ch || r2 > lr_hi)) cls = 0;
-                        else if (r2 > sr_hi && r2 < lr_lo) cls = 2;
-                        else {
-                            const double e2 = exact_r2(d, R, p, j);
-                            cls = e2 <= R->r2sr ? 1 : ((ch && e2 <= R->r2lr) ? 2 : 0);
+    for (int r = 0; r < d.R; ++r) {
+        if (!d.rs[r].rebuild) continue;
+        const RepParams *R = d.rp + r;
+        const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
+        const float sr_lo = R->r2srf * (1.0f - kBand), sr_hi = R->r2srf * (1.0f + kBand);
+        const float lr_lo = R->r2lrf * (1.0f - kBand), lr_hi = R->r2lrf * (1.0f + kBand);
+        for (int p = R->p0 + wid; p < R->p0 + R->npad; p += d.search_warps) {
+            const int c = d.cell_of[p];
+            if (c < 0) {
+                if (lane == 0) { d.n_sr[p] = 0; d.n_lr[p] = 0; }
+                continue;
+            }
+            const int4 qp = d.q[p];
+            const bool chp = is_charged((qp.w >> 8) & 0xff);
+            const int i1 = c / (R->mc[1] * R->mc[2]) + 1, i2 = (c / R->mc[2]) % R->mc[1] + 1, i3 = c % R->mc[2] + 1;
+            int n1[3], n2[3], n3[3];
+            const int m1 = axis_neighbours(i1, R->mc[0], n1);
+            const int m2 = axis_neighbours(i2, R->mc[1], n2);
+            const int m3 = axis_neighbours(i3, R->mc[2], n3);
+            int exl[kExcl];
+            const int nex = d.n_excl[p];
+            for (int t2 = 0; t2 < kExcl; ++t2) exl[t2] = t2 < nex ? d.excl[(size_t)t2 * P + p] : -1;
+            int nsr = 0, nlr = 0;
+            for (int a = 0; a < m1; ++a)
+                for (int b = 0; b < m2; ++b)
+                    for (int e = 0; e < m3; ++e) {
+                        const int cc = (n1[a] - 1) * R->mc[1] * R->mc[2] + (n2[b] - 1) * R->mc[2] + (n3[e] - 1);
+                        const int start = R->p0 + d.cell_start[R->c0 + cc];
+                        const int cnt = d.cell_count[R->c0 + cc];
+                        for (int t0 = 0; t0 < cnt; t0 += 32) {
+                            const int t = t0 + lane;
+                            int cls = 0, j = -1;  // 0 none, 1 SR, 2 LR
+                            if (t < cnt) {
+                                j = d.cell_list[start + t];
+                                if (j != p) {
+                                    const int4 qj = d.qs[start + t];
+                                    const bool ch = chp && is_charged((qj.w >> 8) & 0xff);
+                                    if (D) {
+                                        const double r2 = exact_r2(d, R, p, j);
+                                        cls = r2 <= R->r2sr ? 1 : ((ch && r2 <= R->r2lr) ? 2 : 0);
+                                    } else {
+                                        const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
+                                        const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
+                                        const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
+                                        const float r2 = dx * dx + dy * dy + dz * dz;
+                                        if (r2 < sr_lo) cls = 1;
+                                        else if (r2 > sr_hi && (!ch || r2 > lr_hi)) cls = 0;
+                                        else if (r2 > sr_hi && r2 < lr_lo) cls = 2;
+                                        else {
+                                            const double e2 = exact_r2(d, R, p, j);
+                                            cls = e2 <= R->r2sr ? 1 : ((ch && e2 <= R->r2lr) ? 2 : 0);
+                                        }
+                                    }
+                                }
+                            }
+                            const unsigned bs = __ballot_sync(kFull, cls == 1), bl = __ballot_sync(kFull, cls == 2);
+                            if (cls == 1) {
+                                int m = 0;  // how often the reference subtracts this pair's LJ again
+                                for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
+                                const int pos = nsr + __popc(bs & lt);
+                                if (pos < d.cap_sr) d.nbr_sr[(size_t)pos * P + p] = j | (m << kExclShift);
+                            } else if (cls == 2) {
+                                const int pos = nlr + __popc(bl & lt);
+                                if (pos < d.cap_lr) d.nbr_lr[(size_t)pos * P + p] = j;
+                            }
+                            nsr += __popc(bs);
+                            nlr += __popc(bl);
                         }
                     }
-                    if (cls == 1) {
-                        int m = 0;  // how often the reference subtracts this pair's LJ again
-                        for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
-                        if (nsr < d.cap_sr) d.nbr_sr[(size_t)nsr * P + p] = j | (m << kExclShift);
-                        ++nsr;
-                    } else if (cls == 2) {
-                        if (nlr < d.cap_lr) d.nbr_lr[(size_t)nlr * P + p] = j;
-                        ++nlr;
-                    }
-                }
+            if (lane == 0) {
+                if (nsr > d.cap_sr || nlr > d.cap_lr) atomicOr(&d.rs[r].err, kErrCapacity);
+                d.n_sr[p] = min(nsr, d.cap_sr);
+                d.n_lr[p] = min(nlr, d.cap_lr);
             }
-    if (nsr > d.cap_sr || nlr > d.cap_lr) atomicOr(&d.rs[r].err, kErrCapacity);
-    d.n_sr[p] = min(nsr, d.cap_sr);
-    d.n_lr[p] = min(nlr, d.cap_lr);
+        }
+    }
 }
 
 // hydrogen-bond candidate status and HB_EXCESS (E:1698-1736): a candidate is live
@@ -1207,9 +1246,11 @@ void launch_rebuild(const Dev &d, cudaStream_t s)
     k_cell_assign<<<d.nblk, kBlock, 0, s>>>(d);
     k_cell_scan<<<d.R, 256, 0, s>>>(d);
     k_cell_fill<<<d.nblk, kBlock, 0, s>>>(d);
-    k_cell_sort<<<(d.C + 127) / 128, 128, 0, s>>>(d);
-    if (d.fp64) k_pair_search<true><<<d.nblk, kBlock, 0, s>>>(d);
-    else k_pair_search<false><<<d.nblk, kBlock, 0, s>>>(d);
+    const int cell_blocks = (d.C * 32 + 127) / 128;
+    if (d.fp64) k_cell_order<true><<<cell_blocks, 128, 0, s>>>(d);
+    else k_cell_order<false><<<cell_blocks, 128, 0, s>>>(d);
+    if (d.fp64) k_pair_search<true><<<d.search_warps / 4, 128, 0, s>>>(d);
+    else k_pair_search<false><<<d.search_warps / 4, 128, 0, s>>>(d);
     k_hb_rebuild<<<d.R, 256, 0, s>>>(d);
 }
 

@@ -21,6 +21,8 @@ struct Dev {
     double *gnoise;             // R x kNoise
     // cells
     int *cell_of, *cell_count, *cell_start, *cell_fill, *cell_list;
+    int4 *qs;                   // packed positions in cell order (qs[slot] = q[cell_list[slot]])
+    int search_warps;           // warps of the pair-search grid
     // neighbour lists, column-major: nbr[k * P + p]
     int *nbr_sr, *n_sr, *nbr_lr, *n_lr;
     int cap_sr, cap_lr;
