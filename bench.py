@@ -241,6 +241,12 @@ def gpu_arm(args):
         value = world * N_REPLICAS * K / (ms / 1000.0)
         launches = K * 11
 
+        if not args.extras:
+            if rank == 0:
+                print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "steps": K,
+                                  "ms_per_step": ms_per_step, "note": "timed loop only (--no-extras)"}), flush=True)
+            return
+
         # end to end through the C ABI with host buffers: every 100 steps a state
         # upload from pinned host memory and a frame (positions + energies) read back
         e2e = None
@@ -334,6 +340,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="stop after the timed loop (no e2e, stage timing, plain path): for profiler runs")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
