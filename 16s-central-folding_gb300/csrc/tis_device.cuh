@@ -24,6 +24,14 @@ constexpr float kFixLimit = 1.0e9f;  // |contribution| clamp (int64 range / 2^32
 constexpr int kExcl = 8;             // bonded (1-2, 1-3) partners stored per particle
 constexpr int kExclShift = 30;       // SR list entry: partner | (exclusion multiplicity << 30)
 constexpr int kIdxMask = (1 << kExclShift) - 1;
+constexpr int kLanes = 4;            // threads per particle in the pair kernels
+
+// neighbour slot k of particle p: chunks of four slots per particle, chunk-major,
+// so the four threads of a particle read 16 contiguous bytes and a warp 128
+__host__ __device__ inline size_t nb_idx(int k, int p, int P)
+{
+    return (((size_t)(k >> 2) * (size_t)P + (size_t)p) << 2) + (size_t)(k & 3);
+}
 
 enum ErrBits : int { kErrCapacity = 1, kErrNonFinite = 2, kErrRange = 4 };
 
@@ -41,6 +49,7 @@ struct RepParams {
     double mass[10], k1[10], k2[10], sigma[10], vcap[10];
     // pair tables, 1..45 (E:2908-2938); dm = D_LJ - 1.5852
     float dlj2[46], dm[46], flj[46], elj[46], d2min[46], qclb[46];
+    float ljkeep2[46];           // (D_LJ + skin)^2 with a 1e-5 margin: pruned-list radius of uncharged pairs
     double dlj2_d[46], dlj_d[46], flj_d[46], elj_d[46], d2min_d[46], qclb_d[46];
     unsigned long long seed;
     int bt0, bt1, s30, s31, s20, s21, hb0, hb1, hba0, hba1, ca0, ca1;

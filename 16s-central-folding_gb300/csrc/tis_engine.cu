@@ -351,6 +351,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
                 R.elj[J] = (float)El;
                 R.d2min[J] = (float)dmin;
                 R.qclb[J] = (float)(Q * lB);
+                R.ljkeep2[J] = (float)((Dl + prm.skin) * (Dl + prm.skin) * (1.0 + 1e-5));
             }
         R.seed = (unsigned long long)scalar_i64(s, "seed", r + 1);
 
@@ -523,8 +524,8 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     double rmax_lr = 0;
     for (auto &R : rp) rmax_lr = std::max(rmax_lr, sqrt(R.r2lr));
     const double rsr = prm.sr + prm.skin;
-    int cap_sr = prm.cap_sr > 0 ? prm.cap_sr : std::max(128, round_up((int)(10 * max_rho * 4.0 / 3.0 * pi * rsr * rsr * rsr), 32));
-    int cap_lr = prm.cap_lr > 0 ? prm.cap_lr
+    int cap_sr = prm.cap_sr > 0 ? round_up(prm.cap_sr, 4) : std::max(128, round_up((int)(10 * max_rho * 4.0 / 3.0 * pi * rsr * rsr * rsr), 32));
+    int cap_lr = prm.cap_lr > 0 ? round_up(prm.cap_lr, 4)
                                 : std::max(96, round_up((int)(10 * max_rho_ch * 4.0 / 3.0 * pi * rmax_lr * rmax_lr * rmax_lr), 32));
 
     tis::Dev &d = h->dev;
@@ -533,6 +534,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     d.nblk = h->nblk;
     d.C = h->C;
     d.fp64 = prm.precision == TIS_PREC_FP64;
+    d.full_lists = prm.full_lists ? 1 : 0;
     d.noise = prm.noise;
     d.cap_sr = cap_sr;
     d.cap_lr = cap_lr;
@@ -682,13 +684,15 @@ int tis_get_pairs(tis_handle *h, int r, int which, int32_t *pairs, int64_t cap, 
     const int *cnt = which ? h->dev.n_lr : h->dev.n_sr;
     std::vector<int> c(hr.npad), lst((size_t)capl * hr.npad);
     TIS_CUDA(cudaMemcpyAsync(c.data(), cnt + hr.p0, sizeof(int) * hr.npad, cudaMemcpyDeviceToHost, h->stream));
-    TIS_CUDA(cudaMemcpy2DAsync(lst.data(), sizeof(int) * hr.npad, nbr + hr.p0, sizeof(int) * h->P, sizeof(int) * hr.npad,
-                               capl, cudaMemcpyDeviceToHost, h->stream));
+    // chunk-major slots: chunk k/4 of the replica's particles is 4*npad contiguous ints
+    TIS_CUDA(cudaMemcpy2DAsync(lst.data(), sizeof(int) * 4 * hr.npad, nbr + tis::nb_idx(0, hr.p0, h->P),
+                               sizeof(int) * 4 * (size_t)h->P, sizeof(int) * 4 * hr.npad, capl / 4,
+                               cudaMemcpyDeviceToHost, h->stream));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
     std::vector<std::pair<int, int>> pr;
     for (int i = 0; i < hr.n; ++i)
         for (int k = 0; k < c[i]; ++k) {
-            const int j = (lst[(size_t)k * hr.npad + i] & tis::kIdxMask) - hr.p0;
+            const int j = (lst[tis::nb_idx(k, i, hr.npad)] & tis::kIdxMask) - hr.p0;
             if (i < j) pr.emplace_back(i, j);
         }
     std::sort(pr.begin(), pr.end());

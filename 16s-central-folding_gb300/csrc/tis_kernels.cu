@@ -300,14 +300,14 @@ __global__ void __launch_bounds__(kBlock) k_quantize(Dev d)
 // pair forces over the full (both-direction) neighbour lists
 // ---------------------------------------------------------------------------
 template <bool D, bool LR, bool EN, bool EX>
-__global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
+__global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
 {
     const int r = d.blk_rep[blockIdx.x];
     const RepParams *R = d.rp + r;
     if (LR && !force_all && !d.rs[r].lr_now) return;
     __shared__ float s_dlj2[46], s_dm[46], s_flj[46], s_qclb[46];
     if (!D) {
-        for (int t = threadIdx.x; t < 46; t += kBlock) {
+        for (int t = threadIdx.x; t < 46; t += blockDim.x) {
             s_dlj2[t] = R->dlj2[t];
             s_dm[t] = R->dm[t];
             s_flj[t] = R->flj[t];
@@ -315,7 +315,9 @@ __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
         }
         __syncthreads();
     }
-    const int p = blockIdx.x * kBlock + threadIdx.x;
+    // four threads per particle: slot k of the list goes to thread k % 4
+    const int lane4 = threadIdx.x & (kLanes - 1);
+    const int p = blockIdx.x * kBlock + (threadIdx.x >> 2);
     const int P = d.P;
     const int4 qp = d.q[p];
     const int tp = qp.w & 0xff, kp = (qp.w >> 8) & 0xff, act = (qp.w >> 16) & 1;
@@ -328,8 +330,8 @@ __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
         long long ax = 0, ay = 0, az = 0;
         const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
         const float rc2 = R->rc2f, lo = rc2 * (1.0f - kBand), hi = rc2 * (1.0f + kBand);
-        for (int k = 0; k < cnt; ++k) {
-            const int raw = __ldg(nbr + (size_t)k * P + p);
+        for (int k = lane4; k < cnt; k += kLanes) {
+            const int raw = __ldg(nbr + nb_idx(k, p, P));
             const int j = raw & kIdxMask;
             const float ljw = EX ? (float)(1 - (raw >> kExclShift)) : 1.0f;
             const int4 qj = __ldg(d.q + j);
@@ -370,14 +372,21 @@ __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
                 az += to_fix(F * dz, err);
             }
         }
-        unsigned long long *out = LR ? d.flr : d.f;
-        out[p] = (unsigned long long)ax;
-        out[P + p] = (unsigned long long)ay;
-        out[2 * P + p] = (unsigned long long)az;
+        for (int o = 1; o < kLanes; o <<= 1) {
+            ax += __shfl_xor_sync(kFull, ax, o);
+            ay += __shfl_xor_sync(kFull, ay, o);
+            az += __shfl_xor_sync(kFull, az, o);
+        }
+        if (lane4 == 0) {
+            unsigned long long *out = LR ? d.flr : d.f;
+            out[p] = (unsigned long long)ax;
+            out[P + p] = (unsigned long long)ay;
+            out[2 * P + p] = (unsigned long long)az;
+        }
     } else {
         double ax = 0, ay = 0, az = 0;
-        for (int k = 0; k < cnt; ++k) {
-            const int raw = __ldg(nbr + (size_t)k * P + p);
+        for (int k = lane4; k < cnt; k += kLanes) {
+            const int raw = __ldg(nbr + nb_idx(k, p, P));
             const int j = raw & kIdxMask;
             const double ljw = EX ? (double)(1 - (raw >> kExclShift)) : 1.0;
             const int tj = d.q[j].w & 0xff, kj = (d.q[j].w >> 8) & 0xff;
@@ -411,10 +420,17 @@ __global__ void __launch_bounds__(kBlock) k_pair(Dev d, int force_all)
             ay += v[1] * F;
             az += v[2] * F;
         }
-        double *out = (double *)(LR ? d.flr : d.f);
-        out[p] = ax;
-        out[P + p] = ay;
-        out[2 * P + p] = az;
+        for (int o = 1; o < kLanes; o <<= 1) {
+            ax += __shfl_xor_sync(kFull, ax, o);
+            ay += __shfl_xor_sync(kFull, ay, o);
+            az += __shfl_xor_sync(kFull, az, o);
+        }
+        if (lane4 == 0) {
+            double *out = (double *)(LR ? d.flr : d.f);
+            out[p] = ax;
+            out[P + p] = ay;
+            out[2 * P + p] = az;
+        }
     }
     if (EN) {
         if (!LR) atomicAdd(d.eterm + r * kNE + 0, e_lj);
@@ -1067,6 +1083,13 @@ __global__ void __launch_bounds__(128) k_pair_search(Dev d)
                                 if (j != p) {
                                     const int4 qj = d.qs[start + t];
                                     const bool ch = chp && is_charged((qj.w >> 8) & 0xff);
+                                    float r2f;
+                                    {
+                                        const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
+                                        const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
+                                        const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
+                                        r2f = dx * dx + dy * dy + dz * dz;
+                                    }
                                     if (D) {
                                         const double r2 = exact_r2(d, R, p, j);
                                         cls = r2 <= R->r2sr ? 1 : ((ch && r2 <= R->r2lr) ? 2 : 0);
@@ -1083,6 +1106,11 @@ __global__ void __launch_bounds__(128) k_pair_search(Dev d)
                                             cls = e2 <= R->r2sr ? 1 : ((ch && e2 <= R->r2lr) ? 2 : 0);
                                         }
                                     }
+                                    // pruned list: a pair with an uncharged bead can only exert LJ, which
+                                    // vanishes beyond D_LJ; the skin keeps it exact until the next rebuild
+                                    if (cls == 1 && !d.full_lists && !ch &&
+                                        r2f > R->ljkeep2[jn12(qp.w & 0xff, qj.w & 0xff)])
+                                        cls = 0;
                                 }
                             }
                             const unsigned bs = __ballot_sync(kFull, cls == 1), bl = __ballot_sync(kFull, cls == 2);
@@ -1090,10 +1118,10 @@ __global__ void __launch_bounds__(128) k_pair_search(Dev d)
                                 int m = 0;  // how often the reference subtracts this pair's LJ again
                                 for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
                                 const int pos = nsr + __popc(bs & lt);
-                                if (pos < d.cap_sr) d.nbr_sr[(size_t)pos * P + p] = j | (m << kExclShift);
+                                if (pos < d.cap_sr) d.nbr_sr[nb_idx(pos, p, P)] = j | (m << kExclShift);
                             } else if (cls == 2) {
                                 const int pos = nlr + __popc(bl & lt);
-                                if (pos < d.cap_lr) d.nbr_lr[(size_t)pos * P + p] = j;
+                                if (pos < d.cap_lr) d.nbr_lr[nb_idx(pos, p, P)] = j;
                             }
                             nsr += __popc(bs);
                             nlr += __popc(bl);
@@ -1193,13 +1221,13 @@ void launch_quantize(const Dev &d, cudaStream_t s) { k_quantize<<<d.nblk, kBlock
 void launch_pair_sr(const Dev &d, cudaStream_t s, bool en, bool ex)
 {
     if (d.fp64) {
-        if (en) k_pair<true, false, true, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
-        else if (ex) k_pair<true, false, false, true><<<d.nblk, kBlock, 0, s>>>(d, 1);
-        else k_pair<true, false, false, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        if (en) k_pair<true, false, true, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
+        else if (ex) k_pair<true, false, false, true><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
+        else k_pair<true, false, false, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
     } else {
-        if (en) k_pair<false, false, true, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
-        else if (ex) k_pair<false, false, false, true><<<d.nblk, kBlock, 0, s>>>(d, 1);
-        else k_pair<false, false, false, false><<<d.nblk, kBlock, 0, s>>>(d, 1);
+        if (en) k_pair<false, false, true, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
+        else if (ex) k_pair<false, false, false, true><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
+        else k_pair<false, false, false, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
     }
 }
 
@@ -1207,11 +1235,11 @@ void launch_pair_lr(const Dev &d, cudaStream_t s, bool en, bool force_all)
 {
     const int fa = force_all ? 1 : 0;
     if (d.fp64) {
-        if (en) k_pair<true, true, true, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
-        else k_pair<true, true, false, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
+        if (en) k_pair<true, true, true, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, fa);
+        else k_pair<true, true, false, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, fa);
     } else {
-        if (en) k_pair<false, true, true, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
-        else k_pair<false, true, false, false><<<d.nblk, kBlock, 0, s>>>(d, fa);
+        if (en) k_pair<false, true, true, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, fa);
+        else k_pair<false, true, false, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, fa);
     }
 }
 

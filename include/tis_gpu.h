@@ -115,7 +115,11 @@ typedef struct tis_run_params {
     int32_t device;        /* CUDA device ordinal */
     int32_t use_graph;     /* 1: tis_step replays a captured CUDA graph */
     int32_t graph_steps;   /* steps per captured graph (0: default) */
-    int32_t reserved[6];
+    int32_t full_lists;    /* 1: keep every SR pair within sr+skin (the reference's SR list, E:1626);
+                              0 (default): a pair with a sugar or base bead is kept only within its
+                              LJ range plus the skin, the only pairs that can exert a force before
+                              the next rebuild */
+    int32_t reserved[5];
 } tis_run_params;
 
 int tis_run_params_default(tis_run_params *p);

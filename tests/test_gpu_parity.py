@@ -42,7 +42,7 @@ def test_lists_bit_exact(systems, case, prec_name, prec, tol):
     s = systems[case]
     o = _oracle(s)
     o.populate_lists()
-    e = Engine([s], precision=prec)
+    e = Engine([s], precision=prec, full_lists=1)
     e.populate_lists()
     c, dims = e.cells(0)
     oc, od = o.cells()
@@ -54,6 +54,44 @@ def test_lists_bit_exact(systems, case, prec_name, prec, tol):
     ost, oex = o.hb()
     assert np.array_equal(st, ost)
     assert np.array_equal(ex, oex)
+
+
+def _d_lj(sd, ti, tj):
+    """D_LJ per type pair (E:2918-2926): 3.2 A among RNA beads, else R_i + R_j."""
+    if ti <= 6 and tj <= 6:
+        return 3.2
+    return sd["rlj"][ti - 1] + sd["rlj"][tj - 1]
+
+
+@pytest.mark.parametrize("case", ["small", "central"])
+def test_pruned_sr_list_keeps_every_interacting_pair(systems, case):
+    """The step's SR list (full_lists=0) is the reference's SR set minus pairs with
+    a sugar or base bead that lie beyond their LJ range plus the skin, which can
+    exert no force before the next rebuild."""
+    s = systems[case]
+    sd = s.to_dict()
+    o = _oracle(s)
+    o.populate_lists()
+    full = pair_set(o.pairs(0))
+    e = Engine([s])
+    e.populate_lists()
+    pruned = e.pairs(0, 0)
+    fset = set(map(tuple, full))
+    assert all(tuple(pq) in fset for pq in pruned)
+    pset = set(map(tuple, pruned))
+    X = np.stack([sd["x"], sd["y"], sd["z"]], 1)
+    L = sd["box"]
+    kind, typ = sd["kind"], sd["type"]
+    need = 0
+    for i, j in full:
+        charged = kind[i] not in (1, 2) and kind[j] not in (1, 2)
+        dv = X[i] - X[j]
+        dv -= L * np.round(dv / L)
+        r = np.sqrt(dv @ dv)
+        if charged or r < (_d_lj(sd, typ[i], typ[j]) + 3.0) * (1 - 1e-4):
+            need += 1
+            assert (i, j) in pset, (i, j, r)
+    assert len(pruned) < len(full) and len(pruned) >= need
 
 
 def _frame(s, case, frame):
@@ -260,7 +298,7 @@ def test_nonfinite_state_is_reported(systems):
 
 def test_small_capacity_grows_at_list_build(systems):
     s = systems["central"]
-    e = Engine([s], cap_sr=8, cap_lr=8)
+    e = Engine([s], cap_sr=8, cap_lr=8, full_lists=1)
     e.populate_lists()  # overflows, grows, rebuilds
     o = _oracle(s)
     o.populate_lists()
