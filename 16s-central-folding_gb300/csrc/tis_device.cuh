@@ -64,6 +64,7 @@ struct RepState {
     double progress;
     int rebuild, lr_now, err, n_active;
     double e2hb, e3hb, e2st, e3st;
+    double e2st_acc, e3st_acc;   // stacking energies being summed in the current step
 };
 
 // ---- Philox-4x32-10 (Salmon et al., SC'11) --------------------------------

@@ -601,7 +601,28 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     d.hb_idx = ih; d.hb_nat = nh; d.hb_E = eh; d.hb_dode = dh; d.hb_aoff = ao; d.hb_aidx = ai;
     d.hba_val = hv; d.hba_coff = co; d.hba_cidx = ci; d.hba_n = hn; d.ca_list = ca;
     const size_t nst2 = st2_E.size(), nst3 = st3_E.size(), nhb = hb_E.size(), nhba = hba_val.size();
-    if ((rc = dalloc(O, &d.st2_off_flag, nst2)) || (rc = dalloc(O, &d.st_energy, nst3)) ||
+    d.nbt = (int)bt_idx.size();
+    d.nst3 = (int)nst3;
+    d.nst2 = (int)nst2;
+    {  // secondary stack -> the tertiary stacks whose site can switch it off (E:1960-1981)
+        std::vector<std::vector<int>> offby(nst2);
+        for (int r = 0; r < h->R; ++r)
+            for (int k = h->rep[r].s30; k < h->rep[r].s31; ++k)
+                for (int sd = 0; sd < 2; ++sd) {
+                    const int t = st3_off[2 * k + sd];
+                    if (t >= 0) offby[h->rep[r].s20 + t].push_back(k);
+                }
+        std::vector<int> off{0}, idx;
+        for (auto &v : offby) {
+            for (int k : v) idx.push_back(k);
+            off.push_back((int)idx.size());
+        }
+        int *d_off = nullptr, *d_idx = nullptr;
+        if ((rc = dupload(O, &d_off, off)) || (rc = dupload(O, &d_idx, idx))) return bail(rc);
+        d.st2_offby_off = d_off;
+        d.st2_offby_idx = d_idx;
+    }
+    if ((rc = dalloc(O, &d.st_energy, nst3)) ||
         (rc = dalloc(O, &d.hb_status, nhb)) || (rc = dalloc(O, &d.hb_excess, nhba)) ||
         (rc = dalloc(O, &d.excess, nhba)) || (rc = dalloc(O, &d.hb_active, nhb)) ||
         (rc = dalloc(O, &d.hb_K, (size_t)kscr)) || (rc = dalloc(O, &d.hb_A, ca_list.size())) ||

@@ -3,10 +3,10 @@
 // One step of every replica (E: = src/16SCD_Mg_Cl_K_COPY_fast.cpp):
 //   k_pair_sr     SR_interactions_lists      E:1783-1847   per particle, full neighbour list
 //   k_pair_lr     LR_interactions_lists      E:1851-1907   every lr_interval steps or after a rebuild
-//   k_topology    stacking_interactions      E:1911-2141   one block per replica:
-//                 hydrogen_bonds_interactions E:2145-2350  energies, valence-limited MC, forces
-//                 polymer_constraints        E:2354-2520
-//                 full_forces (the Gaussians) E:2590-2611
+//   k_bonded_stack polymer_constraints      E:2354-2520   one thread per term, all replicas
+//                  stacking_interactions    E:1911-2141
+//   k_hbond       hydrogen_bonds_interactions E:2145-2350  one block per replica:
+//                 energies, valence-limited MC, forces; full_forces' Gaussians E:2590-2611
 //   k_integrate   full_forces (application) + move_rigid_units + leap_frog_move_atom + adjust_box
 //                                             E:2612-2732, E:570-642
 //   k_control     check_shifts               E:1741-1776
@@ -555,13 +555,131 @@ __global__ void k_noise(Dev d)
 }
 
 // ---------------------------------------------------------------------------
-// topology terms of one replica per block: bonded, stacking, hydrogen bonds
-// with the valence-limited Monte Carlo, and this step's Gaussians
+// bonded terms and stacks of every replica, one thread per term
 // ---------------------------------------------------------------------------
 constexpr int kTopoThreads = 256;
 
+// LJ force of an excluded (bonded) pair, as reduce_forces subtracts it (E:880-897)
 template <bool D, bool EN>
-__global__ void __launch_bounds__(kTopoThreads) k_topology(Dev d, int mask, int make_noise, int excl_in_list)
+__device__ void exclusion_lj(const Dev &d, const RepParams *R, const Pos<D> &P, Acc<D> &A, int a, int ex,
+                             double &e_excl)
+{
+    using Rl = Real<D>;
+    const int ta = d.q[a].w & 0xff, tb = d.q[ex].w & 0xff;
+    const int J = jn12(ta, tb);
+    V3<Rl> v = P.vec(ex, a);  // x_a - x_ex, minimum image
+    if (D) {
+        double w[3];
+        exact_vec(d, R, a, ex, w);
+        v = V3<Rl>{(Rl)w[0], (Rl)w[1], (Rl)w[2]};
+    }
+    const Rl r2 = dot(v, v);
+    if (!(r2 <= (Rl)(D ? R->dlj2_d[J] : R->dlj2[J]))) return;
+    const Rl rr = sqrt_(r2);
+    const Rl dr = D ? (Rl)(rr + kSig0 - R->dlj_d[J]) : (Rl)(rr - R->dm[J]);
+    const Rl s = Rl(1.5852) / dr;
+    const Rl s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+    const Rl F = (Rl)(D ? R->flj_d[J] : R->flj[J]) * (s14 - s8) * dr / rr;
+    if (EN) {
+        double e;
+        if ((double)r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
+        else {
+            const Rl s6 = s4 * s2, s12 = s6 * s6;
+            e = (double)((Rl)(D ? R->elj_d[J] : R->elj[J]) * (s12 - Rl(2) * s6 + Rl(1)));
+        }
+        e_excl -= e;
+    }
+    if (F != Rl(0)) {
+        const V3<Rl> g = (Rl(-1) * F) * v;
+        A.add(a, g);
+        A.add(ex, Rl(-1) * g);
+    }
+}
+
+// polymer_constraints (E:2354-2520), then stacking_interactions (E:1911-2141):
+// items [0, nbt) are bonded terms, then tertiary stacks, then secondary stacks.
+// A secondary stack is off this step when a tertiary stack sharing one of its
+// sites (ST_EXCESS == 1) is within 10 A of its native distance (E:1960-1981);
+// each secondary stack checks the few tertiary stacks that can do that.
+template <bool D, bool EN>
+__global__ void __launch_bounds__(kTopoThreads) k_bonded_stack(Dev d, int mask, int excl_in_list)
+{
+    using Rl = Real<D>;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int r, kind;  // kind: 0 bonded, 1 tertiary, 2 secondary
+    int item;
+    if (t < d.nbt) { kind = 0; item = t; r = d.rep_of[d.bt_idx[t].x]; }
+    else if (t < d.nbt + d.nst3) { kind = 1; item = t - d.nbt; r = d.rep_of[d.st3_idx[6 * item]]; }
+    else if (t < d.nbt + d.nst3 + d.nst2) { kind = 2; item = t - d.nbt - d.nst3; r = d.rep_of[d.st2_idx[7 * item]]; }
+    else return;
+    if ((kind == 0 && !(mask & 4)) || (kind > 0 && !(mask & 8))) return;
+    const RepParams *R = d.rp + r;
+    const Pos<D> P = make_pos<D>(d, R);
+    Acc<D> A;
+    A.f = (decltype(A.f))d.f;
+    A.P = d.P;
+    A.err = 0;
+    double e_excl = 0;
+    if (kind == 0) {
+        const int4 id = d.bt_idx[item];
+        const double2 par = d.bt_par[item];
+        const int ex = id.w == 0 ? id.y : id.z;  // excluded pair partner of id.x
+        if (id.w == 0) bond_force<D>(P, A, id.x, id.y, (Rl)par.x, (Rl)par.y);
+        else angle_force<D>(P, A, id.x, id.y, id.z, (Rl)par.x, (Rl)par.y, false);
+        if (!excl_in_list || EN) exclusion_lj<D, EN>(d, R, P, A, id.x, ex, e_excl);
+        if (EN) {
+            double *e = d.eterm + r * kNE;
+            if (id.w == 0) {
+                const Rl rr = distance<D>(P, id.x, id.y);
+                atomicAdd(e + 3, (double)((Rl)par.x * (rr - (Rl)par.y) * (rr - (Rl)par.y)));
+            } else {
+                const Rl th = angle_of<D>(P, id.x, id.y, id.z);
+                atomicAdd(e + 4, (double)((Rl)par.x * (th - (Rl)par.y) * (th - (Rl)par.y)));
+            }
+            if (e_excl != 0) atomicAdd(e + 5, e_excl);
+        }
+    } else if (kind == 1) {
+        const int *id = d.st3_idx + 6 * item;
+        const double *nat = d.st3_nat + 6 * item;
+        const Rl rdev = distance<D>(P, id[1], id[4]) - (Rl)nat[0];
+        int code;
+        const Rl Dn = six_q<D>(P, id, nat, rdev, Rl(1), code);
+        const Rl E = (Rl)d.st3_E[item] / Dn;
+        six_force<D>(P, A, id, nat, code, -E / Dn);
+        d.st_energy[item] = (double)E;
+        atomicAdd(EN ? d.eterm + r * kNE + 7 : &d.rs[r].e3st_acc, (double)E);
+    } else {
+        for (int u = d.st2_offby_off[item]; u < d.st2_offby_off[item + 1]; ++u) {
+            const int k = d.st2_offby_idx[u];
+            const int *tid = d.st3_idx + 6 * k;
+            if (distance<D>(P, tid[1], tid[4]) - (Rl)d.st3_nat[6 * k] < Rl(10)) return;
+        }
+        const int *id = d.st2_idx + 7 * item;  // k_10 k00 k01 k10 k20 k21 k30
+        const Rl rr = distance<D>(P, id[2], id[5]);
+        const Rl p1 = dihedral_of<D>(P, id[0], id[1], id[3], id[4]);
+        const Rl p2 = dihedral_of<D>(P, id[6], id[4], id[3], id[1]);
+        const Rl p10 = psi_shift<Rl>(Rl(-2.58684), psi_branch<Rl>(p1, Rl(-2.58684)));
+        const Rl p20 = psi_shift<Rl>(Rl(3.07135), psi_branch<Rl>(p2, Rl(3.07135)));
+        const Rl r0 = (Rl)d.st2_r0[item];
+        Rl Dn = Rl(1) + Rl(1.4) * (rr - r0) * (rr - r0);
+        Dn += Rl(4) * (p1 - p10) * (p1 - p10);
+        Dn += Rl(4) * (p2 - p20) * (p2 - p20);
+        const Rl E = (Rl)d.st2_E[item] / Dn;
+        const Rl w = -E / Dn;
+        bond_force<D>(P, A, id[2], id[5], Rl(1.4) * w, r0);
+        dihedral_force<D>(P, A, id[0], id[1], id[3], id[4], Rl(4) * w, p10);
+        dihedral_force<D>(P, A, id[6], id[4], id[3], id[1], Rl(4) * w, p20);
+        atomicAdd(EN ? d.eterm + r * kNE + 6 : &d.rs[r].e2st_acc, (double)E);
+    }
+    if (A.err) atomicOr(&d.rs[r].err, A.err);
+}
+
+// ---------------------------------------------------------------------------
+// hydrogen bonds of one replica per block: energies, the valence-limited Monte
+// Carlo, forces; then this step's Gaussians and the recentring shift
+// ---------------------------------------------------------------------------
+template <bool D, bool EN>
+__global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int make_noise)
 {
     using Rl = Real<D>;
     const int r = blockIdx.x;
@@ -573,108 +691,11 @@ __global__ void __launch_bounds__(kTopoThreads) k_topology(Dev d, int mask, int 
     A.P = d.P;
     A.err = 0;
     __shared__ unsigned long long s_ctr;
-    __shared__ double s_red[8 * 32];
+    __shared__ double s_red[2 * 32];
     if (threadIdx.x == 0) s_ctr = S->ctr;
-    double e_bond = 0, e_angle = 0, e_excl = 0, e2st = 0, e3st = 0, e2hb = 0, e3hb = 0;
-
-    // ---- polymer_constraints (E:2354-2520) ----
-    if (mask & 4) {
-        for (int t = R->bt0 + threadIdx.x; t < R->bt1; t += blockDim.x) {
-            const int4 id = d.bt_idx[t];
-            const double2 par = d.bt_par[t];
-            const int ex = id.w == 0 ? id.y : id.z;  // excluded pair partner of id.x
-            if (id.w == 0) bond_force<D>(P, A, id.x, id.y, (Rl)par.x, (Rl)par.y);
-            else angle_force<D>(P, A, id.x, id.y, id.z, (Rl)par.x, (Rl)par.y, false);
-            if (excl_in_list && !EN) continue;  // the SR kernel already left this pair's LJ out
-            // subtract the LJ force of the excluded pair (reduce_forces, E:880-897)
-            const int ta = d.q[id.x].w & 0xff, tb = d.q[ex].w & 0xff;
-            const int J = jn12(ta, tb);
-            V3<Rl> v = P.vec(ex, id.x);  // x_a - x_ex, minimum image
-            if (D) {
-                double w[3];
-                exact_vec(d, R, id.x, ex, w);
-                v = V3<Rl>{(Rl)w[0], (Rl)w[1], (Rl)w[2]};
-            }
-            const Rl r2 = dot(v, v);
-            Rl F = 0;
-            if (r2 <= (Rl)(D ? R->dlj2_d[J] : R->dlj2[J])) {
-                const Rl rr = sqrt_(r2);
-                const Rl dr = D ? (Rl)(rr + kSig0 - R->dlj_d[J]) : (Rl)(rr - R->dm[J]);
-                const Rl s = Rl(1.5852) / dr;
-                const Rl s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
-                F = (Rl)(D ? R->flj_d[J] : R->flj[J]) * (s14 - s8) * dr / rr;
-                if (EN) {
-                    double e;
-                    if ((double)r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
-                    else {
-                        const Rl s6 = s4 * s2, s12 = s6 * s6;
-                        e = (double)((Rl)(D ? R->elj_d[J] : R->elj[J]) * (s12 - Rl(2) * s6 + Rl(1)));
-                    }
-                    e_excl -= e;
-                }
-            }
-            if (F != Rl(0)) {
-                const V3<Rl> g = (Rl(-1) * F) * v;
-                A.add(id.x, g);
-                A.add(ex, Rl(-1) * g);
-            }
-            if (EN) {
-                if (id.w == 0) {
-                    const Rl rr = distance<D>(P, id.x, id.y);
-                    e_bond += (double)((Rl)par.x * (rr - (Rl)par.y) * (rr - (Rl)par.y));
-                } else {
-                    const Rl th = angle_of<D>(P, id.x, id.y, id.z);
-                    e_angle += (double)((Rl)par.x * (th - (Rl)par.y) * (th - (Rl)par.y));
-                }
-            }
-        }
-    }
-
-    // ---- stacking_interactions (E:1911-2141) ----
-    if (mask & 8) {
-        for (int k = R->s20 + threadIdx.x; k < R->s21; k += blockDim.x) d.st2_off_flag[k] = 0;
-        __syncthreads();
-        for (int k = R->s30 + threadIdx.x; k < R->s31; k += blockDim.x) {
-            const int *id = d.st3_idx + 6 * k;
-            if (distance<D>(P, id[1], id[4]) - (Rl)d.st3_nat[6 * k] < Rl(10)) {
-                for (int s = 0; s < 2; ++s) {
-                    const int t = d.st3_off[2 * k + s];
-                    if (t >= 0) d.st2_off_flag[R->s20 + t] = 1;
-                }
-            }
-        }
-        __syncthreads();
-        for (int k = R->s30 + threadIdx.x; k < R->s31; k += blockDim.x) {
-            const int *id = d.st3_idx + 6 * k;
-            const double *nat = d.st3_nat + 6 * k;
-            const Rl rdev = distance<D>(P, id[1], id[4]) - (Rl)nat[0];
-            int code;
-            const Rl Dn = six_q<D>(P, id, nat, rdev, Rl(1), code);
-            const Rl E = (Rl)d.st3_E[k] / Dn;
-            six_force<D>(P, A, id, nat, code, -E / Dn);
-            e3st += (double)E;
-            d.st_energy[k] = (double)E;
-        }
-        for (int k = R->s20 + threadIdx.x; k < R->s21; k += blockDim.x) {
-            if (d.st2_off_flag[k]) continue;
-            const int *id = d.st2_idx + 7 * k;  // k_10 k00 k01 k10 k20 k21 k30
-            const Rl rr = distance<D>(P, id[2], id[5]);
-            const Rl p1 = dihedral_of<D>(P, id[0], id[1], id[3], id[4]);
-            const Rl p2 = dihedral_of<D>(P, id[6], id[4], id[3], id[1]);
-            const Rl p10 = psi_shift<Rl>(Rl(-2.58684), psi_branch<Rl>(p1, Rl(-2.58684)));
-            const Rl p20 = psi_shift<Rl>(Rl(3.07135), psi_branch<Rl>(p2, Rl(3.07135)));
-            const Rl r0 = (Rl)d.st2_r0[k];
-            Rl Dn = Rl(1) + Rl(1.4) * (rr - r0) * (rr - r0);
-            Dn += Rl(4) * (p1 - p10) * (p1 - p10);
-            Dn += Rl(4) * (p2 - p20) * (p2 - p20);
-            const Rl E = (Rl)d.st2_E[k] / Dn;
-            const Rl w = -E / Dn;
-            bond_force<D>(P, A, id[2], id[5], Rl(1.4) * w, r0);
-            dihedral_force<D>(P, A, id[0], id[1], id[3], id[4], Rl(4) * w, p10);
-            dihedral_force<D>(P, A, id[6], id[4], id[3], id[1], Rl(4) * w, p20);
-            e2st += (double)E;
-        }
-    }
+    double e2hb = 0, e3hb = 0;
+    const int mask = do_hb ? 16 : 0;
+    __syncthreads();
 
     // ---- hydrogen_bonds_interactions (E:2145-2350) ----
     if (mask & 16) {
@@ -778,16 +799,14 @@ __global__ void __launch_bounds__(kTopoThreads) k_topology(Dev d, int mask, int 
     // ---- full_forces: the step's Gaussians, then the recentring shift ----
     if (make_noise) noise_and_shift<D>(d, r, s_ctr);
 
-    double v[7] = {e2hb, e3hb, e2st, e3st, e_bond, e_angle, e_excl};
-    block_sum<7>(v, s_red);
+    double v[2] = {e2hb, e3hb};
+    block_sum<2>(v, s_red);
     if (threadIdx.x == 0) {
         S->ctr = s_ctr;
-        if (mask & 16) { S->e2hb = v[0]; S->e3hb = v[1]; }
-        if (mask & 8) { S->e2st = v[2]; S->e3st = v[3]; }
+        if (do_hb) { S->e2hb = v[0]; S->e3hb = v[1]; }
         if (EN) {
             double *e = d.eterm + r * kNE;
-            e[3] += v[4]; e[4] += v[5]; e[5] += v[6];
-            e[6] += v[2]; e[7] += v[3]; e[8] += v[0]; e[9] += v[1];
+            e[8] += v[0]; e[9] += v[1];
         }
     }
     if (A.err) atomicOr(&S->err, A.err);
@@ -864,6 +883,10 @@ __global__ void k_control(Dev d)
         S->rebuild = reb;
         const long long kn = S->klok + 1;
         S->lr_now = (R->lr_interval <= 1) || (kn % R->lr_interval == 1) || (S->progress == 0.0);
+        S->e2st = S->e2st_acc;  // stacking energies of the step just finished (E2_STACK, E3_STACK)
+        S->e3st = S->e3st_acc;
+        S->e2st_acc = 0.0;
+        S->e3st_acc = 0.0;
         s_reb = reb;
     }
     __syncthreads();
@@ -1245,13 +1268,27 @@ void launch_pair_lr(const Dev &d, cudaStream_t s, bool en, bool force_all)
 
 void launch_topology(const Dev &d, cudaStream_t s, int mask, bool en, bool make_noise, bool ex)
 {
-    const int mn = make_noise ? 1 : 0, xl = ex ? 1 : 0;
-    if (d.fp64) {
-        if (en) k_topology<true, true><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn, xl);
-        else k_topology<true, false><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn, xl);
-    } else {
-        if (en) k_topology<false, true><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn, xl);
-        else k_topology<false, false><<<d.R, kTopoThreads, 0, s>>>(d, mask, mn, xl);
+    const int xl = ex ? 1 : 0;
+    const int items = d.nbt + d.nst3 + d.nst2;
+    const int blocks = (items + kTopoThreads - 1) / kTopoThreads;
+    if ((mask & (4 | 8)) && blocks > 0) {
+        if (d.fp64) {
+            if (en) k_bonded_stack<true, true><<<blocks, kTopoThreads, 0, s>>>(d, mask, xl);
+            else k_bonded_stack<true, false><<<blocks, kTopoThreads, 0, s>>>(d, mask, xl);
+        } else {
+            if (en) k_bonded_stack<false, true><<<blocks, kTopoThreads, 0, s>>>(d, mask, xl);
+            else k_bonded_stack<false, false><<<blocks, kTopoThreads, 0, s>>>(d, mask, xl);
+        }
+    }
+    const int hb = (mask & 16) ? 1 : 0, mn = make_noise ? 1 : 0;
+    if (hb || mn) {
+        if (d.fp64) {
+            if (en) k_hbond<true, true><<<d.R, kTopoThreads, 0, s>>>(d, hb, mn);
+            else k_hbond<true, false><<<d.R, kTopoThreads, 0, s>>>(d, hb, mn);
+        } else {
+            if (en) k_hbond<false, true><<<d.R, kTopoThreads, 0, s>>>(d, hb, mn);
+            else k_hbond<false, false><<<d.R, kTopoThreads, 0, s>>>(d, hb, mn);
+        }
     }
 }
 
@@ -1286,7 +1323,7 @@ void launch_force_all_rebuild(const Dev &d, cudaStream_t s) { k_force_rebuild<<<
 
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out) { k_rg<<<1, 256, 0, s>>>(d, replica, out); }
 
-// pair SR, pair LR, topology, integrate, control, 6 rebuild kernels
-int kernel_launches_per_step() { return 11; }
+// pair SR, pair LR, bonded+stacking, H-bonds+noise, integrate, control, 6 rebuild kernels
+int kernel_launches_per_step() { return 12; }
 
 }  // namespace tis

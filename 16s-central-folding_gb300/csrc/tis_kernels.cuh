@@ -35,7 +35,8 @@ struct Dev {
     const double2 *bt_par;      // k0, x0
     const int *st3_idx; const double *st3_nat, *st3_E; const int *st3_off;
     const int *st2_idx; const double *st2_r0, *st2_E;
-    int *st2_off_flag;
+    int nbt, nst3, nst2;        // bonded terms, tertiary and secondary stacks of all replicas
+    const int *st2_offby_off, *st2_offby_idx;  // tertiary stacks that can switch each secondary off
     double *st_energy;          // tertiary energies of the last step (for the Contacts file)
     const int *hb_idx; const double *hb_nat, *hb_E; const int *hb_dode;
     const int *hb_aoff, *hb_aidx;   // atoms of every candidate (CSR, global ids)

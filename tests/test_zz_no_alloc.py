@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _reference_lists(s):
-    e = Engine([s])
+    e = Engine([s], full_lists=1)  # the reference's full SR set, as the no-alloc build returns
     e.populate_lists()
     return e.pairs(0, 0), e.pairs(0, 1)
 
