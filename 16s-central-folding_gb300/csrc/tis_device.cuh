@@ -47,6 +47,7 @@ struct RepParams {
     double T, h, lB, rc2, r2sr, r2lr, skin;
     float rc2f, r2srf, r2lrf, Tf;
     double mass[10], k1[10], k2[10], sigma[10], vcap[10];
+    double k2fix[10], k2sig[10];  // K2 * 2^-32 (fixed-point force to velocity), K2 * sigma (noise)
     // pair tables, 1..45 (E:2908-2938); dm = D_LJ - 1.5852
     float dlj2[46], dm[46], flj[46], elj[46], d2min[46], qclb[46];
     float ljkeep2[46];           // (D_LJ + skin)^2 with a 1e-5 margin: pruned-list radius of uncharged pairs
@@ -113,6 +114,11 @@ __device__ inline float bm_radius(uint32_t v)
 }
 
 // ---- fixed point ----------------------------------------------------------
+// round(v * 2^32) as int64 from 32-bit conversions only (64-bit conversions run
+// on GB300's narrow FP64 pipe).  For |v| < 0.5 the product fits int32 and is
+// rounded to nearest; for |v| >= 0.5, v is a multiple of 2^-24, so the split
+// v = floor(v) + frac is exact and frac * 2^32 is an exact integer below 2^32.
+// The result equals __float2ll_rn(v * 2^32) for every |v| < kFixLimit.
 __device__ inline long long to_fix(float v, int &err)
 {
     if (!(fabsf(v) < kFixLimit)) {
@@ -120,7 +126,10 @@ __device__ inline long long to_fix(float v, int &err)
         err |= kErrNonFinite;
         v = v > 0 ? kFixLimit : -kFixLimit;
     }
-    return __float2ll_rn(v * kFixScaleF);
+    if (fabsf(v) < 0.5f) return (long long)__float2int_rn(v * kFixScaleF);
+    const float hi = floorf(v);
+    const unsigned lo = __float2uint_rz((v - hi) * kFixScaleF);
+    return (long long)((unsigned long long)(long long)__float2int_rz(hi) << 32) + (long long)lo;
 }
 
 __device__ inline void atomic_add_fix(unsigned long long *a, long long v)

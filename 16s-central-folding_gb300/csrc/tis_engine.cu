@@ -330,6 +330,8 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
             R.k2[t] = (1.0 - R.k1[t]) / visc;
             R.sigma[t] = sqrt(2.0 * visc * T / hstep);
             R.vcap[t] = m / (300.0 * T);
+            R.k2fix[t] = R.k2[t] / tis::kFixScale;
+            R.k2sig[t] = R.k2[t] * R.sigma[t];
         }
         for (int a = 1; a <= 9; ++a)
             for (int b = a; b <= 9; ++b) {

@@ -477,33 +477,45 @@ __device__ inline double total_force(const Dev &d, int p, int c)
     return (double)t * (1.0 / kFixScale);
 }
 
-// leap_frog_move_atom (E:570-642) with the noise of full_forces (E:2612-2622)
+// leap_frog_move_atom (E:570-642) with the noise of full_forces (E:2612-2622).
+// FP64 mode follows the reference's operation order.  Mixed mode evaluates the
+// same update v' = K1 v + K2 (f + g sigma) as K1 v + (K2 2^-32) f_fix + (K2 sigma) g
+// with fused multiply-adds, and x' = x + (x - x_old) + (v' - v) h; the velocity
+// cap m v'^2 / (300 T) > 1 uses the precomputed m / (300 T) in both modes.
 template <bool D>
 __device__ inline void leap_frog(const Dev &d, const RepParams *R, int r, int p, double xn[3], double vn[3])
 {
     const int t = d.q[p].w & 0xff;
-    double f[3] = {total_force<D>(d, p, 0), total_force<D>(d, p, 1), total_force<D>(d, p, 2)};
-    if (d.noise == 0) {
-        const int k = (p - R->p0 + 1) % 1000;
-        const double *g = d.gnoise + r * kNoise;
-        const double sg = R->sigma[t];
-        f[0] = __dadd_rn(f[0], __dmul_rn(g[k], sg));
-        f[1] = __dadd_rn(f[1], __dmul_rn(g[k + 1000], sg));
-        f[2] = __dadd_rn(f[2], __dmul_rn(g[k + 2000], sg));
-    }
     const double v0[3] = {d.vx[p], d.vy[p], d.vz[p]};
     const double x0[3] = {d.x[p], d.y[p], d.z[p]};
     const double o0[3] = {d.xo[p], d.yo[p], d.zo[p]};
-    for (int c = 0; c < 3; ++c) vn[c] = __dadd_rn(__dmul_rn(R->k1[t], v0[c]), __dmul_rn(R->k2[t], f[c]));
-    double vsq = __dmul_rn(R->mass[t], __dadd_rn(__dadd_rn(__dmul_rn(vn[0], vn[0]), __dmul_rn(vn[1], vn[1])),
-                                                  __dmul_rn(vn[2], vn[2])));
-    vsq = vsq / (300.0 * R->T);
+    const int k = (p - R->p0 + 1) % 1000;
+    const double *g = d.gnoise + r * kNoise;
+    if (D) {
+        double f[3] = {total_force<D>(d, p, 0), total_force<D>(d, p, 1), total_force<D>(d, p, 2)};
+        if (d.noise == 0) {
+            const double sg = R->sigma[t];
+            for (int c = 0; c < 3; ++c) f[c] = __dadd_rn(f[c], __dmul_rn(g[k + 1000 * c], sg));
+        }
+        for (int c = 0; c < 3; ++c) vn[c] = __dadd_rn(__dmul_rn(R->k1[t], v0[c]), __dmul_rn(R->k2[t], f[c]));
+    } else {
+        const double k1 = R->k1[t], kf = R->k2fix[t], kg = d.noise == 0 ? R->k2sig[t] : 0.0;
+        for (int c = 0; c < 3; ++c) {
+            const long long fx = (long long)(__ldcg(d.f + c * d.P + p) + __ldcg(d.flr + c * d.P + p));
+            vn[c] = fma(kg, g[k + 1000 * c], fma(kf, (double)fx, k1 * v0[c]));
+        }
+    }
+    double vsq = R->vcap[t] * (vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
     if (vsq > 1.0) {
         vsq = 1.0 / sqrt(vsq);
         for (int c = 0; c < 3; ++c) vn[c] *= vsq;
     }
-    for (int c = 0; c < 3; ++c)
-        xn[c] = __dadd_rn(__dsub_rn(__dmul_rn(2.0, x0[c]), o0[c]), __dmul_rn(__dsub_rn(vn[c], v0[c]), R->h));
+    if (D) {
+        for (int c = 0; c < 3; ++c)
+            xn[c] = __dadd_rn(__dsub_rn(__dmul_rn(2.0, x0[c]), o0[c]), __dmul_rn(__dsub_rn(vn[c], v0[c]), R->h));
+    } else {
+        for (int c = 0; c < 3; ++c) xn[c] = fma(vn[c] - v0[c], R->h, x0[c] + (x0[c] - o0[c]));
+    }
 }
 
 // full_forces' Gaussians (E:2594-2606) for one replica, then the recentring
@@ -842,8 +854,9 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
         for (int c = 0; c < 3; ++c) {
             const double e = xn[c] - xo[c];
             d2 += e * e;
-            if (!(fabs(xn[c]) < 1.0e6) || !(fabs(vn[c]) < 1.0e6)) err |= kErrNonFinite;
         }
+        if (!(fabs(xn[0]) + fabs(xn[1]) + fabs(xn[2]) + fabs(vn[0]) + fabs(vn[1]) + fabs(vn[2]) < 1.0e6))
+            err |= kErrNonFinite;
         d.x[p] = xn[0]; d.y[p] = xn[1]; d.z[p] = xn[2];
         d.xo[p] = xo[0]; d.yo[p] = xo[1]; d.zo[p] = xo[2];
         d.vx[p] = vn[0]; d.vy[p] = vn[1]; d.vz[p] = vn[2];
