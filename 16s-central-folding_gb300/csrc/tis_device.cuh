@@ -66,6 +66,8 @@ struct RepState {
     int rebuild, lr_now, err, n_active;
     double e2hb, e3hb, e2st, e3st;
     double e2st_acc, e3st_acc;   // stacking energies being summed in the current step
+    unsigned blocks_done;        // integrator blocks finished this step (the last one runs the skin check)
+    unsigned pad_;
 };
 
 // ---- Philox-4x32-10 (Salmon et al., SC'11) --------------------------------

@@ -190,8 +190,7 @@ void enqueue_step(tis_handle *h)
     tis::launch_pair_sr(h->dev, h->stream, false, true);
     tis::launch_pair_lr(h->dev, h->stream, false, false);
     tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true, true);
-    tis::launch_integrate(h->dev, h->stream);
-    tis::launch_control(h->dev, h->stream);
+    tis::launch_integrate(h->dev, h->stream);  // its last block per replica runs the skin check
     tis::launch_rebuild(h->dev, h->stream);
 }
 
@@ -544,6 +543,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, prm.device);
         d.search_warps = std::max(4, sms * 8 * 4);  // 8 blocks of 4 warps per SM
+        d.sm_count = std::max(1, sms);
     }
     auto &O = h->owned;
     int rc = TIS_OK;
@@ -850,7 +850,7 @@ int tis_move_rigid_units(tis_handle *h)
 int tis_check_shifts(tis_handle *h)
 {
     if (!h) return fail(TIS_ERR_ARG, "null handle");
-    tis::launch_control(h->dev, h->stream);
+    // the displacement check itself ran at the end of tis_move_rigid_units
     tis::launch_rebuild(h->dev, h->stream);
     TIS_CUDA(cudaGetLastError());
     return TIS_OK;
@@ -902,8 +902,7 @@ int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
         TIS_CUDA(cudaEventRecord(ev[3], h->stream));
         tis::launch_integrate(h->dev, h->stream);
         TIS_CUDA(cudaEventRecord(ev[4], h->stream));
-        tis::launch_control(h->dev, h->stream);
-        TIS_CUDA(cudaEventRecord(ev[5], h->stream));
+        TIS_CUDA(cudaEventRecord(ev[5], h->stream));  // skin check: fused into the integrator
         tis::launch_rebuild(h->dev, h->stream);
         TIS_CUDA(cudaEventRecord(ev[6], h->stream));
         TIS_CUDA(cudaEventSynchronize(ev[6]));

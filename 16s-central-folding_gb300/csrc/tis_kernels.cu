@@ -824,6 +824,8 @@ __global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int ma
     if (A.err) atomicOr(&S->err, A.err);
 }
 
+__device__ void control_step(const Dev &d, int r);
+
 template <bool D>
 __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
 {
@@ -874,20 +876,33 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
     }
     if ((threadIdx.x & 31) == 0) atomicMax(&s_max, bits);
     __syncthreads();
-    if (threadIdx.x == 0) atomicMax(&d.rs[r].maxd2, s_max);
+    __shared__ int s_last;
+    if (threadIdx.x == 0) {
+        atomicMax(&d.rs[r].maxd2, s_max);
+        __threadfence();
+        // the replica's last block to finish runs the skin check for it
+        const unsigned done = atomicAdd(&d.rs[r].blocks_done, 1u);
+        s_last = (done == (unsigned)(R->npad / kBlock) - 1u);
+        if (s_last) d.rs[r].blocks_done = 0u;
+    }
     if (err) atomicOr(&d.rs[r].err, err);
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        control_step(d, r);
+    }
 }
 
 // check_shifts (E:1741-1776) and the LR gate of deterministic_forces_MPI (E:2550)
-__global__ void k_control(Dev d)
+// check_shifts (E:1741-1776) and the LR gate of deterministic_forces_MPI (E:2550)
+// for replica r; thread 0 decides, the block zeroes the cell counts on a rebuild
+__device__ void control_step(const Dev &d, int r)
 {
-    const int r = blockIdx.x;
     const RepParams *R = d.rp + r;
     RepState *S = d.rs + r;
     __shared__ int s_reb;
     if (threadIdx.x == 0) {
-        const double d2 = __longlong_as_double((long long)S->maxd2);
-        S->maxd2 = 0ull;
+        const double d2 = __longlong_as_double((long long)atomicExch(&S->maxd2, 0ull));
         const double sh = sqrt(d2);
         S->progress += (sh + sh);
         S->klok += 1;
@@ -906,6 +921,8 @@ __global__ void k_control(Dev d)
     if (s_reb)
         for (int c = threadIdx.x; c < R->nc; c += blockDim.x) d.cell_count[R->c0 + c] = 0;
 }
+
+__global__ void k_control(Dev d) { control_step(d, blockIdx.x); }
 
 __global__ void k_force_rebuild(Dev d)
 {
@@ -933,36 +950,41 @@ __device__ inline int cell_axis(double v, double side, double l)
     return (int)ceil(__ddiv_rn(t, l));
 }
 
+// The rebuild kernels run on a fixed grid that strides over the particles (cells)
+// of the replicas whose skin check asked for a rebuild this step.
 __global__ void __launch_bounds__(kBlock) k_cell_assign(Dev d)
 {
-    const int r = d.blk_rep[blockIdx.x];
-    if (!d.rs[r].rebuild) return;
-    const RepParams *R = d.rp + r;
-    const int p = blockIdx.x * kBlock + threadIdx.x;
-    if (!((d.q[p].w >> 16) & 1)) {
-        d.cell_of[p] = -1;
-        return;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    for (int r = 0; r < d.R; ++r) {
+        if (!d.rs[r].rebuild) continue;
+        const RepParams *R = d.rp + r;
+        for (int p = R->p0 + gt; p < R->p0 + R->npad; p += gs) {
+            if (!((d.q[p].w >> 16) & 1)) {
+                d.cell_of[p] = -1;
+                continue;
+            }
+            const int i1 = cell_axis(d.x[p], R->box[0], R->lcell[0]);
+            const int i2 = cell_axis(d.y[p], R->box[1], R->lcell[1]);
+            const int i3 = cell_axis(d.z[p], R->box[2], R->lcell[2]);
+            if (i1 < 1 || i1 > R->mc[0] || i2 < 1 || i2 > R->mc[1] || i3 < 1 || i3 > R->mc[2]) {
+                d.cell_of[p] = -1;
+                atomicOr(&d.rs[r].err, kErrRange);
+                continue;
+            }
+            const int c = (i1 - 1) * R->mc[1] * R->mc[2] + (i2 - 1) * R->mc[2] + (i3 - 1);
+            d.cell_of[p] = c;
+            atomicAdd(d.cell_count + R->c0 + c, 1);
+        }
     }
-    const int i1 = cell_axis(d.x[p], R->box[0], R->lcell[0]);
-    const int i2 = cell_axis(d.y[p], R->box[1], R->lcell[1]);
-    const int i3 = cell_axis(d.z[p], R->box[2], R->lcell[2]);
-    if (i1 < 1 || i1 > R->mc[0] || i2 < 1 || i2 > R->mc[1] || i3 < 1 || i3 > R->mc[2]) {
-        d.cell_of[p] = -1;
-        atomicOr(&d.rs[r].err, kErrRange);
-        return;
-    }
-    const int c = (i1 - 1) * R->mc[1] * R->mc[2] + (i2 - 1) * R->mc[2] + (i3 - 1);
-    d.cell_of[p] = c;
-    atomicAdd(d.cell_count + R->c0 + c, 1);
 }
 
 __global__ void k_cell_scan(Dev d)
 {
-    const int r = blockIdx.x;
-    if (!d.rs[r].rebuild) return;
-    const RepParams *R = d.rp + r;
     __shared__ int s_warp[32];
     __shared__ int s_carry;
+    for (int r = blockIdx.x; r < d.R; r += gridDim.x) {
+    if (!d.rs[r].rebuild) continue;
+    const RepParams *R = d.rp + r;
     if (threadIdx.x == 0) s_carry = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -994,18 +1016,22 @@ __global__ void k_cell_scan(Dev d)
         if (threadIdx.x == blockDim.x - 1) s_carry = excl + v;
         __syncthreads();
     }
+    }
 }
 
 __global__ void __launch_bounds__(kBlock) k_cell_fill(Dev d)
 {
-    const int r = d.blk_rep[blockIdx.x];
-    if (!d.rs[r].rebuild) return;
-    const RepParams *R = d.rp + r;
-    const int p = blockIdx.x * kBlock + threadIdx.x;
-    const int c = d.cell_of[p];
-    if (c < 0) return;
-    const int slot = atomicAdd(d.cell_fill + R->c0 + c, 1);
-    d.cell_list[R->p0 + d.cell_start[R->c0 + c] + slot] = p;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    for (int r = 0; r < d.R; ++r) {
+        if (!d.rs[r].rebuild) continue;
+        const RepParams *R = d.rp + r;
+        for (int p = R->p0 + gt; p < R->p0 + R->npad; p += gs) {
+            const int c = d.cell_of[p];
+            if (c < 0) continue;
+            const int slot = atomicAdd(d.cell_fill + R->c0 + c, 1);
+            d.cell_list[R->p0 + d.cell_start[R->c0 + c] + slot] = p;
+        }
+    }
 }
 
 // One warp per cell: in FP64 mode the cell's particles are put in index order,
@@ -1016,13 +1042,14 @@ __global__ void __launch_bounds__(kBlock) k_cell_fill(Dev d)
 template <bool D>
 __global__ void k_cell_order(Dev d)
 {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= d.C) return;
-    const int r = d.cell_rep[warp];
-    if (!d.rs[r].rebuild) return;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int r = 0; r < d.R; ++r) {
+    if (!d.rs[r].rebuild) continue;
     const RepParams *R = d.rp + r;
-    const int base = R->p0 + d.cell_start[warp];
-    const int n = d.cell_count[warp];
+    for (int cg = R->c0 + wid; cg < R->c0 + R->nc; cg += nw) {
+    const int base = R->p0 + d.cell_start[cg];
+    const int n = d.cell_count[cg];
     int *seg = d.cell_list + base;
     if (D && n > 1 && n <= 256) {  // rank sort, at most 8 particles per lane held in registers
         int v[8], rk[8];
@@ -1050,6 +1077,8 @@ __global__ void k_cell_order(Dev d)
         __syncwarp();
     }
     for (int i = lane; i < n; i += 32) d.qs[base + i] = d.q[seg[i]];
+    }
+    }
 }
 
 // distinct periodic neighbours of cell index i (1..m) along one axis
@@ -1176,9 +1205,11 @@ __global__ void __launch_bounds__(128) k_pair_search(Dev d)
 // (0) when its central pair is in the SR list, i.e. within the SR radius.
 __global__ void k_hb_rebuild(Dev d)
 {
-    const int r = blockIdx.x;
+    __shared__ int s_warp[32];
+    __shared__ int s_carry;
+    for (int r = blockIdx.x; r < d.R; r += gridDim.x) {
     RepState *S = d.rs + r;
-    if (!S->rebuild) return;
+    if (!S->rebuild) continue;
     const RepParams *R = d.rp + r;
     for (int a = R->hba0 + threadIdx.x; a < R->hba1; a += blockDim.x)
         d.hb_excess[a] = d.hba_n[a] - d.hba_val[a];
@@ -1192,8 +1223,6 @@ __global__ void k_hb_rebuild(Dev d)
     }
     __syncthreads();
     // ordered compaction of the live candidates
-    __shared__ int s_warp[32];
-    __shared__ int s_carry;
     if (threadIdx.x == 0) s_carry = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1219,6 +1248,8 @@ __global__ void k_hb_rebuild(Dev d)
         S->n_active = s_carry;
         S->rebuild = 0;
         S->rebuilds += 1;
+    }
+    __syncthreads();
     }
 }
 
@@ -1321,22 +1352,22 @@ void launch_control(const Dev &d, cudaStream_t s) { k_control<<<d.R, 128, 0, s>>
 
 void launch_rebuild(const Dev &d, cudaStream_t s)
 {
-    k_cell_assign<<<d.nblk, kBlock, 0, s>>>(d);
-    k_cell_scan<<<d.R, 256, 0, s>>>(d);
-    k_cell_fill<<<d.nblk, kBlock, 0, s>>>(d);
-    const int cell_blocks = (d.C * 32 + 127) / 128;
-    if (d.fp64) k_cell_order<true><<<cell_blocks, 128, 0, s>>>(d);
-    else k_cell_order<false><<<cell_blocks, 128, 0, s>>>(d);
+    const int pgrid = d.sm_count * 4, rgrid = d.R < d.sm_count ? d.R : d.sm_count;
+    k_cell_assign<<<pgrid, kBlock, 0, s>>>(d);
+    k_cell_scan<<<rgrid, 256, 0, s>>>(d);
+    k_cell_fill<<<pgrid, kBlock, 0, s>>>(d);
+    if (d.fp64) k_cell_order<true><<<d.sm_count * 4, 128, 0, s>>>(d);
+    else k_cell_order<false><<<d.sm_count * 4, 128, 0, s>>>(d);
     if (d.fp64) k_pair_search<true><<<d.search_warps / 4, 128, 0, s>>>(d);
     else k_pair_search<false><<<d.search_warps / 4, 128, 0, s>>>(d);
-    k_hb_rebuild<<<d.R, 256, 0, s>>>(d);
+    k_hb_rebuild<<<rgrid, 256, 0, s>>>(d);
 }
 
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s) { k_force_rebuild<<<d.R, 128, 0, s>>>(d); }
 
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out) { k_rg<<<1, 256, 0, s>>>(d, replica, out); }
 
-// pair SR, pair LR, bonded+stacking, H-bonds+noise, integrate, control, 6 rebuild kernels
-int kernel_launches_per_step() { return 12; }
+// pair SR, pair LR, bonded+stacking, H-bonds+noise, integrate (+skin check), 6 rebuild kernels
+int kernel_launches_per_step() { return 11; }
 
 }  // namespace tis

@@ -24,6 +24,7 @@ struct Dev {
     int4 *qs;                   // packed positions in cell order (qs[slot] = q[cell_list[slot]])
     int full_lists;             // 1: SR list is the reference's full set; 0: pruned to possible forces
     int search_warps;           // warps of the pair-search grid
+    int sm_count;               // multiprocessors (grid size of the rebuild kernels)
     // neighbour lists, column-major: nbr[k * P + p]
     int *nbr_sr, *n_sr, *nbr_lr, *n_lr;
     int cap_sr, cap_lr;

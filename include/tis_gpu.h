@@ -170,8 +170,9 @@ int tis_compute_forces(tis_handle *h, int replica, int term_mask, double *forces
  * replica (drop-in replacements of the four routines of the run loop). */
 int tis_deterministic_forces(tis_handle *h); /* deterministic_forces_MPI  E:2524 */
 int tis_full_forces(tis_handle *h);          /* full_forces               E:2590 */
-int tis_move_rigid_units(tis_handle *h);     /* move_rigid_units          E:2660 */
-int tis_check_shifts(tis_handle *h);         /* check_shifts              E:1741 */
+int tis_move_rigid_units(tis_handle *h);     /* move_rigid_units          E:2660 (also measures the
+                                                shifts of check_shifts, E:1745-1766) */
+int tis_check_shifts(tis_handle *h);         /* check_shifts              E:1741 (list rebuild) */
 /* The force array of one replica as it stands (after tis_deterministic_forces:
  * the reference's fx,fy,fz after the Allreduce, E:2576-2585), x,y,z interleaved. */
 int tis_get_forces(tis_handle *h, int replica, double *forces);
