@@ -950,32 +950,55 @@ __device__ inline int cell_axis(double v, double side, double l)
     return (int)ceil(__ddiv_rn(t, l));
 }
 
-// The rebuild kernels run on a fixed grid that strides over the particles (cells)
-// of the replicas whose skin check asked for a rebuild this step.
+// Work items of the replicas that rebuild this step, laid end to end (`per`: 0 =
+// padded particles, 1 = cells).  Warp-collective: maps item i to its replica r and
+// the offset within it; returns false past the end.
+__device__ inline bool rebuild_item(const Dev &d, int per, int i, int &r, int &off)
+{
+    const int lane = threadIdx.x & 31;
+    int acc = 0;
+    for (int base = 0; base < d.R; base += 32) {
+        const int rr = base + lane;
+        const int n = (rr < d.R && d.rs[rr].rebuild) ? (per ? d.rp[rr].nc : d.rp[rr].npad) : 0;
+        int incl = n;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int tot = __shfl_sync(kFull, incl, 31);
+        if (i < acc + tot) {
+            const unsigned m = __ballot_sync(kFull, i < acc + incl);
+            const int src = __ffs(m) - 1;
+            r = base + src;
+            off = i - acc - __shfl_sync(kFull, incl - n, src);
+            return true;
+        }
+        acc += tot;
+    }
+    return false;
+}
+
 __global__ void __launch_bounds__(kBlock) k_cell_assign(Dev d)
 {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
-    for (int r = 0; r < d.R; ++r) {
-        if (!d.rs[r].rebuild) continue;
-        const RepParams *R = d.rp + r;
-        for (int p = R->p0 + gt; p < R->p0 + R->npad; p += gs) {
-            if (!((d.q[p].w >> 16) & 1)) {
-                d.cell_of[p] = -1;
-                continue;
-            }
-            const int i1 = cell_axis(d.x[p], R->box[0], R->lcell[0]);
-            const int i2 = cell_axis(d.y[p], R->box[1], R->lcell[1]);
-            const int i3 = cell_axis(d.z[p], R->box[2], R->lcell[2]);
-            if (i1 < 1 || i1 > R->mc[0] || i2 < 1 || i2 > R->mc[1] || i3 < 1 || i3 > R->mc[2]) {
-                d.cell_of[p] = -1;
-                atomicOr(&d.rs[r].err, kErrRange);
-                continue;
-            }
-            const int c = (i1 - 1) * R->mc[1] * R->mc[2] + (i2 - 1) * R->mc[2] + (i3 - 1);
-            d.cell_of[p] = c;
-            atomicAdd(d.cell_count + R->c0 + c, 1);
-        }
+    const int r = d.blk_rep[blockIdx.x];
+    if (!d.rs[r].rebuild) return;
+    const RepParams *R = d.rp + r;
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    if (!((d.q[p].w >> 16) & 1)) {
+        d.cell_of[p] = -1;
+        return;
     }
+    const int i1 = cell_axis(d.x[p], R->box[0], R->lcell[0]);
+    const int i2 = cell_axis(d.y[p], R->box[1], R->lcell[1]);
+    const int i3 = cell_axis(d.z[p], R->box[2], R->lcell[2]);
+    if (i1 < 1 || i1 > R->mc[0] || i2 < 1 || i2 > R->mc[1] || i3 < 1 || i3 > R->mc[2]) {
+        d.cell_of[p] = -1;
+        atomicOr(&d.rs[r].err, kErrRange);
+        return;
+    }
+    const int c = (i1 - 1) * R->mc[1] * R->mc[2] + (i2 - 1) * R->mc[2] + (i3 - 1);
+    d.cell_of[p] = c;
+    atomicAdd(d.cell_count + R->c0 + c, 1);
 }
 
 __global__ void k_cell_scan(Dev d)
@@ -1021,17 +1044,14 @@ __global__ void k_cell_scan(Dev d)
 
 __global__ void __launch_bounds__(kBlock) k_cell_fill(Dev d)
 {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
-    for (int r = 0; r < d.R; ++r) {
-        if (!d.rs[r].rebuild) continue;
-        const RepParams *R = d.rp + r;
-        for (int p = R->p0 + gt; p < R->p0 + R->npad; p += gs) {
-            const int c = d.cell_of[p];
-            if (c < 0) continue;
-            const int slot = atomicAdd(d.cell_fill + R->c0 + c, 1);
-            d.cell_list[R->p0 + d.cell_start[R->c0 + c] + slot] = p;
-        }
-    }
+    const int r = d.blk_rep[blockIdx.x];
+    if (!d.rs[r].rebuild) return;
+    const RepParams *R = d.rp + r;
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int c = d.cell_of[p];
+    if (c < 0) return;
+    const int slot = atomicAdd(d.cell_fill + R->c0 + c, 1);
+    d.cell_list[R->p0 + d.cell_start[R->c0 + c] + slot] = p;
 }
 
 // One warp per cell: in FP64 mode the cell's particles are put in index order,
@@ -1044,10 +1064,11 @@ __global__ void k_cell_order(Dev d)
 {
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int r = 0; r < d.R; ++r) {
-    if (!d.rs[r].rebuild) continue;
+    int r, off;
+    for (int item = wid; rebuild_item(d, 1, item, r, off); item += nw) {
     const RepParams *R = d.rp + r;
-    for (int cg = R->c0 + wid; cg < R->c0 + R->nc; cg += nw) {
+    {
+    const int cg = R->c0 + off;
     const int base = R->p0 + d.cell_start[cg];
     const int n = d.cell_count[cg];
     int *seg = d.cell_list + base;
@@ -1111,13 +1132,14 @@ __global__ void __launch_bounds__(128) k_pair_search(Dev d)
     const unsigned lt = (1u << lane) - 1u;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int P = d.P;
-    for (int r = 0; r < d.R; ++r) {
-        if (!d.rs[r].rebuild) continue;
+    int r, off;
+    for (int item = wid; rebuild_item(d, 0, item, r, off); item += d.search_warps) {
         const RepParams *R = d.rp + r;
         const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
         const float sr_lo = R->r2srf * (1.0f - kBand), sr_hi = R->r2srf * (1.0f + kBand);
         const float lr_lo = R->r2lrf * (1.0f - kBand), lr_hi = R->r2lrf * (1.0f + kBand);
-        for (int p = R->p0 + wid; p < R->p0 + R->npad; p += d.search_warps) {
+        {
+            const int p = R->p0 + off;
             const int c = d.cell_of[p];
             if (c < 0) {
                 if (lane == 0) { d.n_sr[p] = 0; d.n_lr[p] = 0; }
@@ -1352,15 +1374,14 @@ void launch_control(const Dev &d, cudaStream_t s) { k_control<<<d.R, 128, 0, s>>
 
 void launch_rebuild(const Dev &d, cudaStream_t s)
 {
-    const int pgrid = d.sm_count * 4, rgrid = d.R < d.sm_count ? d.R : d.sm_count;
-    k_cell_assign<<<pgrid, kBlock, 0, s>>>(d);
-    k_cell_scan<<<rgrid, 256, 0, s>>>(d);
-    k_cell_fill<<<pgrid, kBlock, 0, s>>>(d);
+    k_cell_assign<<<d.nblk, kBlock, 0, s>>>(d);
+    k_cell_scan<<<d.R, 256, 0, s>>>(d);
+    k_cell_fill<<<d.nblk, kBlock, 0, s>>>(d);
     if (d.fp64) k_cell_order<true><<<d.sm_count * 4, 128, 0, s>>>(d);
     else k_cell_order<false><<<d.sm_count * 4, 128, 0, s>>>(d);
     if (d.fp64) k_pair_search<true><<<d.search_warps / 4, 128, 0, s>>>(d);
     else k_pair_search<false><<<d.search_warps / 4, 128, 0, s>>>(d);
-    k_hb_rebuild<<<rgrid, 256, 0, s>>>(d);
+    k_hb_rebuild<<<d.R, 256, 0, s>>>(d);
 }
 
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s) { k_force_rebuild<<<d.R, 128, 0, s>>>(d); }
