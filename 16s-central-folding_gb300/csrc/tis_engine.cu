@@ -96,6 +96,8 @@ struct tis_handle {
     int R = 0, P = 0, C = 0, nblk = 0;
     tis_run_params prm{};
     cudaStream_t stream = nullptr;
+    cudaStream_t side[3] = {nullptr, nullptr, nullptr};  // concurrent force branches
+    cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
     std::vector<void *> owned;
     std::vector<RepHost> rep;
     tis::Dev dev{};
@@ -109,6 +111,11 @@ struct tis_handle {
     {
         if (graph) cudaGraphExecDestroy(graph);
         for (void *p : owned) cudaFree(p);
+        for (int k = 0; k < 3; ++k) {
+            if (side[k]) cudaStreamDestroy(side[k]);
+            if (join[k]) cudaEventDestroy(join[k]);
+        }
+        if (fork) cudaEventDestroy(fork);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -185,11 +192,27 @@ int populate(tis_handle *h)
     return fail(TIS_ERR_CAPACITY, "neighbour lists keep overflowing");
 }
 
+// deterministic_forces_MPI (E:2524-2586): the four force kernels are independent
+// (fixed-point atomics into one sum, the LR sum kept apart), so they run as
+// concurrent branches joined before the noise
+void enqueue_forces(tis_handle *h)
+{
+    cudaEventRecord(h->fork, h->stream);
+    for (int k = 0; k < 3; ++k) cudaStreamWaitEvent(h->side[k], h->fork, 0);
+    tis::launch_pair_lr(h->dev, h->side[0], false, false);
+    tis::launch_topology(h->dev, h->side[1], 4 | 8, false, false, true);
+    tis::launch_topology(h->dev, h->side[2], 16, false, false, true);
+    tis::launch_pair_sr(h->dev, h->stream, false, true);
+    for (int k = 0; k < 3; ++k) {
+        cudaEventRecord(h->join[k], h->side[k]);
+        cudaStreamWaitEvent(h->stream, h->join[k], 0);
+    }
+}
+
 void enqueue_step(tis_handle *h)
 {
-    tis::launch_pair_sr(h->dev, h->stream, false, true);
-    tis::launch_pair_lr(h->dev, h->stream, false, false);
-    tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true, true);
+    enqueue_forces(h);
+    tis::launch_noise(h->dev, h->stream);      // full_forces' Gaussians + recentring shift
     tis::launch_integrate(h->dev, h->stream);  // its last block per replica runs the skin check
     tis::launch_rebuild(h->dev, h->stream);
 }
@@ -245,6 +268,12 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     };
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
         return bail(fail(TIS_ERR_CUDA, "cudaStreamCreate failed"));
+    for (int k = 0; k < 3; ++k)
+        if (cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->join[k], cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(TIS_ERR_CUDA, "cudaStreamCreate/cudaEventCreate failed"));
+    if (cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming) != cudaSuccess)
+        return bail(fail(TIS_ERR_CUDA, "cudaEventCreate failed"));
 
     std::vector<tis::RepParams> rp(n_replicas);
     std::vector<int> code, blk_rep, rep_of, cell_rep;
@@ -749,8 +778,8 @@ int tis_compute_forces(tis_handle *h, int r, int mask, double *forces, double *e
     if ((rc = clear_flags(h))) return rc;
     const tis::Dev &d = h->dev;
     TIS_CUDA(cudaMemsetAsync(d.eterm, 0, sizeof(double) * h->R * tis::kNE, h->stream));
+    TIS_CUDA(cudaMemsetAsync(d.f, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
     if (mask & TIS_TERM_SR) tis::launch_pair_sr(d, h->stream, true, false);
-    else TIS_CUDA(cudaMemsetAsync(d.f, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
     if (mask & TIS_TERM_LR) tis::launch_pair_lr(d, h->stream, true, true);
     else TIS_CUDA(cudaMemsetAsync(d.flr, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
     const int tmask = (mask & TIS_TERM_BONDED ? 4 : 0) | (mask & TIS_TERM_STACK ? 8 : 0) | (mask & TIS_TERM_HB ? 16 : 0);
@@ -768,6 +797,9 @@ int tis_compute_forces(tis_handle *h, int r, int mask, double *forces, double *e
     TIS_CUDA(cudaMemcpyAsync(et, d.eterm + r * tis::kNE, sizeof et, cudaMemcpyDeviceToHost, h->stream));
     TIS_CUDA(cudaMemcpyAsync(&rg, h->d_scalar, sizeof rg, cudaMemcpyDeviceToHost, h->stream));
     TIS_CUDA(cudaMemcpyAsync(&st, d.rs + r, sizeof st, cudaMemcpyDeviceToHost, h->stream));
+    // the step's force kernels accumulate into a zero sum: leave it so
+    TIS_CUDA(cudaMemsetAsync(d.f, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
+    TIS_CUDA(cudaMemsetAsync(d.flr, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
     if (forces)
         for (int i = 0; i < hr.n; ++i)
@@ -796,9 +828,9 @@ int tis_deterministic_forces(tis_handle *h)
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     int rc;
     if (!h->lists_built && (rc = populate(h))) return rc;
-    tis::launch_pair_sr(h->dev, h->stream, false, true);
-    tis::launch_pair_lr(h->dev, h->stream, false, false);
-    tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, false, true);
+    // E:2532: the force sum starts from zero (the fused step's integrator leaves it zero)
+    TIS_CUDA(cudaMemsetAsync(h->dev.f, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
+    enqueue_forces(h);
     TIS_CUDA(cudaGetLastError());
     return TIS_OK;
 }
@@ -898,7 +930,8 @@ int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
         TIS_CUDA(cudaEventRecord(ev[1], h->stream));
         tis::launch_pair_lr(h->dev, h->stream, false, false);
         TIS_CUDA(cudaEventRecord(ev[2], h->stream));
-        tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true, true);
+        tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, false, true);
+        tis::launch_noise(h->dev, h->stream);
         TIS_CUDA(cudaEventRecord(ev[3], h->stream));
         tis::launch_integrate(h->dev, h->stream);
         TIS_CUDA(cudaEventRecord(ev[4], h->stream));

@@ -378,10 +378,15 @@ __global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
             az += __shfl_xor_sync(kFull, az, o);
         }
         if (lane4 == 0) {
-            unsigned long long *out = LR ? d.flr : d.f;
-            out[p] = (unsigned long long)ax;
-            out[P + p] = (unsigned long long)ay;
-            out[2 * P + p] = (unsigned long long)az;
+            if (LR) {  // the LR force is kept for the MTS interval: overwrite
+                d.flr[p] = (unsigned long long)ax;
+                d.flr[P + p] = (unsigned long long)ay;
+                d.flr[2 * P + p] = (unsigned long long)az;
+            } else if (act) {  // other force kernels run concurrently: accumulate
+                atomic_add_fix(d.f + p, ax);
+                atomic_add_fix(d.f + P + p, ay);
+                atomic_add_fix(d.f + 2 * P + p, az);
+            }
         }
     } else {
         double ax = 0, ay = 0, az = 0;
@@ -426,10 +431,17 @@ __global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
             az += __shfl_xor_sync(kFull, az, o);
         }
         if (lane4 == 0) {
-            double *out = (double *)(LR ? d.flr : d.f);
-            out[p] = ax;
-            out[P + p] = ay;
-            out[2 * P + p] = az;
+            if (LR) {
+                double *out = (double *)d.flr;
+                out[p] = ax;
+                out[P + p] = ay;
+                out[2 * P + p] = az;
+            } else if (act) {
+                double *out = (double *)d.f;
+                atomicAdd(out + p, ax);
+                atomicAdd(out + P + p, ay);
+                atomicAdd(out + 2 * P + p, az);
+            }
         }
     }
     if (EN) {
@@ -862,6 +874,9 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
         d.x[p] = xn[0]; d.y[p] = xn[1]; d.z[p] = xn[2];
         d.xo[p] = xo[0]; d.yo[p] = xo[1]; d.zo[p] = xo[2];
         d.vx[p] = vn[0]; d.vy[p] = vn[1]; d.vz[p] = vn[2];
+        d.f[p] = 0ull;  // consumed: the next step's force kernels accumulate from zero
+        d.f[d.P + p] = 0ull;
+        d.f[2 * d.P + p] = 0ull;
         int4 q = qp;
         q.x = (int)(unsigned)(long long)floor(xn[0] * R->qinv[0]);
         q.y = (int)(unsigned)(long long)floor(xn[1] * R->qinv[1]);
@@ -1388,7 +1403,7 @@ void launch_force_all_rebuild(const Dev &d, cudaStream_t s) { k_force_rebuild<<<
 
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out) { k_rg<<<1, 256, 0, s>>>(d, replica, out); }
 
-// pair SR, pair LR, bonded+stacking, H-bonds+noise, integrate (+skin check), 6 rebuild kernels
-int kernel_launches_per_step() { return 11; }
+// pair SR, pair LR, bonded+stacking, H-bonds, noise+shift, integrate (+skin check), 6 rebuild kernels
+int kernel_launches_per_step() { return 12; }
 
 }  // namespace tis
