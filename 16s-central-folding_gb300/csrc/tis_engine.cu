@@ -92,7 +92,9 @@ int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
 }  // namespace
 
-struct tis_handle {
+// One group of replicas: its own device state, streams and CUDA graph.  A handle
+// holds several groups whose step graphs run concurrently.
+struct Group {
     int R = 0, P = 0, C = 0, nblk = 0;
     tis_run_params prm{};
     cudaStream_t stream = nullptr;
@@ -104,10 +106,11 @@ struct tis_handle {
     bool lists_built = false;
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
+    int base = 0;  // handle-wide index of the group's first replica
     long long launches = 0;
     double *d_scalar = nullptr;
 
-    ~tis_handle()
+    ~Group()
     {
         if (graph) cudaGraphExecDestroy(graph);
         for (void *p : owned) cudaFree(p);
@@ -122,21 +125,21 @@ struct tis_handle {
 
 namespace {
 
-int check_flags(tis_handle *h)
+int check_flags(Group *h)
 {
     std::vector<tis::RepState> rs(h->R);
     TIS_CUDA(cudaMemcpyAsync(rs.data(), h->dev.rs, sizeof(tis::RepState) * h->R, cudaMemcpyDeviceToHost, h->stream));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
     for (int r = 0; r < h->R; ++r) {
         const int e = rs[r].err;
-        if (e & tis::kErrCapacity) return fail(TIS_ERR_CAPACITY, "replica %d: neighbour list capacity exceeded", r);
-        if (e & tis::kErrRange) return fail(TIS_ERR_RANGE, "replica %d: a particle left the cell grid's range", r);
-        if (e & tis::kErrNonFinite) return fail(TIS_ERR_NONFINITE, "replica %d: non-finite or runaway force/state", r);
+        if (e & tis::kErrCapacity) return fail(TIS_ERR_CAPACITY, "replica %d: neighbour list capacity exceeded", h->base + r);
+        if (e & tis::kErrRange) return fail(TIS_ERR_RANGE, "replica %d: a particle left the cell grid's range", h->base + r);
+        if (e & tis::kErrNonFinite) return fail(TIS_ERR_NONFINITE, "replica %d: non-finite or runaway force/state", h->base + r);
     }
     return TIS_OK;
 }
 
-int clear_flags(tis_handle *h)
+int clear_flags(Group *h)
 {
     // err is the 4th int after 4 eight-byte counters and a double; clear via a host round trip
     std::vector<tis::RepState> rs(h->R);
@@ -148,7 +151,7 @@ int clear_flags(tis_handle *h)
     return TIS_OK;
 }
 
-int grow_lists(tis_handle *h, int cap_sr, int cap_lr)
+int grow_lists(Group *h, int cap_sr, int cap_lr)
 {
     // lists are the last allocations that depend on capacity; allocate anew
     TIS_CUDA(cudaStreamSynchronize(h->stream));
@@ -173,7 +176,7 @@ int grow_lists(tis_handle *h, int cap_sr, int cap_lr)
     return TIS_OK;
 }
 
-int populate(tis_handle *h)
+int populate(Group *h)
 {
     for (int attempt = 0; attempt < 6; ++attempt) {
         int rc = clear_flags(h);
@@ -195,7 +198,7 @@ int populate(tis_handle *h)
 // deterministic_forces_MPI (E:2524-2586): the four force kernels are independent
 // (fixed-point atomics into one sum, the LR sum kept apart), so they run as
 // concurrent branches joined before the noise
-void enqueue_forces(tis_handle *h)
+void enqueue_forces(Group *h)
 {
     cudaEventRecord(h->fork, h->stream);
     for (int k = 0; k < 3; ++k) cudaStreamWaitEvent(h->side[k], h->fork, 0);
@@ -209,7 +212,7 @@ void enqueue_forces(tis_handle *h)
     }
 }
 
-void enqueue_step(tis_handle *h)
+void enqueue_step(Group *h)
 {
     enqueue_forces(h);
     tis::launch_noise(h->dev, h->stream);      // full_forces' Gaussians + recentring shift
@@ -217,7 +220,7 @@ void enqueue_step(tis_handle *h)
     tis::launch_rebuild(h->dev, h->stream);
 }
 
-int valid_replica(tis_handle *h, int r)
+int valid_replica(Group *h, int r)
 {
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     if (r < 0 || r >= h->R) return fail(TIS_ERR_ARG, "replica %d out of range (0..%d)", r, h->R - 1);
@@ -226,42 +229,13 @@ int valid_replica(tis_handle *h, int r)
 
 }  // namespace
 
-extern "C" {
 
-int tis_run_params_default(tis_run_params *p)
+static int grp_create(const tis_system *const *systems, int n_replicas, const tis_run_params &prm, int base, Group **out)
 {
-    if (!p) return fail(TIS_ERR_ARG, "null params");
-    memset(p, 0, sizeof *p);
-    p->precision = TIS_PREC_MIXED;
-    p->noise = TIS_NOISE_REFERENCE;
-    p->sr = 12.0;
-    p->skin = 3.0;
-    p->lr_interval = 10;
-    p->use_graph = 1;
-    p->graph_steps = 20;
-    return TIS_OK;
-}
-
-int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_params *prm_in, tis_handle **out)
-{
-    tis::clear_error();
-    if (!systems || n_replicas < 1 || !out) return fail(TIS_ERR_ARG, "tis_create: bad argument");
-    tis_run_params prm;
-    if (prm_in) prm = *prm_in;
-    else tis_run_params_default(&prm);
-    if (prm.lr_interval < 1) prm.lr_interval = 10;
-    if (prm.graph_steps < 1) prm.graph_steps = 20;
-    if (prm.sr <= 0) prm.sr = 12.0;
-    if (prm.skin <= 0) prm.skin = 3.0;
-
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(TIS_ERR_CUDA, "no CUDA device available");
-    if (prm.device < 0 || prm.device >= ndev) return fail(TIS_ERR_ARG, "device %d out of range", prm.device);
-    TIS_CUDA(cudaSetDevice(prm.device));
-
-    tis_handle *h = new tis_handle();
+    Group *h = new Group();
     h->prm = prm;
     h->R = n_replicas;
+    h->base = base;
     auto bail = [&](int rc) {
         delete h;
         return rc;
@@ -290,21 +264,21 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
 
     for (int r = 0; r < n_replicas; ++r) {
         const tis_system *s = systems[r];
-        if (!s) return bail(fail(TIS_ERR_ARG, "replica %d: null system", r));
+        if (!s) return bail(fail(TIS_ERR_ARG, "replica %d: null system", base + r));
         const int n = (int)scalar_i64(s, "n_particles", -1);
         const int nrna = (int)scalar_i64(s, "n_rna", -1);
-        if (n <= 0 || nrna <= 0 || nrna > n) return bail(fail(TIS_ERR_ARG, "replica %d: bad n_particles/n_rna", r));
-        const tis::Array *box = need(s, "box", r, TIS_F64, 3);
-        const tis::Array *type = need(s, "type", r, TIS_I32, n), *kind = need(s, "kind", r, TIS_I32, n);
-        const tis::Array *mass = need(s, "mass", r, TIS_F64, 9), *rlj = need(s, "rlj", r, TIS_F64, 9);
-        const tis::Array *elj = need(s, "elj", r, TIS_F64, 9), *qc = need(s, "qc", r, TIS_F64, 9);
+        if (n <= 0 || nrna <= 0 || nrna > n) return bail(fail(TIS_ERR_ARG, "replica %d: bad n_particles/n_rna", base + r));
+        const tis::Array *box = need(s, "box", base + r, TIS_F64, 3);
+        const tis::Array *type = need(s, "type", base + r, TIS_I32, n), *kind = need(s, "kind", base + r, TIS_I32, n);
+        const tis::Array *mass = need(s, "mass", base + r, TIS_F64, 9), *rlj = need(s, "rlj", base + r, TIS_F64, 9);
+        const tis::Array *elj = need(s, "elj", base + r, TIS_F64, 9), *qc = need(s, "qc", base + r, TIS_F64, 9);
         if (!box || !type || !kind || !mass || !rlj || !elj || !qc) return bail(TIS_ERR_ARG);
         const tis::Array *sv[9];
         for (int k = 0; k < 9; ++k)
-            if (!(sv[k] = need(s, snames[k], r, TIS_F64, n))) return bail(TIS_ERR_ARG);
+            if (!(sv[k] = need(s, snames[k], base + r, TIS_F64, n))) return bail(TIS_ERR_ARG);
         excl_of.resize((size_t)p0 + round_up(n, tis::kBlock));
         const int center = (int)scalar_i64(s, "center", 499);
-        if (center < 0 || center >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: centre bead %d outside the RNA", r, center));
+        if (center < 0 || center >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: centre bead %d outside the RNA", base + r, center));
 
         RepHost hr{};
         hr.n = n;
@@ -316,7 +290,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
         const double T = scalar_f64(s, "T", 0.615), hstep = scalar_f64(s, "h", 0.05);
         const double lB = scalar_f64(s, "lB", 332.0637090 * (0.03273600947 * T - 0.00669625750));
         const double rc = scalar_f64(s, "rc", 50.0);
-        if (rc < prm.sr) return bail(fail(TIS_ERR_ARG, "replica %d: Coulomb cutoff %g below the SR radius %g", r, rc, prm.sr));
+        if (rc < prm.sr) return bail(fail(TIS_ERR_ARG, "replica %d: Coulomb cutoff %g below the SR radius %g", base + r, rc, prm.sr));
         for (int k = 0; k < 3; ++k) {
             const double L = box->as<double>()[k];
             R.box[k] = L;
@@ -324,7 +298,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
             R.qinv[k] = 4294967296.0 / L;
             R.qstep[k] = (float)(L / 4294967296.0);
             R.mc[k] = (int)(L / (rc + prm.skin));  // E:1484-1490
-            if (R.mc[k] < 1) return bail(fail(TIS_ERR_ARG, "replica %d: box smaller than the LR list radius", r));
+            if (R.mc[k] < 1) return bail(fail(TIS_ERR_ARG, "replica %d: box smaller than the LR list radius", base + r));
             R.lcell[k] = L / R.mc[k];
             hr.mc[k] = R.mc[k];
         }
@@ -383,14 +357,14 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
                 R.qclb[J] = (float)(Q * lB);
                 R.ljkeep2[J] = (float)((Dl + prm.skin) * (Dl + prm.skin) * (1.0 + 1e-5));
             }
-        R.seed = (unsigned long long)scalar_i64(s, "seed", r + 1);
+        R.seed = (unsigned long long)scalar_i64(s, "seed", base + r + 1);
 
         // particles
         for (int i = 0; i < hr.npad; ++i) {
             if (i < n) {
                 const int t = type->as<int32_t>()[i], k = kind->as<int32_t>()[i];
-                if (t < 1 || t > 9 || k < 0 || k > 5) return bail(fail(TIS_ERR_ARG, "replica %d: bad type/kind of particle %d", r, i));
-                if ((i < nrna) != (k <= 2)) return bail(fail(TIS_ERR_ARG, "replica %d: RNA beads must precede the ions", r));
+                if (t < 1 || t > 9 || k < 0 || k > 5) return bail(fail(TIS_ERR_ARG, "replica %d: bad type/kind of particle %d", base + r, i));
+                if ((i < nrna) != (k <= 2)) return bail(fail(TIS_ERR_ARG, "replica %d: RNA beads must precede the ions", base + r));
                 code.push_back(t | (k << 8) | (1 << 16));
                 for (int c = 0; c < 9; ++c) st[c].push_back(sv[c]->as<double>()[i]);
             } else {
@@ -408,19 +382,19 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
         max_rho_ch = std::max(max_rho_ch, nch / vol);
 
         // bonded terms (polymer_constraints order)
-        const tis::Array *btk = need(s, "bt_kind", r, TIS_I32);
+        const tis::Array *btk = need(s, "bt_kind", base + r, TIS_I32);
         if (!btk) return bail(TIS_ERR_ARG);
         const int64_t nbt = btk->count();
-        const tis::Array *bta = need(s, "bt_a", r, TIS_I32, nbt), *btb = need(s, "bt_b", r, TIS_I32, nbt);
-        const tis::Array *btc = need(s, "bt_c", r, TIS_I32, nbt), *btk0 = need(s, "bt_k0", r, TIS_F64, nbt);
-        const tis::Array *btx0 = need(s, "bt_x0", r, TIS_F64, nbt);
+        const tis::Array *bta = need(s, "bt_a", base + r, TIS_I32, nbt), *btb = need(s, "bt_b", base + r, TIS_I32, nbt);
+        const tis::Array *btc = need(s, "bt_c", base + r, TIS_I32, nbt), *btk0 = need(s, "bt_k0", base + r, TIS_F64, nbt);
+        const tis::Array *btx0 = need(s, "bt_x0", base + r, TIS_F64, nbt);
         if (!bta || !btb || !btc || !btk0 || !btx0) return bail(TIS_ERR_ARG);
         hr.bt0 = (int)bt_idx.size();
         for (int64_t t = 0; t < nbt; ++t) {
             const int kd = btk->as<int32_t>()[t];
             const int a = bta->as<int32_t>()[t], b = btb->as<int32_t>()[t], c = btc->as<int32_t>()[t];
             if (a < 0 || a >= nrna || b < 0 || b >= nrna || (kd == 1 && (c < 0 || c >= nrna)))
-                return bail(fail(TIS_ERR_ARG, "replica %d: bonded term %lld has a bad index", r, (long long)t));
+                return bail(fail(TIS_ERR_ARG, "replica %d: bonded term %lld has a bad index", base + r, (long long)t));
             bt_idx.push_back(make_int4(p0 + a, p0 + b, kd == 1 ? p0 + c : p0 + b, kd));
             bt_par.push_back(make_double2(btk0->as<double>()[t], btx0->as<double>()[t]));
         }
@@ -434,25 +408,25 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
             for (int side = 0; side < 2; ++side) {
                 const int self = side ? b : a, other = side ? a : b;
                 if ((int)excl_of[self].size() >= tis::kExcl)
-                    return bail(fail(TIS_ERR_ARG, "replica %d: particle %d has more than %d bonded partners", r, self - p0, tis::kExcl));
+                    return bail(fail(TIS_ERR_ARG, "replica %d: particle %d has more than %d bonded partners", base + r, self - p0, tis::kExcl));
                 excl_of[self].push_back(other);
             }
         }
 
         // stacks
-        const tis::Array *s3E = need(s, "st3_E", r, TIS_F64), *s2E = need(s, "st2_E", r, TIS_F64);
+        const tis::Array *s3E = need(s, "st3_E", base + r, TIS_F64), *s2E = need(s, "st2_E", base + r, TIS_F64);
         if (!s3E || !s2E) return bail(TIS_ERR_ARG);
         const int64_t n3 = s3E->count(), n2 = s2E->count();
-        const tis::Array *s3i = need(s, "st3_idx", r, TIS_I32, 6 * n3), *s3n = need(s, "st3_native", r, TIS_F64, 6 * n3);
-        const tis::Array *s2i = need(s, "st2_idx", r, TIS_I32, 7 * n2), *s2r = need(s, "st2_r0", r, TIS_F64, n2);
+        const tis::Array *s3i = need(s, "st3_idx", base + r, TIS_I32, 6 * n3), *s3n = need(s, "st3_native", base + r, TIS_F64, 6 * n3);
+        const tis::Array *s2i = need(s, "st2_idx", base + r, TIS_I32, 7 * n2), *s2r = need(s, "st2_r0", base + r, TIS_F64, n2);
         if (!s3i || !s3n || !s2i || !s2r) return bail(TIS_ERR_ARG);
         std::vector<int> off3(2 * n3, -1);
         if (const tis::Array *o = s->get("st3_off")) {
-            if (o->dtype != TIS_I32 || o->count() != 2 * n3) return bail(fail(TIS_ERR_ARG, "replica %d: bad st3_off", r));
+            if (o->dtype != TIS_I32 || o->count() != 2 * n3) return bail(fail(TIS_ERR_ARG, "replica %d: bad st3_off", base + r));
             for (int64_t t = 0; t < 2 * n3; ++t) off3[t] = o->as<int32_t>()[t];
         } else {  // E:1960-1981: a site with ST_EXCESS == 1 switches off stack s3_N + ceil(site/2) - 1
-            const tis::Array *site = need(s, "st3_site", r, TIS_I32, 2 * n3);
-            const tis::Array *exc = need(s, "st_excess", r, TIS_I32);
+            const tis::Array *site = need(s, "st3_site", base + r, TIS_I32, 2 * n3);
+            const tis::Array *exc = need(s, "st_excess", base + r, TIS_I32);
             if (!site || !exc) return bail(TIS_ERR_ARG);
             for (int64_t t = 0; t < 2 * n3; ++t) {
                 const int e = site->as<int32_t>()[t];
@@ -466,7 +440,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
         for (int64_t k = 0; k < n3; ++k) {
             for (int c = 0; c < 6; ++c) {
                 const int v = s3i->as<int32_t>()[6 * k + c];
-                if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: tertiary stack %lld bad index", r, (long long)k));
+                if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: tertiary stack %lld bad index", base + r, (long long)k));
                 st3_idx.push_back(p0 + v);
                 st3_nat.push_back(s3n->as<double>()[6 * k + c]);
             }
@@ -479,7 +453,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
         for (int64_t k = 0; k < n2; ++k) {
             for (int c = 0; c < 7; ++c) {
                 const int v = s2i->as<int32_t>()[7 * k + c];
-                if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: secondary stack %lld bad index", r, (long long)k));
+                if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: secondary stack %lld bad index", base + r, (long long)k));
                 st2_idx.push_back(p0 + v);
             }
             st2_r0.push_back(s2r->as<double>()[k]);
@@ -488,23 +462,23 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
         hr.s21 = (int)st2_E.size();
 
         // hydrogen bonds
-        const tis::Array *hE = need(s, "hb_E", r, TIS_F64);
-        const tis::Array *hv = need(s, "hba_valence", r, TIS_I32);
+        const tis::Array *hE = need(s, "hb_E", base + r, TIS_F64);
+        const tis::Array *hv = need(s, "hba_valence", base + r, TIS_I32);
         if (!hE || !hv) return bail(TIS_ERR_ARG);
         const int64_t nh = hE->count(), na = hv->count();
-        const tis::Array *hi = need(s, "hb_idx", r, TIS_I32, 6 * nh), *hn = need(s, "hb_native", r, TIS_F64, 6 * nh);
-        const tis::Array *hd = need(s, "hb_dode", r, TIS_I32, nh), *hao = need(s, "hb_atom_off", r, TIS_I32, nh + 1);
-        const tis::Array *hco = need(s, "hba_cand_off", r, TIS_I32, na + 1);
+        const tis::Array *hi = need(s, "hb_idx", base + r, TIS_I32, 6 * nh), *hn = need(s, "hb_native", base + r, TIS_F64, 6 * nh);
+        const tis::Array *hd = need(s, "hb_dode", base + r, TIS_I32, nh), *hao = need(s, "hb_atom_off", base + r, TIS_I32, nh + 1);
+        const tis::Array *hco = need(s, "hba_cand_off", base + r, TIS_I32, na + 1);
         if (!hi || !hn || !hd || !hao || !hco) return bail(TIS_ERR_ARG);
-        const tis::Array *hai = need(s, "hb_atom_idx", r, TIS_I32, hao->as<int32_t>()[nh]);
-        const tis::Array *hci = need(s, "hba_cand_idx", r, TIS_I32, hco->as<int32_t>()[na]);
+        const tis::Array *hai = need(s, "hb_atom_idx", base + r, TIS_I32, hao->as<int32_t>()[nh]);
+        const tis::Array *hci = need(s, "hba_cand_idx", base + r, TIS_I32, hco->as<int32_t>()[na]);
         if (!hai || !hci) return bail(TIS_ERR_ARG);
         hr.hb0 = (int)hb_E.size();
         hr.hba0 = (int)hba_val.size();
         for (int64_t k = 0; k < nh; ++k) {
             for (int c = 0; c < 6; ++c) {
                 const int v = hi->as<int32_t>()[6 * k + c];
-                if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond candidate %lld bad index", r, (long long)k));
+                if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond candidate %lld bad index", base + r, (long long)k));
                 hb_idx.push_back(p0 + v);
                 hb_nat.push_back(hn->as<double>()[6 * k + c]);
             }
@@ -512,7 +486,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
             hb_dode.push_back(hd->as<int32_t>()[k]);
             for (int u = hao->as<int32_t>()[k]; u < hao->as<int32_t>()[k + 1]; ++u) {
                 const int a = hai->as<int32_t>()[u];
-                if (a < 0 || a >= na) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond atom index out of range", r));
+                if (a < 0 || a >= na) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond atom index out of range", base + r));
                 hb_aidx.push_back(hr.hba0 + a);
             }
             hb_aoff.push_back((int)hb_aidx.size());
@@ -528,7 +502,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
             maxk = std::max(maxk, cnt);
             for (int u = hco->as<int32_t>()[a]; u < hco->as<int32_t>()[a + 1]; ++u) {
                 const int k = hci->as<int32_t>()[u];
-                if (k < 0 || k >= nh) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond candidate index out of range", r));
+                if (k < 0 || k >= nh) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond candidate index out of range", base + r));
                 hba_cidx.push_back(hr.hb0 + k);
             }
             hba_coff.push_back((int)hba_cidx.size());
@@ -666,7 +640,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     return TIS_OK;
 }
 
-int tis_destroy(tis_handle *h)
+static int grp_destroy(Group *h)
 {
     if (h) {
         cudaSetDevice(h->prm.device);
@@ -676,7 +650,7 @@ int tis_destroy(tis_handle *h)
     return TIS_OK;
 }
 
-int tis_set_state(tis_handle *h, int r, const double *x, const double *y, const double *z, const double *xo,
+static int grp_set_state(Group *h, int r, const double *x, const double *y, const double *z, const double *xo,
                   const double *yo, const double *zo, const double *vx, const double *vy, const double *vz)
 {
     int rc = valid_replica(h, r);
@@ -695,7 +669,7 @@ int tis_set_state(tis_handle *h, int r, const double *x, const double *y, const 
     return TIS_OK;
 }
 
-int tis_get_state(tis_handle *h, int r, double *x, double *y, double *z, double *xo, double *yo, double *zo,
+static int grp_get_state(Group *h, int r, double *x, double *y, double *z, double *xo, double *yo, double *zo,
                   double *vx, double *vy, double *vz)
 {
     int rc = valid_replica(h, r);
@@ -709,13 +683,13 @@ int tis_get_state(tis_handle *h, int r, double *x, double *y, double *z, double 
     return TIS_OK;
 }
 
-int tis_populate_lists(tis_handle *h)
+static int grp_populate_lists(Group *h)
 {
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     return populate(h);
 }
 
-int tis_get_cells(tis_handle *h, int r, int32_t *cell, int32_t *dims)
+static int grp_get_cells(Group *h, int r, int32_t *cell, int32_t *dims)
 {
     int rc = valid_replica(h, r);
     if (rc) return rc;
@@ -726,7 +700,7 @@ int tis_get_cells(tis_handle *h, int r, int32_t *cell, int32_t *dims)
     return TIS_OK;
 }
 
-int tis_get_pairs(tis_handle *h, int r, int which, int32_t *pairs, int64_t cap, int64_t *n)
+static int grp_get_pairs(Group *h, int r, int which, int32_t *pairs, int64_t cap, int64_t *n)
 {
     int rc = valid_replica(h, r);
     if (rc) return rc;
@@ -757,7 +731,7 @@ int tis_get_pairs(tis_handle *h, int r, int which, int32_t *pairs, int64_t cap, 
     return TIS_OK;
 }
 
-int tis_get_hb_status(tis_handle *h, int r, int32_t *status, int32_t *excess)
+static int grp_get_hb_status(Group *h, int r, int32_t *status, int32_t *excess)
 {
     int rc = valid_replica(h, r);
     if (rc) return rc;
@@ -770,7 +744,7 @@ int tis_get_hb_status(tis_handle *h, int r, int32_t *status, int32_t *excess)
     return TIS_OK;
 }
 
-int tis_compute_forces(tis_handle *h, int r, int mask, double *forces, double *energies)
+static int grp_compute_forces(Group *h, int r, int mask, double *forces, double *energies)
 {
     int rc = valid_replica(h, r);
     if (rc) return rc;
@@ -823,7 +797,7 @@ int tis_compute_forces(tis_handle *h, int r, int mask, double *forces, double *e
     return check_flags(h);
 }
 
-int tis_deterministic_forces(tis_handle *h)
+static int grp_deterministic_forces(Group *h)
 {
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     int rc;
@@ -835,7 +809,7 @@ int tis_deterministic_forces(tis_handle *h)
     return TIS_OK;
 }
 
-int tis_get_forces(tis_handle *h, int r, double *forces)
+static int grp_get_forces(Group *h, int r, double *forces)
 {
     int rc = valid_replica(h, r);
     if (rc) return rc;
@@ -863,7 +837,7 @@ int tis_get_forces(tis_handle *h, int r, double *forces)
     return check_flags(h);
 }
 
-int tis_full_forces(tis_handle *h)
+static int grp_full_forces(Group *h)
 {
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     tis::launch_noise(h->dev, h->stream);
@@ -871,7 +845,7 @@ int tis_full_forces(tis_handle *h)
     return TIS_OK;
 }
 
-int tis_move_rigid_units(tis_handle *h)
+static int grp_move_rigid_units(Group *h)
 {
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     tis::launch_integrate(h->dev, h->stream);
@@ -879,7 +853,7 @@ int tis_move_rigid_units(tis_handle *h)
     return TIS_OK;
 }
 
-int tis_check_shifts(tis_handle *h)
+static int grp_check_shifts(Group *h)
 {
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     // the displacement check itself ran at the end of tis_move_rigid_units
@@ -888,7 +862,7 @@ int tis_check_shifts(tis_handle *h)
     return TIS_OK;
 }
 
-int tis_step(tis_handle *h, int64_t n)
+static int grp_step(Group *h, int64_t n)
 {
     if (!h || n < 0) return fail(TIS_ERR_ARG, "tis_step: bad argument");
     int rc;
@@ -916,7 +890,7 @@ int tis_step(tis_handle *h, int64_t n)
     return TIS_OK;
 }
 
-int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
+static int grp_profile_stages(Group *h, int64_t n, double *ms)
 {
     if (!h || n < 1 || !ms) return fail(TIS_ERR_ARG, "tis_profile_stages: bad argument");
     int rc;
@@ -951,13 +925,13 @@ int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
     return check_flags(h);
 }
 
-int tis_sync(tis_handle *h)
+static int grp_sync(Group *h)
 {
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     return check_flags(h);
 }
 
-int tis_get_energies(tis_handle *h, int r, double *out5)
+static int grp_get_energies(Group *h, int r, double *out5)
 {
     int rc = valid_replica(h, r);
     if (rc) return rc;
@@ -976,7 +950,7 @@ int tis_get_energies(tis_handle *h, int r, double *out5)
     return TIS_OK;
 }
 
-int tis_get_stack_energies(tis_handle *h, int r, double *out, int64_t cap, int64_t *n)
+static int grp_get_stack_energies(Group *h, int r, double *out, int64_t cap, int64_t *n)
 {
     int rc = valid_replica(h, r);
     if (rc) return rc;
@@ -989,7 +963,7 @@ int tis_get_stack_energies(tis_handle *h, int r, double *out, int64_t cap, int64
     return TIS_OK;
 }
 
-int tis_get_counters(tis_handle *h, int r, int64_t *klok, int64_t *rebuilds, int64_t *draws)
+static int grp_get_counters(Group *h, int r, int64_t *klok, int64_t *rebuilds, int64_t *draws)
 {
     int rc = valid_replica(h, r);
     if (rc) return rc;
@@ -1000,6 +974,314 @@ int tis_get_counters(tis_handle *h, int r, int64_t *klok, int64_t *rebuilds, int
     if (rebuilds) *rebuilds = st.rebuilds;
     if (draws) *draws = (int64_t)st.ctr;
     return TIS_OK;
+}
+
+static int grp_replica_size(Group *h, int r, int *n_particles)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    if (n_particles) *n_particles = h->rep[r].n;
+    return TIS_OK;
+}
+
+static int grp_get_launch_count(Group *h, int64_t *n)
+{
+    if (!h || !n) return fail(TIS_ERR_ARG, "bad argument");
+    *n = h->launches;
+    return TIS_OK;
+}
+
+
+// The public handle: replicas split into groups of consecutive replicas.  Each
+// group's work is forked from and joined back into the handle's stream, so the
+// groups' kernels overlap on the GPU while calls stay ordered on one stream.
+struct tis_handle {
+    int R = 0;
+    tis_run_params prm{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<Group *> groups;
+    std::vector<cudaEvent_t> join;
+    std::vector<int> grp_of, loc_of;
+
+    ~tis_handle()
+    {
+        for (Group *g : groups) delete g;
+        for (cudaEvent_t e : join) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+// the groups' streams wait for the work queued so far on the handle's stream
+int fork_groups(tis_handle *h)
+{
+    TIS_CUDA(cudaEventRecord(h->fork, h->stream));
+    for (Group *g : h->groups) TIS_CUDA(cudaStreamWaitEvent(g->stream, h->fork, 0));
+    return TIS_OK;
+}
+
+// the handle's stream waits for everything queued on the groups' streams
+int join_groups(tis_handle *h)
+{
+    for (size_t k = 0; k < h->groups.size(); ++k) {
+        TIS_CUDA(cudaEventRecord(h->join[k], h->groups[k]->stream));
+        TIS_CUDA(cudaStreamWaitEvent(h->stream, h->join[k], 0));
+    }
+    return TIS_OK;
+}
+
+// runs fn on every group between a fork and a join; stops at the first error
+template <class F>
+int each_group(tis_handle *h, F fn)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    int rc = fork_groups(h);
+    for (size_t k = 0; k < h->groups.size() && rc == TIS_OK; ++k) rc = fn(h->groups[k]);
+    const int rj = join_groups(h);
+    return rc ? rc : rj;
+}
+
+// the group and its local index for replica r, after validating r
+int locate(tis_handle *h, int r, Group **g, int *loc)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    if (r < 0 || r >= h->R) return fail(TIS_ERR_ARG, "replica %d out of range (0..%d)", r, h->R - 1);
+    *g = h->groups[h->grp_of[r]];
+    *loc = h->loc_of[r];
+    return TIS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tis_run_params_default(tis_run_params *p)
+{
+    if (!p) return fail(TIS_ERR_ARG, "null params");
+    memset(p, 0, sizeof *p);
+    p->precision = TIS_PREC_MIXED;
+    p->noise = TIS_NOISE_REFERENCE;
+    p->sr = 12.0;
+    p->skin = 3.0;
+    p->lr_interval = 10;
+    p->use_graph = 1;
+    p->graph_steps = 20;
+    return TIS_OK;
+}
+
+int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_params *prm_in, tis_handle **out)
+{
+    tis::clear_error();
+    if (!systems || n_replicas < 1 || !out) return fail(TIS_ERR_ARG, "tis_create: bad argument");
+    tis_run_params prm;
+    if (prm_in) prm = *prm_in;
+    else tis_run_params_default(&prm);
+    if (prm.lr_interval < 1) prm.lr_interval = 10;
+    if (prm.graph_steps < 1) prm.graph_steps = 20;
+    if (prm.sr <= 0) prm.sr = 12.0;
+    if (prm.skin <= 0) prm.skin = 3.0;
+    if (prm.groups < 0) return fail(TIS_ERR_ARG, "tis_create: negative group count");
+    int G = prm.groups > 0 ? prm.groups : (n_replicas + 7) / 8;
+    G = std::min(G, n_replicas);
+    prm.groups = G;
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(TIS_ERR_CUDA, "no CUDA device available");
+    if (prm.device < 0 || prm.device >= ndev) return fail(TIS_ERR_ARG, "device %d out of range", prm.device);
+    TIS_CUDA(cudaSetDevice(prm.device));
+
+    tis_handle *h = new tis_handle();
+    h->R = n_replicas;
+    h->prm = prm;
+    auto bail = [&](int rc) {
+        delete h;
+        return rc;
+    };
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming) != cudaSuccess)
+        return bail(fail(TIS_ERR_CUDA, "cudaStreamCreate/cudaEventCreate failed"));
+    for (int k = 0; k < G; ++k) {
+        // replicas [first, last) in group k: sizes differ by at most one
+        const int first = (int)((int64_t)n_replicas * k / G), last = (int)((int64_t)n_replicas * (k + 1) / G);
+        Group *g = nullptr;
+        const int rc = grp_create(systems + first, last - first, prm, first, &g);
+        if (rc) return bail(rc);
+        h->groups.push_back(g);
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(TIS_ERR_CUDA, "cudaEventCreate failed"));
+        h->join.push_back(e);
+        for (int r = first; r < last; ++r) {
+            h->grp_of.push_back(k);
+            h->loc_of.push_back(r - first);
+        }
+    }
+    *out = h;
+    return TIS_OK;
+}
+
+int tis_destroy(tis_handle *h)
+{
+    if (h) {
+        cudaSetDevice(h->prm.device);
+        for (Group *g : h->groups) grp_destroy(g);
+        h->groups.clear();
+        cudaStreamSynchronize(h->stream);
+        delete h;
+    }
+    return TIS_OK;
+}
+
+int tis_set_state(tis_handle *h, int r, const double *x, const double *y, const double *z, const double *xo,
+                  const double *yo, const double *zo, const double *vx, const double *vy, const double *vz)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_set_state(g, loc, x, y, z, xo, yo, zo, vx, vy, vz);
+}
+
+int tis_get_state(tis_handle *h, int r, double *x, double *y, double *z, double *xo, double *yo, double *zo,
+                  double *vx, double *vy, double *vz)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_get_state(g, loc, x, y, z, xo, yo, zo, vx, vy, vz);
+}
+
+int tis_populate_lists(tis_handle *h)
+{
+    return each_group(h, [](Group *g) { return grp_populate_lists(g); });
+}
+
+int tis_get_cells(tis_handle *h, int r, int32_t *cell, int32_t *dims)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_get_cells(g, loc, cell, dims);
+}
+
+int tis_get_pairs(tis_handle *h, int r, int which, int32_t *pairs, int64_t cap, int64_t *n)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_get_pairs(g, loc, which, pairs, cap, n);
+}
+
+int tis_get_hb_status(tis_handle *h, int r, int32_t *status, int32_t *excess)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_get_hb_status(g, loc, status, excess);
+}
+
+int tis_compute_forces(tis_handle *h, int r, int mask, double *forces, double *energies)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_compute_forces(g, loc, mask, forces, energies);
+}
+
+int tis_deterministic_forces(tis_handle *h)
+{
+    return each_group(h, [](Group *g) { return grp_deterministic_forces(g); });
+}
+
+int tis_get_forces(tis_handle *h, int r, double *forces)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_get_forces(g, loc, forces);
+}
+
+int tis_full_forces(tis_handle *h)
+{
+    return each_group(h, [](Group *g) { return grp_full_forces(g); });
+}
+
+int tis_move_rigid_units(tis_handle *h)
+{
+    return each_group(h, [](Group *g) { return grp_move_rigid_units(g); });
+}
+
+int tis_check_shifts(tis_handle *h)
+{
+    return each_group(h, [](Group *g) { return grp_check_shifts(g); });
+}
+
+int tis_step(tis_handle *h, int64_t n)
+{
+    if (!h || n < 0) return fail(TIS_ERR_ARG, "tis_step: bad argument");
+    return each_group(h, [n](Group *g) { return grp_step(g, n); });
+}
+
+int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
+{
+    // stage times of the groups run one after another, summed over the groups
+    if (!h || n < 1 || !ms) return fail(TIS_ERR_ARG, "tis_profile_stages: bad argument");
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 6; ++k) ms[k] = 0;
+    for (Group *g : h->groups) {
+        double part[6];
+        const int rc = grp_profile_stages(g, n, part);
+        if (rc) return rc;
+        for (int k = 0; k < 6; ++k) ms[k] += part[k];
+    }
+    return TIS_OK;
+}
+
+int tis_sync(tis_handle *h)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    for (Group *g : h->groups) {
+        const int rc = grp_sync(g);
+        if (rc) return rc;
+    }
+    return TIS_OK;
+}
+
+int tis_get_energies(tis_handle *h, int r, double *out5)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_get_energies(g, loc, out5);
+}
+
+int tis_get_stack_energies(tis_handle *h, int r, double *out, int64_t cap, int64_t *n)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_get_stack_energies(g, loc, out, cap, n);
+}
+
+int tis_get_counters(tis_handle *h, int r, int64_t *klok, int64_t *rebuilds, int64_t *draws)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_get_counters(g, loc, klok, rebuilds, draws);
 }
 
 int tis_get_info(tis_handle *h, int *n_replicas, int *device, void **stream)
@@ -1013,16 +1295,18 @@ int tis_get_info(tis_handle *h, int *n_replicas, int *device, void **stream)
 
 int tis_replica_size(tis_handle *h, int r, int *n_particles)
 {
-    int rc = valid_replica(h, r);
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
     if (rc) return rc;
-    if (n_particles) *n_particles = h->rep[r].n;
-    return TIS_OK;
+    return grp_replica_size(g, loc, n_particles);
 }
 
 int tis_get_launch_count(tis_handle *h, int64_t *n)
 {
     if (!h || !n) return fail(TIS_ERR_ARG, "bad argument");
-    *n = h->launches;
+    int64_t total = 0;
+    for (Group *g : h->groups) total += g->launches;
+    *n = total;
     return TIS_OK;
 }
 

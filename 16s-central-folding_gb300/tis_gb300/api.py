@@ -37,7 +37,7 @@ class RunParams(C.Structure):
     _fields_ = [("precision", C.c_int32), ("noise", C.c_int32), ("sr", C.c_double), ("skin", C.c_double),
                 ("lr_interval", C.c_int32), ("cap_sr", C.c_int32), ("cap_lr", C.c_int32), ("device", C.c_int32),
                 ("use_graph", C.c_int32), ("graph_steps", C.c_int32), ("full_lists", C.c_int32),
-                ("reserved", C.c_int32 * 5)]
+                ("groups", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 _lib = None

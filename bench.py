@@ -211,7 +211,8 @@ def gpu_arm(args):
         for sp in specs:
             sp["seed"] += 100000 * rank
         systems = load_systems(files, specs)
-        eng = Engine(systems, precision=PREC_MIXED, device=local, use_graph=1, graph_steps=GRAPH_STEPS)
+        eng = Engine(systems, precision=PREC_MIXED, device=local, use_graph=1, graph_steps=GRAPH_STEPS,
+                     groups=args.groups)
         eng.populate_lists()
         stream = torch.cuda.ExternalStream(eng.stream())
         flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
@@ -330,7 +331,8 @@ def gpu_arm(args):
             "config": {"workload": "64 replicas x 346-nt TIS chain (1037 beads) + Mg 0-20 mM sweep, 76 mM KCl, "
                                    "350 A box, T 298 K, rc 30 A",
                        "replicas_per_gpu": N_REPLICAS, "particles_per_gpu": n_part, "precision": "mixed",
-                       "graph_steps": GRAPH_STEPS, "l2": "flushed (256 MB write) between timed iterations of "
+                       "graph_steps": GRAPH_STEPS, "replica_groups": eng.params.groups or (N_REPLICAS + 7) // 8,
+                       "l2": "flushed (256 MB write) between timed iterations of "
                                                          f"{GRAPH_STEPS} steps", "parallelism": f"replicas x{world}"},
             "plain_fp64_single_replica_steps_per_s": plain_sps,
             "batched_vs_plain": value / world / plain_sps,
@@ -351,6 +353,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--groups", type=int, default=0,
+                    help="replica groups run concurrently (0: the library's default)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="stop after the timed loop (no e2e, stage timing, plain path): for profiler runs")

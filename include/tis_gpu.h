@@ -119,7 +119,9 @@ typedef struct tis_run_params {
                               0 (default): a pair with a sugar or base bead is kept only within its
                               LJ range plus the skin, the only pairs that can exert a force before
                               the next rebuild */
-    int32_t reserved[5];
+    int32_t groups;        /* replica groups whose step graphs run concurrently on the GPU
+                              (0: one group per 8 replicas); results do not depend on it */
+    int32_t reserved[4];
 } tis_run_params;
 
 int tis_run_params_default(tis_run_params *p);

@@ -260,6 +260,33 @@ def test_batch_equals_single_bitwise(synth_dir):
         assert batch.counters(r) == one.counters(0)
 
 
+def test_replica_groups_equal_one_group_bitwise(synth_dir):
+    """Splitting a handle's replicas into concurrently running groups changes no
+    result: the fused graph step and the four drop-in calls both match one group."""
+    f = synth_dir["small"]
+    specs = [dict(seed=3 + 2 * k, n_mg=10 + 2 * k, n_cl=261 + 4 * k, n_k=317) for k in range(5)]
+    sys_ = [load(f, "small", **sp) for sp in specs]
+    runs = []
+    for groups, split in [(1, False), (3, False), (2, True)]:
+        e = Engine(sys_, groups=groups, graph_steps=20)
+        e.populate_lists()
+        if split:
+            for _ in range(120):
+                e.deterministic_forces()
+                e.full_forces()
+                e.move_rigid_units()
+                e.check_shifts()
+        else:
+            e.step(120)
+        e.sync()
+        runs.append(([e.get_state(r) for r in range(len(sys_))], [e.counters(r) for r in range(len(sys_))]))
+    for states, counters in runs[1:]:
+        assert counters == runs[0][1]
+        for r in range(len(sys_)):
+            for k in states[r]:
+                assert np.array_equal(states[r][k], runs[0][0][r][k]), (r, k)
+
+
 def test_split_calls_and_graph_equal_fused_step(systems):
     """The four drop-in calls (deterministic_forces, full_forces, move_rigid_units,
     check_shifts), the fused step and the captured graph give identical states."""
