@@ -10,6 +10,7 @@
 // from the FP64 positions with the reference's own image convention.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace tis {
@@ -98,11 +99,60 @@ __host__ __device__ inline uint32_t rand_value(unsigned long long seed, unsigned
     return v ? v : 1u;
 }
 
-#ifdef __CUDACC__
-// FP64 uniform exactly as the reference forms it: (double) rand () / RAND_MAX.
-__device__ inline double rand_uniform(unsigned long long seed, unsigned long long k)
+// v / (2^31 - 1) rounded to nearest double, for 1 <= v <= 2^31 - 1: the reference's
+// uniform (double) rand () / RAND_MAX from integer operations.  The binary expansion
+// of v / (2^31 - 1) is the 31-bit pattern of v repeated without end, so the 53
+// leading bits and the rounding bit come from at most three copies of it, and the
+// bits beyond are never all zero: rounding to nearest adds the rounding bit.
+__host__ __device__ inline double u31_ratio(uint32_t v)
 {
-    return (double)rand_value(seed, k) / 2147483647.0;
+    if (v >= 2147483647u) return 1.0;
+#ifdef __CUDA_ARCH__
+    const int s = 32 - __clz((int)v);  // significant bits of v
+#else
+    const int s = 32 - __builtin_clz(v);
+#endif
+    unsigned long long m = ((unsigned long long)v << 31) | v;  // the expansion from its leading one: s + 31 bits
+    int len = s + 31;
+    if (len < 54) {  // append the next copy's leading bits
+        m = (m << (54 - len)) | ((unsigned long long)v >> (31 - (54 - len)));
+        len = 54;
+    }
+    const unsigned long long b54 = m >> (len - 54);
+    const unsigned long long mant = (b54 >> 1) + (b54 & 1ull);  // below 2^53: only v = 2^31 - 1 rounds up to it
+    const unsigned long long bits = ((unsigned long long)(1023 - (31 - s) - 1) << 52) | (mant & ((1ull << 52) - 1ull));
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)bits);
+#else
+    double out;
+    memcpy(&out, &bits, sizeof out);
+    return out;
+#endif
+}
+
+// ceil(u n) clamped to [1, n] as the reference picks a list entry, for u = v / (2^31 - 1)
+// and 1 <= n < 2^20: v n / (2^31 - 1) is never an integer for v < 2^31 - 1 (the divisor
+// is prime) and lies at least 2^-31 from one, far beyond the FP64 rounding of u and u n.
+__host__ __device__ inline int pick_index(uint32_t v, int n)
+{
+    if (v >= 2147483647u) return n;
+    return (int)(((unsigned long long)v * (unsigned)n) / 2147483647ull) + 1;
+}
+
+#ifdef __CUDACC__
+// u < exp((ea - eb) / T) for u = v / (2^31 - 1), the Metropolis test of the H-bond
+// Monte Carlo (E:2290-2300).  Decided in FP32 when u lies outside a margin around the
+// FP32 estimate that covers its rounding (relative 1e-6 + 4e-7 |x|); else in FP64 as
+// written.  Identical to the FP64 test for every input.
+__device__ inline bool accept_move(uint32_t v, double ea, double eb, double T, float inv_t)
+{
+    const float x = (float)(ea - eb) * inv_t;
+    const float ef = expf(x);
+    const float uf = (float)v * (1.0f / 2147483647.0f);
+    const float m = 1.0e-6f + 4.0e-7f * fabsf(x);
+    if (uf < ef * (1.0f - m)) return true;
+    if (uf > ef * (1.0f + m)) return false;
+    return u31_ratio(v) < exp((ea - eb) / T);
 }
 
 // sqrt(-2 ln u) for u = v / (2^31-1), accurate in FP32 over the whole range.

@@ -198,13 +198,13 @@ int populate(Group *h)
 // deterministic_forces_MPI (E:2524-2586): the four force kernels are independent
 // (fixed-point atomics into one sum, the LR sum kept apart), so they run as
 // concurrent branches joined before the noise
-void enqueue_forces(Group *h)
+void enqueue_forces(Group *h, bool make_noise)
 {
     cudaEventRecord(h->fork, h->stream);
     for (int k = 0; k < 3; ++k) cudaStreamWaitEvent(h->side[k], h->fork, 0);
     tis::launch_pair_lr(h->dev, h->side[0], false, false);
     tis::launch_topology(h->dev, h->side[1], 4 | 8, false, false, true);
-    tis::launch_topology(h->dev, h->side[2], 16, false, false, true);
+    tis::launch_topology(h->dev, h->side[2], 16, false, make_noise, true);
     tis::launch_pair_sr(h->dev, h->stream, false, true);
     for (int k = 0; k < 3; ++k) {
         cudaEventRecord(h->join[k], h->side[k]);
@@ -214,9 +214,8 @@ void enqueue_forces(Group *h)
 
 void enqueue_step(Group *h)
 {
-    enqueue_forces(h);
-    tis::launch_noise(h->dev, h->stream);      // full_forces' Gaussians + recentring shift
-    tis::launch_integrate(h->dev, h->stream);  // its last block per replica runs the skin check
+    enqueue_forces(h, true);                   // the H-bond kernel also draws full_forces' Gaussians
+    tis::launch_integrate(h->dev, h->stream);  // recentring shift; last block per replica: skin check
     tis::launch_rebuild(h->dev, h->stream);
 }
 
@@ -584,7 +583,7 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         (rc = dalloc(O, &d.cell_fill, h->C)) || (rc = dalloc(O, &d.cell_list, h->P)) || (rc = dalloc(O, &d.qs, h->P)) ||
         (rc = dalloc(O, &d.n_sr, h->P)) || (rc = dalloc(O, &d.n_lr, h->P)) ||
         (rc = dalloc(O, &d.nbr_sr, (size_t)cap_sr * h->P)) || (rc = dalloc(O, &d.nbr_lr, (size_t)cap_lr * h->P)) ||
-        (rc = dalloc(O, &d.eterm, (size_t)h->R * tis::kNE)) || (rc = dalloc(O, &d.shift, (size_t)h->R * 3)) ||
+        (rc = dalloc(O, &d.eterm, (size_t)h->R * tis::kNE)) || (rc = dalloc(O, &d.shift, (size_t)h->R * 3)) || 
         (rc = dalloc(O, &h->d_scalar, 4)))
         return bail(rc);
     int4 *d_bti = nullptr;
@@ -629,10 +628,43 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
     }
     if ((rc = dalloc(O, &d.st_energy, nst3)) ||
         (rc = dalloc(O, &d.hb_status, nhb)) || (rc = dalloc(O, &d.hb_excess, nhba)) ||
-        (rc = dalloc(O, &d.excess, nhba)) || (rc = dalloc(O, &d.hb_active, nhb)) ||
+        (rc = dalloc(O, &d.hb_active, nhb)) || (rc = dalloc(O, &d.ca_exc, ca_list.size())) ||
         (rc = dalloc(O, &d.hb_K, (size_t)kscr)) || (rc = dalloc(O, &d.hb_A, ca_list.size())) ||
         (rc = dalloc(O, &d.hb_energy, nhb)) || (rc = dalloc(O, &d.hb_code, nhb)))
         return bail(rc);
+    {  // the Monte Carlo's views of the candidates: per over-valence atom its candidates, per candidate its such atoms
+        std::vector<int> ca_pos(nhba, -1), ca_coff{0}, ca_cidx, hb_coff{0}, hb_cpos;
+        int hb_nmax = 0, ca_nmax = 0, k_nmax = 0;
+        for (int r = 0; r < h->R; ++r) {
+            const tis::RepParams &Q = rp[r];
+            for (int i = Q.ca0; i < Q.ca1; ++i) {
+                const int a = ca_list[i];
+                ca_pos[a] = i - Q.ca0;
+                for (int t = hba_coff[a]; t < hba_coff[a + 1]; ++t) ca_cidx.push_back(hba_cidx[t] - Q.hb0);
+                ca_coff.push_back((int)ca_cidx.size());
+            }
+            hb_nmax = std::max(hb_nmax, Q.hb1 - Q.hb0);
+            ca_nmax = std::max(ca_nmax, Q.ca1 - Q.ca0);
+            k_nmax = std::max(k_nmax, Q.maxk);
+        }
+        for (size_t k = 0; k < nhb; ++k) {
+            for (int u = hb_aoff[k]; u < hb_aoff[k + 1]; ++u)
+                if (ca_pos[hb_aidx[u]] >= 0) hb_cpos.push_back(ca_pos[hb_aidx[u]]);
+            hb_coff.push_back((int)hb_cpos.size());
+        }
+        int *d1 = nullptr, *d2 = nullptr, *d3 = nullptr, *d4 = nullptr;
+        if ((rc = dupload(O, &d1, ca_coff)) || (rc = dupload(O, &d2, ca_cidx)) || (rc = dupload(O, &d3, hb_coff)) ||
+            (rc = dupload(O, &d4, hb_cpos)))
+            return bail(rc);
+        d.ca_coff = d1; d.ca_cidx = d2; d.hb_coff = d3; d.hb_cpos = d4;
+        d.hb_nmax = hb_nmax;
+        d.ca_nmax = ca_nmax;
+        d.k_nmax = k_nmax;
+        // energies (8 B), status and branch code (4 B each) per candidate; excess and A per atom; K
+        const size_t smem = 16 * (size_t)hb_nmax + 8 * (size_t)ca_nmax + 4 * (size_t)k_nmax + 16;
+        d.hb_smem = smem <= 160 * 1024 ? (int)smem : 0;
+    }
+    if (tis::configure_kernels(d) != 0) return bail(fail(TIS_ERR_CUDA, "cudaFuncSetAttribute failed"));
     tis::launch_quantize(h->dev, h->stream);
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess)
         return bail(fail(TIS_ERR_CUDA, "quantisation kernel failed"));
@@ -804,7 +836,7 @@ static int grp_deterministic_forces(Group *h)
     if (!h->lists_built && (rc = populate(h))) return rc;
     // E:2532: the force sum starts from zero (the fused step's integrator leaves it zero)
     TIS_CUDA(cudaMemsetAsync(h->dev.f, 0, sizeof(unsigned long long) * 3 * h->P, h->stream));
-    enqueue_forces(h);
+    enqueue_forces(h, false);
     TIS_CUDA(cudaGetLastError());
     return TIS_OK;
 }
@@ -904,8 +936,7 @@ static int grp_profile_stages(Group *h, int64_t n, double *ms)
         TIS_CUDA(cudaEventRecord(ev[1], h->stream));
         tis::launch_pair_lr(h->dev, h->stream, false, false);
         TIS_CUDA(cudaEventRecord(ev[2], h->stream));
-        tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, false, true);
-        tis::launch_noise(h->dev, h->stream);
+        tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true, true);
         TIS_CUDA(cudaEventRecord(ev[3], h->stream));
         tis::launch_integrate(h->dev, h->stream);
         TIS_CUDA(cudaEventRecord(ev[4], h->stream));

@@ -8,8 +8,8 @@
 //   k_hbond       hydrogen_bonds_interactions E:2145-2350  one block per replica:
 //                 energies, valence-limited MC, forces; full_forces' Gaussians E:2590-2611
 //   k_integrate   full_forces (application) + move_rigid_units + leap_frog_move_atom + adjust_box
-//                                             E:2612-2732, E:570-642
-//   k_control     check_shifts               E:1741-1776
+//                                             E:2612-2732, E:570-642; its last block per
+//                 replica runs check_shifts      E:1741-1776
 //   rebuild       populate_lists + separate_in_cells E:1461-1737, gated per replica
 #include <cstdio>
 
@@ -530,52 +530,43 @@ __device__ inline void leap_frog(const Dev &d, const RepParams *R, int r, int p,
     }
 }
 
-// full_forces' Gaussians (E:2594-2606) for one replica, then the recentring
-// shift of adjust_box (E:2632-2656) from the centre bead's new position.  Runs
-// in one block after every force on the replica is final.
+// full_forces' Gaussians (E:2594-2606) of one replica from draw c0 on, by the
+// threads of one block
 template <bool D>
-__device__ void noise_and_shift(const Dev &d, int r, unsigned long long &s_ctr)
+__device__ void gen_noise(const Dev &d, int r, unsigned long long c0)
 {
     const RepParams *R = d.rp + r;
-    __syncthreads();
-    const unsigned long long c0 = s_ctr;
-    if (d.noise == 0) {
-        for (int t = threadIdx.x; t < kNoise / 2; t += blockDim.x) {
-            const uint32_t v1 = rand_value(R->seed, c0 + 2 * t);
-            const uint32_t v2 = rand_value(R->seed, c0 + 2 * t + 1);
-            if (D) {  // Box-Muller as the reference forms it (E:2598-2606), in FP64
-                const double a = sqrt(-2.0 * log((double)v1 / 2147483647.0));
-                const double b = 2.0 * 3.14159265358979323846 * ((double)v2 / 2147483647.0);
-                double sn, cs;
-                sincos(b, &sn, &cs);
-                d.gnoise[r * kNoise + 2 * t] = a * cs;
-                d.gnoise[r * kNoise + 2 * t + 1] = a * sn;
-            } else {  // FP32 Box-Muller, radius accurate over the whole uniform range
-                const float a = bm_radius(v1);
-                float sn, cs;
-                sincospif(2.0f * ((float)v2 * (1.0f / 2147483647.0f)), &sn, &cs);
-                d.gnoise[r * kNoise + 2 * t] = (double)(a * cs);
-                d.gnoise[r * kNoise + 2 * t + 1] = (double)(a * sn);
-            }
+    if (d.noise != 0) return;
+    for (int t = threadIdx.x; t < kNoise / 2; t += blockDim.x) {
+        const uint32_t v1 = rand_value(R->seed, c0 + 2 * t);
+        const uint32_t v2 = rand_value(R->seed, c0 + 2 * t + 1);
+        if (D) {  // Box-Muller as the reference forms it (E:2598-2606), in FP64
+            const double a = sqrt(-2.0 * log(u31_ratio(v1)));
+            const double b = 2.0 * 3.14159265358979323846 * u31_ratio(v2);
+            double sn, cs;
+            sincos(b, &sn, &cs);
+            d.gnoise[r * kNoise + 2 * t] = a * cs;
+            d.gnoise[r * kNoise + 2 * t + 1] = a * sn;
+        } else {  // FP32 Box-Muller, radius accurate over the whole uniform range
+            const float a = bm_radius(v1);
+            float sn, cs;
+            sincospif(2.0f * ((float)v2 * (1.0f / 2147483647.0f)), &sn, &cs);
+            d.gnoise[r * kNoise + 2 * t] = (double)(a * cs);
+            d.gnoise[r * kNoise + 2 * t + 1] = (double)(a * sn);
         }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        s_ctr = c0 + kNoise;  // the reference draws them even when the noise amplitude is zero
-        double xn[3], vn[3];
-        leap_frog<D>(d, R, r, R->center, xn, vn);
-        for (int c = 0; c < 3; ++c) d.shift[3 * r + c] = R->hbox[c] - xn[c];
     }
 }
 
+// the step's Gaussians alone (the drop-in full_forces call), one block per replica;
+// the reference draws them even when the noise amplitude is zero
 template <bool D>
 __global__ void k_noise(Dev d)
 {
-    __shared__ unsigned long long s_ctr;
     const int r = blockIdx.x;
-    if (threadIdx.x == 0) s_ctr = d.rs[r].ctr;
-    noise_and_shift<D>(d, r, s_ctr);
-    if (threadIdx.x == 0) d.rs[r].ctr = s_ctr;
+    const unsigned long long c0 = d.rs[r].ctr;
+    gen_noise<D>(d, r, c0);
+    __syncthreads();
+    if (threadIdx.x == 0) d.rs[r].ctr = c0 + kNoise;
 }
 
 // ---------------------------------------------------------------------------
@@ -700,12 +691,30 @@ __global__ void __launch_bounds__(kTopoThreads) k_bonded_stack(Dev d, int mask, 
 
 // ---------------------------------------------------------------------------
 // hydrogen bonds of one replica per block: energies, the valence-limited Monte
-// Carlo, forces; then this step's Gaussians and the recentring shift
+// Carlo, forces; then (fused step) this step's Gaussians
 // ---------------------------------------------------------------------------
+// Working arrays of one replica's H-bonds, indexed by the replica's local bond
+// and over-valence atom numbers: in shared memory when they fit (Dev::hb_smem),
+// else in global scratch.  status starts as the list build left it (0: live,
+// -1: out of range) and every live bond is back to 0 when the kernel ends, so
+// the shared copy is never written back.
+struct HbWork {
+    double *en;  // energy of each live bond this step
+    int *st;     // status: 0 formed, 1 broken this step, -1 out of range
+    int *code;   // imaging branch of its dihedrals
+    int *exc;    // excess valence of each over-valence atom
+    int *al;     // over-valence atoms with positive excess (the reference's A list)
+    int *kl;     // candidate bonds of the chosen atom (the reference's K list)
+};
+
 template <bool D, bool EN>
 __global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int make_noise)
 {
     using Rl = Real<D>;
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ uint32_t s_v[32];  // the next 32 draws of the replica's rand() stream
+    __shared__ unsigned long long s_ctr;
+    __shared__ double s_red[2 * 32];
     const int r = blockIdx.x;
     const RepParams *R = d.rp + r;
     RepState *S = d.rs + r;
@@ -714,119 +723,145 @@ __global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int ma
     A.f = (decltype(A.f))d.f;
     A.P = d.P;
     A.err = 0;
-    __shared__ unsigned long long s_ctr;
-    __shared__ double s_red[2 * 32];
     if (threadIdx.x == 0) s_ctr = S->ctr;
     double e2hb = 0, e3hb = 0;
-    const int mask = do_hb ? 16 : 0;
-    __syncthreads();
+    const int hb0 = R->hb0, nhb = R->hb1 - R->hb0, ca0 = R->ca0, nca = R->ca1 - R->ca0;
 
     // ---- hydrogen_bonds_interactions (E:2145-2350) ----
-    if (mask & 16) {
-        for (int a = R->hba0 + threadIdx.x; a < R->hba1; a += blockDim.x) d.excess[a] = d.hb_excess[a];
+    if (do_hb) {
+        HbWork w;
+        if (d.hb_smem) {
+            w.en = (double *)s_dyn;
+            w.st = (int *)(w.en + d.hb_nmax);
+            w.code = w.st + d.hb_nmax;
+            w.exc = w.code + d.hb_nmax;
+            w.al = w.exc + d.ca_nmax;
+            w.kl = w.al + d.ca_nmax;
+            for (int i = threadIdx.x; i < nhb; i += blockDim.x) w.st[i] = d.hb_status[hb0 + i];
+        } else {
+            w.en = d.hb_energy + hb0;
+            w.st = d.hb_status + hb0;
+            w.code = d.hb_code + hb0;
+            w.exc = d.ca_exc + ca0;
+            w.al = d.hb_A + ca0;
+            w.kl = d.hb_K + R->kscr0;
+        }
+        for (int i = threadIdx.x; i < nca; i += blockDim.x) w.exc[i] = d.hb_excess[d.ca_list[ca0 + i]];
         __syncthreads();
         const int nact = S->n_active;
         for (int t = threadIdx.x; t < nact; t += blockDim.x) {
-            const int k = d.hb_active[R->hb0 + t];
+            const int k = d.hb_active[hb0 + t];
             const int *id = d.hb_idx + 6 * k;
             const double *nat = d.hb_nat + 6 * k;
             const Rl rr = distance<D>(P, id[1], id[4]);
             if (fabs((double)(rr - (Rl)nat[0])) > 2.0) {
-                d.hb_status[k] = 1;
-                for (int u = d.hb_aoff[k]; u < d.hb_aoff[k + 1]; ++u) atomicSub(d.excess + d.hb_aidx[u], 1);
-                d.hb_energy[k] = 0.0;
+                w.st[k - hb0] = 1;
+                for (int u = d.hb_coff[k]; u < d.hb_coff[k + 1]; ++u) atomicSub(w.exc + d.hb_cpos[u], 1);
+                w.en[k - hb0] = 0.0;
                 continue;
             }
             int code;
             const Rl q = six_q<D>(P, id, nat, rr - (Rl)nat[0], Rl(0), code);
-            d.hb_energy[k] = (double)((Rl)d.hb_E[k] * exp_(-q));
-            d.hb_code[k] = code;
+            w.en[k - hb0] = (double)((Rl)d.hb_E[k] * exp_(-q));
+            w.code[k - hb0] = code;
         }
         __syncthreads();
         if (threadIdx.x < 32) {  // valence-limited Monte Carlo (E:2239-2315), one warp
             const int lane = threadIdx.x;
             const unsigned lt = (1u << lane) - 1u;
             unsigned long long ctr = s_ctr;
-            const int ca0 = R->ca0, nca = R->ca1 - R->ca0;
             const double T = R->T;
+            const float inv_t = 1.0f / R->Tf;
             int guard = nact + 2;
             while (guard-- > 0) {
+                // A: atoms with positive excess, in atom order
                 int nA = 0;
                 for (int base = 0; base < nca; base += 32) {
                     const int i = base + lane;
-                    const int a = i < nca ? d.ca_list[ca0 + i] : -1;
-                    const bool pos = a >= 0 && d.excess[a] > 0;
+                    const bool pos = i < nca && w.exc[i] > 0;
                     const unsigned m = __ballot_sync(kFull, pos);
-                    if (pos) d.hb_A[ca0 + nA + __popc(m & lt)] = a;
+                    if (pos) w.al[nA + __popc(m & lt)] = i;
                     nA += __popc(m);
                 }
-                __syncwarp();
                 if (nA == 0) break;
-                int bad = 0;
-                if (lane == 0) {
-                    double u = rand_uniform(R->seed, ctr++);
-                    int j = (int)ceil(u * nA);
-                    if (j == nA + 1) j = nA;
-                    if (j == 0) j = 1;
-                    const int atom = d.hb_A[ca0 + j - 1];
-                    int *K = d.hb_K + R->kscr0;
-                    int nK = 0;
-                    for (int t = d.hba_coff[atom]; t < d.hba_coff[atom + 1]; ++t) {
-                        const int k = d.hba_cidx[t];
-                        if (d.hb_status[k] == 0 && nK < R->maxk) K[nK++] = k;
-                    }
-                    if (nK == 0) bad = 1;
-                    else {
-                        for (int i = 1; i <= nK; ++i) {
-                            u = rand_uniform(R->seed, ctr++);
-                            j = (int)ceil(u * nK);
-                            if (j == nK + 1) j = nK;
-                            if (j == 0) j = 1;
-                            const int tmp = K[i - 1];
-                            K[i - 1] = K[j - 1];
-                            K[j - 1] = tmp;
-                        }
-                        int k = K[0];
-                        for (int i = 2; i <= nK; ++i) {
-                            const int c = K[i - 1];
-                            const double acc = exp((d.hb_energy[c] - d.hb_energy[k]) / T);
-                            u = rand_uniform(R->seed, ctr++);
-                            if (u < acc) k = c;
-                        }
-                        d.hb_status[k] = 1;
-                        for (int t = d.hb_aoff[k]; t < d.hb_aoff[k + 1]; ++t) d.excess[d.hb_aidx[t]] -= 1;
-                    }
-                }
-                bad = __shfl_sync(kFull, bad, 0);
+                // draws ctr, ctr+1, ...: the atom, the K shuffle, the acceptances
+                s_v[lane] = rand_value(R->seed, ctr + lane);
                 __syncwarp();
-                if (bad) {
+                const int atom = w.al[pick_index(s_v[0], nA) - 1];
+                // K: the atom's candidates still formed, in candidate order
+                const int c0 = d.ca_coff[ca0 + atom], nc = d.ca_coff[ca0 + atom + 1] - c0;
+                int nK = 0;
+                for (int base = 0; base < nc; base += 32) {
+                    const int t = base + lane;
+                    const int k = t < nc ? d.ca_cidx[c0 + t] : 0;
+                    const bool ok = t < nc && w.st[k] == 0;
+                    const unsigned m = __ballot_sync(kFull, ok);
+                    if (ok) w.kl[nK + __popc(m & lt)] = k;
+                    nK += __popc(m);
+                }
+                __syncwarp();
+                if (nK == 0) {
+                    ctr += 1;
                     A.err |= kErrRange;
                     break;
                 }
+                if (lane == 0)
+                    for (int i = 1; i <= nK; ++i) {
+                        const int jj = pick_index(i < 32 ? s_v[i] : rand_value(R->seed, ctr + i), nK);
+                        const int tmp = w.kl[i - 1];
+                        w.kl[i - 1] = w.kl[jj - 1];
+                        w.kl[jj - 1] = tmp;
+                    }
+                __syncwarp();
+                // Metropolis walk over the shuffled K (draws nK+1 .. 2nK-1): lane a*nK+b
+                // decides whether candidate a replaces candidate b
+                int kc = 0;
+                if (nK * nK <= 32) {
+                    const int a = lane / nK, b = lane - a * nK;
+                    const bool acc = lane < nK * nK && a >= 1 &&
+                                     accept_move(s_v[nK + a], w.en[w.kl[a]], w.en[w.kl[b]], T, inv_t);
+                    const unsigned dm = __ballot_sync(kFull, acc);
+                    for (int a2 = 1; a2 < nK; ++a2)
+                        if ((dm >> (a2 * nK + kc)) & 1u) kc = a2;
+                } else if (lane == 0) {
+                    for (int i = 2; i <= nK; ++i) {
+                        const int di = nK + i - 1;
+                        const uint32_t v = di < 32 ? s_v[di] : rand_value(R->seed, ctr + di);
+                        if (accept_move(v, w.en[w.kl[i - 1]], w.en[w.kl[kc]], T, inv_t)) kc = i - 1;
+                    }
+                }
+                if (lane == 0) {
+                    const int k = w.kl[kc];
+                    w.st[k] = 1;
+                    for (int u = d.hb_coff[hb0 + k]; u < d.hb_coff[hb0 + k + 1]; ++u) w.exc[d.hb_cpos[u]] -= 1;
+                }
+                ctr += 2 * nK;
+                __syncwarp();
             }
             if (lane == 0) s_ctr = ctr;
         }
         __syncthreads();
         for (int t = threadIdx.x; t < nact; t += blockDim.x) {
-            const int k = d.hb_active[R->hb0 + t];
-            if (d.hb_status[k] == 1) {
-                d.hb_status[k] = 0;
+            const int k = d.hb_active[hb0 + t];
+            if (w.st[k - hb0] == 1) {
+                w.st[k - hb0] = 0;
                 continue;
             }
-            const Rl w = -(Rl)d.hb_energy[k];
-            if (d.hb_dode[k]) e3hb -= (double)w;
-            else e2hb -= (double)w;
-            six_force<D>(P, A, d.hb_idx + 6 * k, d.hb_nat + 6 * k, d.hb_code[k], w);
+            const Rl wk = -(Rl)w.en[k - hb0];
+            if (d.hb_dode[k]) e3hb -= (double)wk;
+            else e2hb -= (double)wk;
+            six_force<D>(P, A, d.hb_idx + 6 * k, d.hb_nat + 6 * k, w.code[k - hb0], wk);
         }
     }
-
-    // ---- full_forces: the step's Gaussians, then the recentring shift ----
-    if (make_noise) noise_and_shift<D>(d, r, s_ctr);
+    __syncthreads();
+    // ---- full_forces: the step's Gaussians follow the Monte Carlo draws ----
+    const unsigned long long c1 = s_ctr;
+    if (make_noise) gen_noise<D>(d, r, c1);
 
     double v[2] = {e2hb, e3hb};
     block_sum<2>(v, s_red);
     if (threadIdx.x == 0) {
-        S->ctr = s_ctr;
+        S->ctr = make_noise ? c1 + kNoise : c1;
         if (do_hb) { S->e2hb = v[0]; S->e3hb = v[1]; }
         if (EN) {
             double *e = d.eterm + r * kNE;
@@ -838,6 +873,38 @@ __global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int ma
 
 __device__ void control_step(const Dev &d, int r);
 
+// x < 0 and x > L (L > 0) on the bit patterns, as IEEE comparisons decide them for
+// finite x (-0.0 is not below zero): integer instructions instead of FP64 compares
+__device__ inline bool below_zero(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return b < 0 && b != (long long)0x8000000000000000ull;
+}
+__device__ inline bool above(double x, double L) { return __double_as_longlong(x) > __double_as_longlong(L); }
+
+// |x| < 2^20 and finite, from the exponent field
+__device__ inline bool bounded(double x)
+{
+    return ((unsigned)(__double_as_longlong(x) >> 52) & 0x7ffu) < 1023u + 20u;
+}
+
+// the recentring shift of adjust_box (E:2632-2656): the centre bead's new position
+// moved to the box centre; one warp per replica, after every force is final
+template <bool D>
+__global__ void k_shift(Dev d)
+{
+    const int r = blockIdx.x;
+    const RepParams *R = d.rp + r;
+    if (threadIdx.x == 0) {
+        double xn[3], vn[3];
+        leap_frog<D>(d, R, r, R->center, xn, vn);
+        for (int c = 0; c < 3; ++c) d.shift[3 * r + c] = R->hbox[c] - xn[c];
+    }
+}
+
+// move_rigid_units (E:2660-2731) of one particle per thread: leap-frog, the
+// recentring shift, the periodic wrap of the ions; the replica's last block to
+// finish runs the skin check
 template <bool D>
 __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
 {
@@ -846,7 +913,7 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
     __shared__ unsigned long long s_max;
     if (threadIdx.x == 0) s_max = 0ull;
     __syncthreads();
-    const double s_shift[3] = {d.shift[3 * r], d.shift[3 * r + 1], d.shift[3 * r + 2]};
+    const double sh[3] = {d.shift[3 * r], d.shift[3 * r + 1], d.shift[3 * r + 2]};
     const int p = blockIdx.x * kBlock + threadIdx.x;
     const int4 qp = d.q[p];
     double d2 = 0.0;
@@ -856,31 +923,33 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
         leap_frog<D>(d, R, r, p, xn, vn);
         double xo[3] = {d.x[p], d.y[p], d.z[p]};
         for (int c = 0; c < 3; ++c) {
-            xn[c] = xn[c] + s_shift[c];
-            xo[c] = xo[c] + s_shift[c];
+            xn[c] = xn[c] + sh[c];
+            xo[c] = xo[c] + sh[c];
         }
         if (p - R->p0 >= R->nrna) {  // periodic wrap of the ions (E:2676-2731)
             for (int c = 0; c < 3; ++c) {
-                if (xn[c] < 0) { xn[c] += R->box[c]; xo[c] += R->box[c]; }
-                if (xn[c] > R->box[c]) { xn[c] -= R->box[c]; xo[c] -= R->box[c]; }
+                if (below_zero(xn[c])) { xn[c] += R->box[c]; xo[c] += R->box[c]; }
+                if (above(xn[c], R->box[c])) { xn[c] -= R->box[c]; xo[c] -= R->box[c]; }
             }
         }
         for (int c = 0; c < 3; ++c) {
             const double e = xn[c] - xo[c];
             d2 += e * e;
         }
-        if (!(fabs(xn[0]) + fabs(xn[1]) + fabs(xn[2]) + fabs(vn[0]) + fabs(vn[1]) + fabs(vn[2]) < 1.0e6))
-            err |= kErrNonFinite;
+        // a runaway or non-finite particle (|x| or |v| component >= 2^20) stops the run
+        bool ok = true;
+        for (int c = 0; c < 3; ++c) ok = ok && bounded(xn[c]) && bounded(vn[c]);
+        if (!ok) err |= kErrNonFinite;
         d.x[p] = xn[0]; d.y[p] = xn[1]; d.z[p] = xn[2];
         d.xo[p] = xo[0]; d.yo[p] = xo[1]; d.zo[p] = xo[2];
         d.vx[p] = vn[0]; d.vy[p] = vn[1]; d.vz[p] = vn[2];
         d.f[p] = 0ull;  // consumed: the next step's force kernels accumulate from zero
         d.f[d.P + p] = 0ull;
         d.f[2 * d.P + p] = 0ull;
-        int4 q = qp;
-        q.x = (int)(unsigned)(long long)floor(xn[0] * R->qinv[0]);
-        q.y = (int)(unsigned)(long long)floor(xn[1] * R->qinv[1]);
-        q.z = (int)(unsigned)(long long)floor(xn[2] * R->qinv[2]);
+        int4 q = qp;  // floor(x L / 2^32) modulo 2^32, one rounding conversion per axis
+        q.x = (int)(unsigned)__double2ll_rd(xn[0] * R->qinv[0]);
+        q.y = (int)(unsigned)__double2ll_rd(xn[1] * R->qinv[1]);
+        q.z = (int)(unsigned)__double2ll_rd(xn[2] * R->qinv[2]);
         d.q[p] = q;
     }
     // check_shifts (E:1745-1762): max |x - x_old|^2; non-negative doubles order as integers
@@ -908,7 +977,6 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
     }
 }
 
-// check_shifts (E:1741-1776) and the LR gate of deterministic_forces_MPI (E:2550)
 // check_shifts (E:1741-1776) and the LR gate of deterministic_forces_MPI (E:2550)
 // for replica r; thread 0 decides, the block zeroes the cell counts on a rebuild
 __device__ void control_step(const Dev &d, int r)
@@ -1362,15 +1430,29 @@ void launch_topology(const Dev &d, cudaStream_t s, int mask, bool en, bool make_
         }
     }
     const int hb = (mask & 16) ? 1 : 0, mn = make_noise ? 1 : 0;
+    const size_t sm = hb ? (size_t)d.hb_smem : 0;
     if (hb || mn) {
         if (d.fp64) {
-            if (en) k_hbond<true, true><<<d.R, kTopoThreads, 0, s>>>(d, hb, mn);
-            else k_hbond<true, false><<<d.R, kTopoThreads, 0, s>>>(d, hb, mn);
+            if (en) k_hbond<true, true><<<d.R, kTopoThreads, sm, s>>>(d, hb, mn);
+            else k_hbond<true, false><<<d.R, kTopoThreads, sm, s>>>(d, hb, mn);
         } else {
-            if (en) k_hbond<false, true><<<d.R, kTopoThreads, 0, s>>>(d, hb, mn);
-            else k_hbond<false, false><<<d.R, kTopoThreads, 0, s>>>(d, hb, mn);
+            if (en) k_hbond<false, true><<<d.R, kTopoThreads, sm, s>>>(d, hb, mn);
+            else k_hbond<false, false><<<d.R, kTopoThreads, sm, s>>>(d, hb, mn);
         }
     }
+}
+
+int configure_kernels(const Dev &d)
+{
+    cudaError_t e = cudaSuccess;
+    if (d.hb_smem > 48 * 1024) {
+        const int b = d.hb_smem;
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hbond<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hbond<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hbond<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hbond<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    }
+    return (int)e;
 }
 
 void launch_noise(const Dev &d, cudaStream_t s)
@@ -1381,8 +1463,13 @@ void launch_noise(const Dev &d, cudaStream_t s)
 
 void launch_integrate(const Dev &d, cudaStream_t s)
 {
-    if (d.fp64) k_integrate<true><<<d.nblk, kBlock, 0, s>>>(d);
-    else k_integrate<false><<<d.nblk, kBlock, 0, s>>>(d);
+    if (d.fp64) {
+        k_shift<true><<<d.R, 32, 0, s>>>(d);
+        k_integrate<true><<<d.nblk, kBlock, 0, s>>>(d);
+    } else {
+        k_shift<false><<<d.R, 32, 0, s>>>(d);
+        k_integrate<false><<<d.nblk, kBlock, 0, s>>>(d);
+    }
 }
 
 void launch_control(const Dev &d, cudaStream_t s) { k_control<<<d.R, 128, 0, s>>>(d); }
@@ -1403,7 +1490,7 @@ void launch_force_all_rebuild(const Dev &d, cudaStream_t s) { k_force_rebuild<<<
 
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out) { k_rg<<<1, 256, 0, s>>>(d, replica, out); }
 
-// pair SR, pair LR, bonded+stacking, H-bonds, noise+shift, integrate (+skin check), 6 rebuild kernels
+// pair SR, pair LR, bonded+stacking, H-bonds (+Gaussians), shift, integrate (+skin check), 6 rebuild kernels
 int kernel_launches_per_step() { return 12; }
 
 }  // namespace tis

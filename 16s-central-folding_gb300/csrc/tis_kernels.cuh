@@ -43,9 +43,13 @@ struct Dev {
     const int *hb_aoff, *hb_aidx;   // atoms of every candidate (CSR, global ids)
     const int *hba_val, *hba_coff, *hba_cidx, *hba_n;
     const int *ca_list;             // atoms whose candidate count exceeds their valence
-    int *hb_status, *hb_excess, *excess, *hb_active, *hb_K, *hb_A;
+    const int *ca_coff, *ca_cidx;   // candidates of each such atom (CSR; replica-local bond numbers)
+    const int *hb_coff, *hb_cpos;   // such atoms of each candidate (CSR; replica-local numbers in ca_list)
+    int *hb_status, *hb_excess, *hb_active, *hb_K, *hb_A, *ca_exc;
     double *hb_energy;
     int *hb_code;               // imaging branch of the three native dihedrals
+    int hb_nmax, ca_nmax, k_nmax;   // largest per-replica candidate, over-valence atom and K counts
+    int hb_smem;                // dynamic shared bytes of the H-bond kernel (0: its arrays stay in global scratch)
     double *eterm;              // R x kNE (per-term energies, compute_forces only)
     double *shift;              // R x 3, recentring shift of the current step (adjust_box)
     const int *cell_rep;        // replica of every cell
@@ -60,8 +64,9 @@ void launch_quantize(const Dev &d, cudaStream_t s);
 void launch_pair_sr(const Dev &d, cudaStream_t s, bool energies, bool excl_in_list);
 void launch_pair_lr(const Dev &d, cudaStream_t s, bool energies, bool force_all);
 void launch_topology(const Dev &d, cudaStream_t s, int mask, bool energies, bool make_noise, bool excl_in_list);
-void launch_noise(const Dev &d, cudaStream_t s);  // Gaussians + recentring shift only
-void launch_integrate(const Dev &d, cudaStream_t s);
+void launch_noise(const Dev &d, cudaStream_t s);  // the step's Gaussians only
+int configure_kernels(const Dev &d);              // kernel attributes (shared-memory limits); cudaError_t
+void launch_integrate(const Dev &d, cudaStream_t s);  // recentring shift, then the particles
 void launch_control(const Dev &d, cudaStream_t s);
 void launch_rebuild(const Dev &d, cudaStream_t s);  // gated on RepState::rebuild
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s);
