@@ -546,6 +546,10 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, prm.device);
         d.search_warps = std::max(4, sms * 8 * 4);  // 8 blocks of 4 warps per SM
         d.sm_count = std::max(1, sms);
+        int nc_max = 1;
+        for (auto &Q : rp) nc_max = std::max(nc_max, Q.nc);
+        d.nc_max = nc_max;
+        d.cell_smem = 8 * nc_max <= 160 * 1024 ? 8 * nc_max : 0;  // count/first slot and fill counter per cell
     }
     auto &O = h->owned;
     int rc = TIS_OK;

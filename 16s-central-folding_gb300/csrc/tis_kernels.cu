@@ -978,12 +978,12 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
 }
 
 // check_shifts (E:1741-1776) and the LR gate of deterministic_forces_MPI (E:2550)
-// for replica r; thread 0 decides, the block zeroes the cell counts on a rebuild
+// for replica r, by thread 0.  RepState::rebuild stays as decided here until the
+// next step's decision: the rebuild kernels that follow read it.
 __device__ void control_step(const Dev &d, int r)
 {
     const RepParams *R = d.rp + r;
     RepState *S = d.rs + r;
-    __shared__ int s_reb;
     if (threadIdx.x == 0) {
         const double d2 = __longlong_as_double((long long)atomicExch(&S->maxd2, 0ull));
         const double sh = sqrt(d2);
@@ -998,27 +998,18 @@ __device__ void control_step(const Dev &d, int r)
         S->e3st = S->e3st_acc;
         S->e2st_acc = 0.0;
         S->e3st_acc = 0.0;
-        s_reb = reb;
     }
-    __syncthreads();
-    if (s_reb)
-        for (int c = threadIdx.x; c < R->nc; c += blockDim.x) d.cell_count[R->c0 + c] = 0;
 }
-
-__global__ void k_control(Dev d) { control_step(d, blockIdx.x); }
 
 __global__ void k_force_rebuild(Dev d)
 {
-    const int r = blockIdx.x;
-    const RepParams *R = d.rp + r;
-    RepState *S = d.rs + r;
+    RepState *S = d.rs + blockIdx.x;
     if (threadIdx.x == 0) {
         S->rebuild = 1;
         S->progress = 0.0;
         S->lr_now = 1;
         S->maxd2 = 0ull;
     }
-    for (int c = threadIdx.x; c < R->nc; c += blockDim.x) d.cell_count[R->c0 + c] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1061,42 +1052,58 @@ __device__ inline bool rebuild_item(const Dev &d, int per, int i, int &r, int &o
     return false;
 }
 
-__global__ void __launch_bounds__(kBlock) k_cell_assign(Dev d)
-{
-    const int r = d.blk_rep[blockIdx.x];
-    if (!d.rs[r].rebuild) return;
-    const RepParams *R = d.rp + r;
-    const int p = blockIdx.x * kBlock + threadIdx.x;
-    if (!((d.q[p].w >> 16) & 1)) {
-        d.cell_of[p] = -1;
-        return;
-    }
-    const int i1 = cell_axis(d.x[p], R->box[0], R->lcell[0]);
-    const int i2 = cell_axis(d.y[p], R->box[1], R->lcell[1]);
-    const int i3 = cell_axis(d.z[p], R->box[2], R->lcell[2]);
-    if (i1 < 1 || i1 > R->mc[0] || i2 < 1 || i2 > R->mc[1] || i3 < 1 || i3 > R->mc[2]) {
-        d.cell_of[p] = -1;
-        atomicOr(&d.rs[r].err, kErrRange);
-        return;
-    }
-    const int c = (i1 - 1) * R->mc[1] * R->mc[2] + (i2 - 1) * R->mc[2] + (i3 - 1);
-    d.cell_of[p] = c;
-    atomicAdd(d.cell_count + R->c0 + c, 1);
-}
+// populate_lists' cell binning (separate_in_cells, E:1461-1542) and hydrogen-bond
+// candidate status (E:1698-1736) of one rebuilding replica per block.  Counting
+// and filling run on shared-memory cell counters when the replica's cells fit
+// (Dev::cell_smem), else on the global ones.  In FP64 mode each cell's particles
+// are put in index order, as the reference appends them (E:1536-1540), so that
+// list order and FP64 summation order are reproducible; mixed-precision sums are
+// exact in fixed point and need no order.  Then the packed positions are copied
+// in cell order, so the pair search reads each cell's candidates contiguously.
+constexpr int kCellThreads = 1024;
 
-__global__ void k_cell_scan(Dev d)
+template <bool D>
+__global__ void __launch_bounds__(kCellThreads) k_cells(Dev d)
 {
+    extern __shared__ int s_cells[];
     __shared__ int s_warp[32];
     __shared__ int s_carry;
-    for (int r = blockIdx.x; r < d.R; r += gridDim.x) {
-    if (!d.rs[r].rebuild) continue;
+    const int r = blockIdx.x;
+    RepState *S = d.rs + r;
+    if (!S->rebuild) return;
     const RepParams *R = d.rp + r;
-    if (threadIdx.x == 0) s_carry = 0;
+    const int nc = R->nc, tid = threadIdx.x, bd = blockDim.x, lane = tid & 31, w = tid >> 5, nw = bd >> 5;
+    // per cell: particle count, first slot (in place of the count in shared memory), fill counter
+    int *cnt = d.cell_smem ? s_cells : d.cell_count + R->c0;
+    int *first = d.cell_smem ? s_cells : d.cell_start + R->c0;
+    int *fill = d.cell_smem ? s_cells + d.nc_max : d.cell_fill + R->c0;
+    for (int c = tid; c < nc; c += bd) {
+        cnt[c] = 0;
+        fill[c] = 0;
+    }
+    if (tid == 0) s_carry = 0;
     __syncthreads();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int base = 0; base < R->nc; base += blockDim.x) {
-        const int c = base + threadIdx.x;
-        const int v = c < R->nc ? d.cell_count[R->c0 + c] : 0;
+    for (int i = tid; i < R->npad; i += bd) {
+        const int p = R->p0 + i;
+        int c = -1;
+        if ((d.q[p].w >> 16) & 1) {
+            const int i1 = cell_axis(d.x[p], R->box[0], R->lcell[0]);
+            const int i2 = cell_axis(d.y[p], R->box[1], R->lcell[1]);
+            const int i3 = cell_axis(d.z[p], R->box[2], R->lcell[2]);
+            if (i1 < 1 || i1 > R->mc[0] || i2 < 1 || i2 > R->mc[1] || i3 < 1 || i3 > R->mc[2]) {
+                atomicOr(&S->err, kErrRange);
+            } else {
+                c = (i1 - 1) * R->mc[1] * R->mc[2] + (i2 - 1) * R->mc[2] + (i3 - 1);
+                atomicAdd(cnt + c, 1);
+            }
+        }
+        d.cell_of[p] = c;
+    }
+    __syncthreads();
+    // exclusive scan of the counts: first slot of every cell
+    for (int base = 0; base < nc; base += bd) {
+        const int c = base + tid;
+        const int v = c < nc ? cnt[c] : 0;
         int incl = v;
         for (int o = 1; o < 32; o <<= 1) {
             const int t = __shfl_up_sync(kFull, incl, o);
@@ -1114,74 +1121,89 @@ __global__ void k_cell_scan(Dev d)
         }
         __syncthreads();
         const int excl = s_carry + (w > 0 ? s_warp[w - 1] : 0) + incl - v;
-        if (c < R->nc) {
+        if (c < nc) {
+            first[c] = excl;
             d.cell_start[R->c0 + c] = excl;
-            d.cell_fill[R->c0 + c] = 0;
+            d.cell_count[R->c0 + c] = v;
         }
         __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) s_carry = excl + v;
+        if (tid == bd - 1) s_carry = excl + v;
         __syncthreads();
     }
+    const int nslots = s_carry;
+    for (int i = tid; i < R->npad; i += bd) {
+        const int p = R->p0 + i;
+        const int c = d.cell_of[p];
+        if (c >= 0) d.cell_list[R->p0 + first[c] + atomicAdd(fill + c, 1)] = p;
     }
-}
-
-__global__ void __launch_bounds__(kBlock) k_cell_fill(Dev d)
-{
-    const int r = d.blk_rep[blockIdx.x];
-    if (!d.rs[r].rebuild) return;
-    const RepParams *R = d.rp + r;
-    const int p = blockIdx.x * kBlock + threadIdx.x;
-    const int c = d.cell_of[p];
-    if (c < 0) return;
-    const int slot = atomicAdd(d.cell_fill + R->c0 + c, 1);
-    d.cell_list[R->p0 + d.cell_start[R->c0 + c] + slot] = p;
-}
-
-// One warp per cell: in FP64 mode the cell's particles are put in index order,
-// as the reference appends them (E:1536-1540), so that list order and hence
-// FP64 summation order are reproducible; mixed-precision sums are exact in fixed
-// point and need no order.  Then the packed positions are copied in cell order
-// so the pair search reads each cell's candidates contiguously.
-template <bool D>
-__global__ void k_cell_order(Dev d)
-{
-    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    int r, off;
-    for (int item = wid; rebuild_item(d, 1, item, r, off); item += nw) {
-    const RepParams *R = d.rp + r;
-    {
-    const int cg = R->c0 + off;
-    const int base = R->p0 + d.cell_start[cg];
-    const int n = d.cell_count[cg];
-    int *seg = d.cell_list + base;
-    if (D && n > 1 && n <= 256) {  // rank sort, at most 8 particles per lane held in registers
-        int v[8], rk[8];
-        int m = 0;
-        for (int i = lane; i < n; i += 32, ++m) {
-            v[m] = seg[i];
-            int c = 0;
-            for (int k = 0; k < n; ++k) c += seg[k] < v[m];
-            rk[m] = c;
-        }
-        __syncwarp();
-        for (int t = 0; t < m; ++t) seg[rk[t]] = v[t];
-        __syncwarp();
-    } else if (D && n > 256) {  // very full cell: insertion sort by one lane
-        if (lane == 0)
-            for (int i = 1; i < n; ++i) {
-                const int v = seg[i];
-                int j = i - 1;
-                while (j >= 0 && seg[j] > v) {
-                    seg[j + 1] = seg[j];
-                    --j;
+    __syncthreads();
+    if (D)  // one warp per cell: rank sort (at most 8 particles per lane), or insertion sort by one lane
+        for (int c = w; c < nc; c += nw) {
+            const int n = d.cell_count[R->c0 + c];
+            int *seg = d.cell_list + R->p0 + first[c];
+            if (n > 1 && n <= 256) {
+                int v[8], rk[8];
+                int m = 0;
+                for (int i = lane; i < n; i += 32, ++m) {
+                    v[m] = seg[i];
+                    int k = 0;
+                    for (int u = 0; u < n; ++u) k += seg[u] < v[m];
+                    rk[m] = k;
                 }
-                seg[j + 1] = v;
+                __syncwarp();
+                for (int t = 0; t < m; ++t) seg[rk[t]] = v[t];
+                __syncwarp();
+            } else if (n > 256) {
+                if (lane == 0)
+                    for (int i = 1; i < n; ++i) {
+                        const int v = seg[i];
+                        int j = i - 1;
+                        while (j >= 0 && seg[j] > v) {
+                            seg[j + 1] = seg[j];
+                            --j;
+                        }
+                        seg[j + 1] = v;
+                    }
+                __syncwarp();
             }
-        __syncwarp();
+        }
+    __syncthreads();
+    for (int i = tid; i < nslots; i += bd) d.qs[R->p0 + i] = d.q[d.cell_list[R->p0 + i]];
+
+    // hydrogen-bond candidates: live (0) when the central pair is within the SR radius
+    for (int a = R->hba0 + tid; a < R->hba1; a += bd) d.hb_excess[a] = d.hba_n[a] - d.hba_val[a];
+    __syncthreads();
+    for (int k = R->hb0 + tid; k < R->hb1; k += bd) {
+        const int a = d.hb_idx[6 * k + 1], b = d.hb_idx[6 * k + 4];
+        const int st = (a != b && exact_r2(d, R, a, b) <= R->r2sr) ? 0 : -1;
+        d.hb_status[k] = st;
+        if (st != 0)
+            for (int u = d.hb_aoff[k]; u < d.hb_aoff[k + 1]; ++u) atomicSub(d.hb_excess + d.hb_aidx[u], 1);
     }
-    for (int i = lane; i < n; i += 32) d.qs[base + i] = d.q[seg[i]];
+    if (tid == 0) s_carry = 0;
+    __syncthreads();
+    // ordered compaction of the live candidates
+    const int nh = R->hb1 - R->hb0;
+    for (int base = 0; base < nh; base += bd) {
+        const int k = R->hb0 + base + tid;
+        const bool live = (base + tid < nh) && d.hb_status[k] == 0;
+        const unsigned m = __ballot_sync(kFull, live);
+        if (lane == 0) s_warp[w] = __popc(m);
+        __syncthreads();
+        int off = s_carry;
+        for (int t = 0; t < w; ++t) off += s_warp[t];
+        if (live) d.hb_active[R->hb0 + off + __popc(m & ((1u << lane) - 1u))] = k;
+        __syncthreads();
+        if (tid == 0) {
+            int tot = 0;
+            for (int t = 0; t < nw; ++t) tot += s_warp[t];
+            s_carry += tot;
+        }
+        __syncthreads();
     }
+    if (tid == 0) {
+        S->n_active = s_carry;
+        S->rebuilds += 1;
     }
 }
 
@@ -1211,6 +1233,7 @@ __device__ inline int axis_neighbours(int i, int m, int out[3])
 template <bool D>
 __global__ void __launch_bounds__(128) k_pair_search(Dev d)
 {
+    __shared__ int s_pre[4][32], s_beg[4][32];  // per warp: candidate offsets and first slots of its cells
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1238,123 +1261,87 @@ __global__ void __launch_bounds__(128) k_pair_search(Dev d)
             int exl[kExcl];
             const int nex = d.n_excl[p];
             for (int t2 = 0; t2 < kExcl; ++t2) exl[t2] = t2 < nex ? d.excl[(size_t)t2 * P + p] : -1;
-            int nsr = 0, nlr = 0;
-            for (int a = 0; a < m1; ++a)
-                for (int b = 0; b < m2; ++b)
-                    for (int e = 0; e < m3; ++e) {
-                        const int cc = (n1[a] - 1) * R->mc[1] * R->mc[2] + (n2[b] - 1) * R->mc[2] + (n3[e] - 1);
-                        const int start = R->p0 + d.cell_start[R->c0 + cc];
-                        const int cnt = d.cell_count[R->c0 + cc];
-                        for (int t0 = 0; t0 < cnt; t0 += 32) {
-                            const int t = t0 + lane;
-                            int cls = 0, j = -1;  // 0 none, 1 SR, 2 LR
-                            if (t < cnt) {
-                                j = d.cell_list[start + t];
-                                if (j != p) {
-                                    const int4 qj = d.qs[start + t];
-                                    const bool ch = chp && is_charged((qj.w >> 8) & 0xff);
-                                    float r2f;
-                                    {
-                                        const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
-                                        const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
-                                        const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
-                                        r2f = dx * dx + dy * dy + dz * dz;
-                                    }
-                                    if (D) {
-                                        const double r2 = exact_r2(d, R, p, j);
-                                        cls = r2 <= R->r2sr ? 1 : ((ch && r2 <= R->r2lr) ? 2 : 0);
-                                    } else {
-                                        const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
-                                        const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
-                                        const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
-                                        const float r2 = dx * dx + dy * dy + dz * dz;
-                                        if (r2 < sr_lo) cls = 1;
-                                        else if (r2 > sr_hi && (!ch || r2 > lr_hi)) cls = 0;
-                                        else if (r2 > sr_hi && r2 < lr_lo) cls = 2;
-                                        else {
-                                            const double e2 = exact_r2(d, R, p, j);
-                                            cls = e2 <= R->r2sr ? 1 : ((ch && e2 <= R->r2lr) ? 2 : 0);
-                                        }
-                                    }
-                                    // pruned list: a pair with an uncharged bead can only exert LJ, which
-                                    // vanishes beyond D_LJ; the skin keeps it exact until the next rebuild
-                                    if (cls == 1 && !d.full_lists && !ch &&
-                                        r2f > R->ljkeep2[jn12(qp.w & 0xff, qj.w & 0xff)])
-                                        cls = 0;
-                                }
-                            }
-                            const unsigned bs = __ballot_sync(kFull, cls == 1), bl = __ballot_sync(kFull, cls == 2);
-                            if (cls == 1) {
-                                int m = 0;  // how often the reference subtracts this pair's LJ again
-                                for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
-                                const int pos = nsr + __popc(bs & lt);
-                                if (pos < d.cap_sr) d.nbr_sr[nb_idx(pos, p, P)] = j | (m << kExclShift);
-                            } else if (cls == 2) {
-                                const int pos = nlr + __popc(bl & lt);
-                                if (pos < d.cap_lr) d.nbr_lr[nb_idx(pos, p, P)] = j;
-                            }
-                            nsr += __popc(bs);
-                            nlr += __popc(bl);
+            // the neighbour cells' candidate ranges laid end to end, in the reference's
+            // cell order (lane s < 27 holds cell s of the 3 x 3 x 3 block)
+            const int nseg = m1 * m2 * m3;
+            __syncwarp();  // the previous particle's reads of pre/beg are done
+            int cnt_l = 0, start_l = 0;
+            if (lane < nseg) {
+                const int a = lane / (m2 * m3), b = (lane / m3) % m2, e = lane % m3;
+                const int cc = (n1[a] - 1) * R->mc[1] * R->mc[2] + (n2[b] - 1) * R->mc[2] + (n3[e] - 1);
+                start_l = R->p0 + d.cell_start[R->c0 + cc];
+                cnt_l = d.cell_count[R->c0 + cc];
+            }
+            int incl = cnt_l;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(kFull, incl, 31);
+            int *pre = s_pre[threadIdx.x >> 5], *beg = s_beg[threadIdx.x >> 5];
+            if (lane < nseg) {
+                pre[lane] = incl - cnt_l;
+                beg[lane] = start_l;
+            }
+            if (lane == 0) pre[nseg] = total;
+            __syncwarp();
+            int nsr = 0, nlr = 0, seg = 0;
+            for (int t0 = 0; t0 < total; t0 += 32) {
+                const int t = t0 + lane;
+                int cls = 0, j = -1;  // 0 none, 1 SR, 2 LR
+                if (t < total) {
+                    while (t >= pre[seg + 1]) ++seg;
+                    const int slot = beg[seg] + (t - pre[seg]);
+                    j = d.cell_list[slot];
+                    if (j != p) {
+                        const int4 qj = d.qs[slot];
+                        const bool ch = chp && is_charged((qj.w >> 8) & 0xff);
+                        float r2f;
+                        {
+                            const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
+                            const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
+                            const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
+                            r2f = dx * dx + dy * dy + dz * dz;
                         }
+                        if (D) {
+                            const double r2 = exact_r2(d, R, p, j);
+                            cls = r2 <= R->r2sr ? 1 : ((ch && r2 <= R->r2lr) ? 2 : 0);
+                        } else {
+                            const float r2 = r2f;
+                            if (r2 < sr_lo) cls = 1;
+                            else if (r2 > sr_hi && (!ch || r2 > lr_hi)) cls = 0;
+                            else if (r2 > sr_hi && r2 < lr_lo) cls = 2;
+                            else {
+                                const double e2 = exact_r2(d, R, p, j);
+                                cls = e2 <= R->r2sr ? 1 : ((ch && e2 <= R->r2lr) ? 2 : 0);
+                            }
+                        }
+                        // pruned list: a pair with an uncharged bead can only exert LJ, which
+                        // vanishes beyond D_LJ; the skin keeps it exact until the next rebuild
+                        if (cls == 1 && !d.full_lists && !ch &&
+                            r2f > R->ljkeep2[jn12(qp.w & 0xff, qj.w & 0xff)])
+                            cls = 0;
                     }
+                }
+                const unsigned bs = __ballot_sync(kFull, cls == 1), bl = __ballot_sync(kFull, cls == 2);
+                if (cls == 1) {
+                    int m = 0;  // how often the reference subtracts this pair's LJ again
+                    for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
+                    const int pos = nsr + __popc(bs & lt);
+                    if (pos < d.cap_sr) d.nbr_sr[nb_idx(pos, p, P)] = j | (m << kExclShift);
+                } else if (cls == 2) {
+                    const int pos = nlr + __popc(bl & lt);
+                    if (pos < d.cap_lr) d.nbr_lr[nb_idx(pos, p, P)] = j;
+                }
+                nsr += __popc(bs);
+                nlr += __popc(bl);
+            }
             if (lane == 0) {
                 if (nsr > d.cap_sr || nlr > d.cap_lr) atomicOr(&d.rs[r].err, kErrCapacity);
                 d.n_sr[p] = min(nsr, d.cap_sr);
                 d.n_lr[p] = min(nlr, d.cap_lr);
             }
         }
-    }
-}
-
-// hydrogen-bond candidate status and HB_EXCESS (E:1698-1736): a candidate is live
-// (0) when its central pair is in the SR list, i.e. within the SR radius.
-__global__ void k_hb_rebuild(Dev d)
-{
-    __shared__ int s_warp[32];
-    __shared__ int s_carry;
-    for (int r = blockIdx.x; r < d.R; r += gridDim.x) {
-    RepState *S = d.rs + r;
-    if (!S->rebuild) continue;
-    const RepParams *R = d.rp + r;
-    for (int a = R->hba0 + threadIdx.x; a < R->hba1; a += blockDim.x)
-        d.hb_excess[a] = d.hba_n[a] - d.hba_val[a];
-    __syncthreads();
-    for (int k = R->hb0 + threadIdx.x; k < R->hb1; k += blockDim.x) {
-        const int a = d.hb_idx[6 * k + 1], b = d.hb_idx[6 * k + 4];
-        const int st = (a != b && exact_r2(d, R, a, b) <= R->r2sr) ? 0 : -1;
-        d.hb_status[k] = st;
-        if (st != 0)
-            for (int u = d.hb_aoff[k]; u < d.hb_aoff[k + 1]; ++u) atomicSub(d.hb_excess + d.hb_aidx[u], 1);
-    }
-    __syncthreads();
-    // ordered compaction of the live candidates
-    if (threadIdx.x == 0) s_carry = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int nh = R->hb1 - R->hb0;
-    for (int base = 0; base < nh; base += blockDim.x) {
-        const int k = R->hb0 + base + threadIdx.x;
-        const bool live = (base + threadIdx.x < nh) && d.hb_status[k] == 0;
-        const unsigned m = __ballot_sync(kFull, live);
-        if (lane == 0) s_warp[w] = __popc(m);
-        __syncthreads();
-        int off = s_carry;
-        for (int t = 0; t < w; ++t) off += s_warp[t];
-        if (live) d.hb_active[R->hb0 + off + __popc(m & ((1u << lane) - 1u))] = k;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int tot = 0;
-            for (int t = 0; t < (int)(blockDim.x >> 5); ++t) tot += s_warp[t];
-            s_carry += tot;
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        S->n_active = s_carry;
-        S->rebuild = 0;
-        S->rebuilds += 1;
-    }
-    __syncthreads();
     }
 }
 
@@ -1445,6 +1432,11 @@ void launch_topology(const Dev &d, cudaStream_t s, int mask, bool en, bool make_
 int configure_kernels(const Dev &d)
 {
     cudaError_t e = cudaSuccess;
+    if (d.cell_smem > 48 * 1024) {
+        const int b = d.cell_smem;
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cells<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cells<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    }
     if (d.hb_smem > 48 * 1024) {
         const int b = d.hb_smem;
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hbond<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
@@ -1472,25 +1464,19 @@ void launch_integrate(const Dev &d, cudaStream_t s)
     }
 }
 
-void launch_control(const Dev &d, cudaStream_t s) { k_control<<<d.R, 128, 0, s>>>(d); }
-
 void launch_rebuild(const Dev &d, cudaStream_t s)
 {
-    k_cell_assign<<<d.nblk, kBlock, 0, s>>>(d);
-    k_cell_scan<<<d.R, 256, 0, s>>>(d);
-    k_cell_fill<<<d.nblk, kBlock, 0, s>>>(d);
-    if (d.fp64) k_cell_order<true><<<d.sm_count * 4, 128, 0, s>>>(d);
-    else k_cell_order<false><<<d.sm_count * 4, 128, 0, s>>>(d);
+    if (d.fp64) k_cells<true><<<d.R, kCellThreads, d.cell_smem, s>>>(d);
+    else k_cells<false><<<d.R, kCellThreads, d.cell_smem, s>>>(d);
     if (d.fp64) k_pair_search<true><<<d.search_warps / 4, 128, 0, s>>>(d);
     else k_pair_search<false><<<d.search_warps / 4, 128, 0, s>>>(d);
-    k_hb_rebuild<<<d.R, 256, 0, s>>>(d);
 }
 
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s) { k_force_rebuild<<<d.R, 128, 0, s>>>(d); }
 
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out) { k_rg<<<1, 256, 0, s>>>(d, replica, out); }
 
-// pair SR, pair LR, bonded+stacking, H-bonds (+Gaussians), shift, integrate (+skin check), 6 rebuild kernels
-int kernel_launches_per_step() { return 12; }
+// pair SR, pair LR, bonded+stacking, H-bonds (+Gaussians), shift, integrate (+skin check), cells, pair search
+int kernel_launches_per_step() { return 8; }
 
 }  // namespace tis

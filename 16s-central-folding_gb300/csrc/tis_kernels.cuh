@@ -25,6 +25,8 @@ struct Dev {
     int full_lists;             // 1: SR list is the reference's full set; 0: pruned to possible forces
     int search_warps;           // warps of the pair-search grid
     int sm_count;               // multiprocessors (grid size of the rebuild kernels)
+    int nc_max;                 // most cells of one replica
+    int cell_smem;              // dynamic shared bytes of the cell kernel (0: its counters stay in global memory)
     // neighbour lists, column-major: nbr[k * P + p]
     int *nbr_sr, *n_sr, *nbr_lr, *n_lr;
     int cap_sr, cap_lr;
@@ -67,7 +69,6 @@ void launch_topology(const Dev &d, cudaStream_t s, int mask, bool energies, bool
 void launch_noise(const Dev &d, cudaStream_t s);  // the step's Gaussians only
 int configure_kernels(const Dev &d);              // kernel attributes (shared-memory limits); cudaError_t
 void launch_integrate(const Dev &d, cudaStream_t s);  // recentring shift, then the particles
-void launch_control(const Dev &d, cudaStream_t s);
 void launch_rebuild(const Dev &d, cudaStream_t s);  // gated on RepState::rebuild
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s);
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out);
