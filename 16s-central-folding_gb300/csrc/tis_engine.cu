@@ -176,20 +176,55 @@ int grow_lists(Group *h, int cap_sr, int cap_lr)
     return TIS_OK;
 }
 
+int uncount_rebuilds(Group *h, int n)
+{
+    std::vector<tis::RepState> rs(h->R);
+    TIS_CUDA(cudaMemcpyAsync(rs.data(), h->dev.rs, sizeof(tis::RepState) * h->R, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    for (auto &s : rs) s.rebuilds -= n;
+    TIS_CUDA(cudaMemcpyAsync(h->dev.rs, rs.data(), sizeof(tis::RepState) * h->R, cudaMemcpyHostToDevice, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return TIS_OK;
+}
+
+// largest SR and LR neighbour counts of the lists just built
+int list_peaks(Group *h, int *max_sr, int *max_lr)
+{
+    std::vector<int> a(h->P), b(h->P);
+    TIS_CUDA(cudaMemcpyAsync(a.data(), h->dev.n_sr, sizeof(int) * h->P, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaMemcpyAsync(b.data(), h->dev.n_lr, sizeof(int) * h->P, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    *max_sr = *std::max_element(a.begin(), a.end());
+    *max_lr = *std::max_element(b.begin(), b.end());
+    return TIS_OK;
+}
+
+// populate_lists for the group.  The lists grow until they hold twice the largest
+// neighbour count found, so that later rebuilds (ions gathering at the RNA, the
+// chain compacting) have room; a step that still overflows reports TIS_ERR_CAPACITY.
 int populate(Group *h)
 {
-    for (int attempt = 0; attempt < 6; ++attempt) {
+    for (int attempt = 0; attempt < 8; ++attempt) {
         int rc = clear_flags(h);
         if (rc) return rc;
         tis::launch_force_all_rebuild(h->dev, h->stream);
         tis::launch_rebuild(h->dev, h->stream);
         TIS_CUDA(cudaGetLastError());
         rc = check_flags(h);
-        if (rc != TIS_ERR_CAPACITY) {
-            if (rc == TIS_OK) h->lists_built = true;
-            return rc;
+        if (rc != TIS_OK && rc != TIS_ERR_CAPACITY) return rc;
+        int msr = 0, mlr = 0;
+        const int rp = list_peaks(h, &msr, &mlr);
+        if (rp) return rp;
+        const int want_sr = std::max(h->dev.cap_sr, round_up(2 * msr, 32));
+        const int want_lr = std::max(h->dev.cap_lr, round_up(2 * mlr, 32));
+        if (rc == TIS_OK && want_sr == h->dev.cap_sr && want_lr == h->dev.cap_lr) {
+            h->lists_built = true;
+            // the builds discarded for capacity do not count as list rebuilds
+            return attempt ? uncount_rebuilds(h, attempt) : TIS_OK;
         }
-        rc = grow_lists(h, round_up(h->dev.cap_sr * 3 / 2, 32), round_up(h->dev.cap_lr * 3 / 2, 32));
+        // an overflowing list reports its capacity as its count: grow by half at least
+        rc = grow_lists(h, rc ? std::max(want_sr, round_up(h->dev.cap_sr * 3 / 2, 32)) : want_sr,
+                        rc ? std::max(want_lr, round_up(h->dev.cap_lr * 3 / 2, 32)) : want_lr);
         if (rc) return rc;
     }
     return fail(TIS_ERR_CAPACITY, "neighbour lists keep overflowing");
@@ -634,27 +669,34 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         (rc = dalloc(O, &d.hb_status, nhb)) || (rc = dalloc(O, &d.hb_excess, nhba)) ||
         (rc = dalloc(O, &d.hb_active, nhb)) || (rc = dalloc(O, &d.ca_exc, ca_list.size())) ||
         (rc = dalloc(O, &d.hb_K, (size_t)kscr)) || (rc = dalloc(O, &d.hb_A, ca_list.size())) ||
-        (rc = dalloc(O, &d.hb_energy, nhb)) || (rc = dalloc(O, &d.hb_code, nhb)))
+        (rc = dalloc(O, &d.hb_energy, nhb)) || (rc = dalloc(O, &d.hb_code, nhb)) ||
+        (rc = dalloc(O, &d.hb_term, 6 * nhb)) || (rc = dalloc(O, &d.hb_br, 3 * nhb)))
         return bail(rc);
     {  // the Monte Carlo's views of the candidates: per over-valence atom its candidates, per candidate its such atoms
         std::vector<int> ca_pos(nhba, -1), ca_coff{0}, ca_cidx, hb_coff{0}, hb_cpos;
-        int hb_nmax = 0, ca_nmax = 0, k_nmax = 0;
+        int hb_nmax = 0, ca_nmax = 0, k_nmax = 0, cidx_max = 0, cpos_max = 0;
         for (int r = 0; r < h->R; ++r) {
             const tis::RepParams &Q = rp[r];
+            const size_t c_first = ca_cidx.size();
             for (int i = Q.ca0; i < Q.ca1; ++i) {
                 const int a = ca_list[i];
                 ca_pos[a] = i - Q.ca0;
                 for (int t = hba_coff[a]; t < hba_coff[a + 1]; ++t) ca_cidx.push_back(hba_cidx[t] - Q.hb0);
                 ca_coff.push_back((int)ca_cidx.size());
             }
+            cidx_max = std::max(cidx_max, (int)(ca_cidx.size() - c_first));
             hb_nmax = std::max(hb_nmax, Q.hb1 - Q.hb0);
             ca_nmax = std::max(ca_nmax, Q.ca1 - Q.ca0);
             k_nmax = std::max(k_nmax, Q.maxk);
         }
-        for (size_t k = 0; k < nhb; ++k) {
-            for (int u = hb_aoff[k]; u < hb_aoff[k + 1]; ++u)
-                if (ca_pos[hb_aidx[u]] >= 0) hb_cpos.push_back(ca_pos[hb_aidx[u]]);
-            hb_coff.push_back((int)hb_cpos.size());
+        for (int r = 0; r < h->R; ++r) {
+            const size_t p_first = hb_cpos.size();
+            for (int k = rp[r].hb0; k < rp[r].hb1; ++k) {
+                for (int u = hb_aoff[k]; u < hb_aoff[k + 1]; ++u)
+                    if (ca_pos[hb_aidx[u]] >= 0) hb_cpos.push_back(ca_pos[hb_aidx[u]]);
+                hb_coff.push_back((int)hb_cpos.size());
+            }
+            cpos_max = std::max(cpos_max, (int)(hb_cpos.size() - p_first));
         }
         int *d1 = nullptr, *d2 = nullptr, *d3 = nullptr, *d4 = nullptr;
         if ((rc = dupload(O, &d1, ca_coff)) || (rc = dupload(O, &d2, ca_cidx)) || (rc = dupload(O, &d3, hb_coff)) ||
@@ -664,8 +706,9 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         d.hb_nmax = hb_nmax;
         d.ca_nmax = ca_nmax;
         d.k_nmax = k_nmax;
-        // energies (8 B), status and branch code (4 B each) per candidate; excess and A per atom; K
-        const size_t smem = 16 * (size_t)hb_nmax + 8 * (size_t)ca_nmax + 4 * (size_t)k_nmax + 16;
+        d.cidx_max = cidx_max;
+        d.cpos_max = cpos_max;
+        const size_t smem = tis::hb_layout(hb_nmax, ca_nmax, k_nmax, cidx_max, cpos_max).total;
         d.hb_smem = smem <= 160 * 1024 ? (int)smem : 0;
     }
     if (tis::configure_kernels(d) != 0) return bail(fail(TIS_ERR_CUDA, "cudaFuncSetAttribute failed"));

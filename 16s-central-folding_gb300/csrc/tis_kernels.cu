@@ -241,6 +241,44 @@ __device__ void six_force(const Pos<D> &P, Acc<D> &A, const int *k, const double
     dihedral_force<D>(P, A, k[1], k[4], k[3], k[5], R(0.15) * w, psi_shift<R>((R)nat[5], b2));
 }
 
+// Term s of the six-term restraint (0: the central distance, from rdev; 1-2: the
+// angles; 3-5: the dihedrals, with the imaging branch of each in br): its weighted
+// squared deviation, as six_q adds it.
+template <bool D>
+__device__ inline Real<D> six_term(const Pos<D> &P, const int *k, const double *nat, int s, Real<D> rdev, int &br)
+{
+    using R = Real<D>;
+    br = 0;
+    if (s == 0) return R(5) * rdev * rdev;
+    if (s <= 2) {
+        const R t = s == 1 ? angle_of<D>(P, k[0], k[1], k[4]) : angle_of<D>(P, k[3], k[4], k[1]);
+        const R n = (R)nat[s];
+        return R(1.5) * (t - n) * (t - n);
+    }
+    R p;
+    if (s == 3) p = dihedral_of<D>(P, k[0], k[1], k[4], k[3]);
+    else if (s == 4) p = dihedral_of<D>(P, k[4], k[1], k[0], k[2]);
+    else p = dihedral_of<D>(P, k[1], k[4], k[3], k[5]);
+    br = psi_branch<R>(p, (R)nat[s]);
+    const R dd = p - psi_shift<R>((R)nat[s], br);
+    return R(0.15) * dd * dd;
+}
+
+// force of term s of the six-term restraint (six_force's six calls, one at a time)
+template <bool D>
+__device__ inline void six_force_term(const Pos<D> &P, Acc<D> &A, const int *k, const double *nat, int code,
+                                      Real<D> w, int s)
+{
+    using R = Real<D>;
+    if (s == 0) bond_force<D>(P, A, k[1], k[4], R(5) * w, (R)nat[0]);
+    else if (s == 1) angle_force<D>(P, A, k[0], k[1], k[4], R(1.5) * w, (R)nat[1], true);
+    else if (s == 2) angle_force<D>(P, A, k[3], k[4], k[1], R(1.5) * w, (R)nat[2], true);
+    else if (s == 3) dihedral_force<D>(P, A, k[0], k[1], k[4], k[3], R(0.15) * w, psi_shift<R>((R)nat[3], code % 3 - 1));
+    else if (s == 4)
+        dihedral_force<D>(P, A, k[4], k[1], k[0], k[2], R(0.15) * w, psi_shift<R>((R)nat[4], (code / 3) % 3 - 1));
+    else dihedral_force<D>(P, A, k[1], k[4], k[3], k[5], R(0.15) * w, psi_shift<R>((R)nat[5], code / 9 - 1));
+}
+
 template <bool D>
 __device__ inline Real<D> distance(const Pos<D> &P, int a, int b)
 {
@@ -699,16 +737,25 @@ __global__ void __launch_bounds__(kTopoThreads) k_bonded_stack(Dev d, int mask, 
 // -1: out of range) and every live bond is back to 0 when the kernel ends, so
 // the shared copy is never written back.
 struct HbWork {
-    double *en;  // energy of each live bond this step
-    int *st;     // status: 0 formed, 1 broken this step, -1 out of range
-    int *code;   // imaging branch of its dihedrals
-    int *exc;    // excess valence of each over-valence atom
-    int *al;     // over-valence atoms with positive excess (the reference's A list)
-    int *kl;     // candidate bonds of the chosen atom (the reference's K list)
+    double *en;    // energy of each live bond this step
+    double *term;  // its six restraint terms (six per bond)
+    int *st;       // status: 0 formed, 1 broken this step, -1 out of range
+    int *code;     // imaging branch of its dihedrals
+    int *br;       // the branches of its three dihedrals (three per bond)
+    int *exc;      // excess valence of each over-valence atom
+    int *al;       // over-valence atoms with positive excess (the reference's A list)
+    int *kl;       // candidate bonds of the chosen atom (the reference's K list)
+    const int *ca_off, *ca_idx;  // candidates of each over-valence atom: ca_idx[ca_off[i] ..]
+    const int *hb_off, *hb_pos;  // over-valence atoms of each bond: hb_pos[hb_off[k] ..]
 };
 
+constexpr int kHbThreads = 512;
+
+// One block per replica.  The restraint energies and forces of the live bonds run
+// as (chunk of 32 bonds, term) warp tasks, so that the lanes of a warp evaluate
+// the same term; the Monte Carlo runs on one warp; then the step's Gaussians.
 template <bool D, bool EN>
-__global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int make_noise)
+__global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make_noise)
 {
     using Rl = Real<D>;
     extern __shared__ __align__(16) unsigned char s_dyn[];
@@ -726,48 +773,81 @@ __global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int ma
     if (threadIdx.x == 0) s_ctr = S->ctr;
     double e2hb = 0, e3hb = 0;
     const int hb0 = R->hb0, nhb = R->hb1 - R->hb0, ca0 = R->ca0, nca = R->ca1 - R->ca0;
+    const int tid = threadIdx.x, bd = blockDim.x, warp = tid >> 5, nwarp = bd >> 5, lane = tid & 31;
 
     // ---- hydrogen_bonds_interactions (E:2145-2350) ----
     if (do_hb) {
         HbWork w;
+        const int c_base = d.ca_coff[ca0], n_cidx = d.ca_coff[R->ca1] - c_base;
+        const int h_base = d.hb_coff[hb0], n_cpos = d.hb_coff[R->hb1] - h_base;
         if (d.hb_smem) {
-            w.en = (double *)s_dyn;
-            w.st = (int *)(w.en + d.hb_nmax);
-            w.code = w.st + d.hb_nmax;
-            w.exc = w.code + d.hb_nmax;
-            w.al = w.exc + d.ca_nmax;
-            w.kl = w.al + d.ca_nmax;
-            for (int i = threadIdx.x; i < nhb; i += blockDim.x) w.st[i] = d.hb_status[hb0 + i];
+            const HbLayout L = hb_layout(d.hb_nmax, d.ca_nmax, d.k_nmax, d.cidx_max, d.cpos_max);
+            w.en = (double *)(s_dyn + L.en);
+            w.term = (double *)(s_dyn + L.term);
+            w.st = (int *)(s_dyn + L.st);
+            w.code = (int *)(s_dyn + L.code);
+            w.br = (int *)(s_dyn + L.br);
+            w.exc = (int *)(s_dyn + L.exc);
+            w.al = (int *)(s_dyn + L.al);
+            w.kl = (int *)(s_dyn + L.kl);
+            int *cao = (int *)(s_dyn + L.ca_off), *cai = (int *)(s_dyn + L.ca_idx);
+            int *hbo = (int *)(s_dyn + L.hb_off), *hbp = (int *)(s_dyn + L.hb_pos);
+            for (int i = tid; i < nhb; i += bd) w.st[i] = d.hb_status[hb0 + i];
+            for (int i = tid; i <= nca; i += bd) cao[i] = d.ca_coff[ca0 + i] - c_base;
+            for (int i = tid; i < n_cidx; i += bd) cai[i] = d.ca_cidx[c_base + i];
+            for (int i = tid; i <= nhb; i += bd) hbo[i] = d.hb_coff[hb0 + i] - h_base;
+            for (int i = tid; i < n_cpos; i += bd) hbp[i] = d.hb_cpos[h_base + i];
+            w.ca_off = cao; w.ca_idx = cai; w.hb_off = hbo; w.hb_pos = hbp;
         } else {
             w.en = d.hb_energy + hb0;
+            w.term = d.hb_term + 6 * (size_t)hb0;
             w.st = d.hb_status + hb0;
             w.code = d.hb_code + hb0;
+            w.br = d.hb_br + 3 * (size_t)hb0;
             w.exc = d.ca_exc + ca0;
             w.al = d.hb_A + ca0;
             w.kl = d.hb_K + R->kscr0;
+            w.ca_off = d.ca_coff + ca0; w.ca_idx = d.ca_cidx;
+            w.hb_off = d.hb_coff + hb0; w.hb_pos = d.hb_cpos;
         }
-        for (int i = threadIdx.x; i < nca; i += blockDim.x) w.exc[i] = d.hb_excess[d.ca_list[ca0 + i]];
+        for (int i = tid; i < nca; i += bd) w.exc[i] = d.hb_excess[d.ca_list[ca0 + i]];
         __syncthreads();
         const int nact = S->n_active;
-        for (int t = threadIdx.x; t < nact; t += blockDim.x) {
-            const int k = d.hb_active[hb0 + t];
-            const int *id = d.hb_idx + 6 * k;
-            const double *nat = d.hb_nat + 6 * k;
-            const Rl rr = distance<D>(P, id[1], id[4]);
-            if (fabs((double)(rr - (Rl)nat[0])) > 2.0) {
-                w.st[k - hb0] = 1;
-                for (int u = d.hb_coff[k]; u < d.hb_coff[k + 1]; ++u) atomicSub(w.exc + d.hb_cpos[u], 1);
-                w.en[k - hb0] = 0.0;
-                continue;
+        // a live bond whose central distance strays more than 2 A from native breaks (E:2165-2175)
+        for (int t = tid; t < nact; t += bd) {
+            const int k = d.hb_active[hb0 + t], kl = k - hb0;
+            const Rl rdev = distance<D>(P, d.hb_idx[6 * k + 1], d.hb_idx[6 * k + 4]) - (Rl)d.hb_nat[6 * k];
+            if (fabs((double)rdev) > 2.0) {
+                w.st[kl] = 1;
+                for (int u = w.hb_off[kl]; u < w.hb_off[kl + 1]; ++u) atomicSub(w.exc + w.hb_pos[u], 1);
+                w.en[kl] = 0.0;
             }
-            int code;
-            const Rl q = six_q<D>(P, id, nat, rr - (Rl)nat[0], Rl(0), code);
-            w.en[k - hb0] = (double)((Rl)d.hb_E[k] * exp_(-q));
-            w.code[k - hb0] = code;
+            int br;
+            w.term[6 * kl] = (double)six_term<D>(P, d.hb_idx + 6 * k, d.hb_nat + 6 * k, 0, rdev, br);
+        }
+        // the angle and dihedral terms: warp task (chunk of 32 live bonds, term 1..5)
+        const int nchunk = (nact + 31) >> 5;
+        for (int task = warp; task < 5 * nchunk; task += nwarp) {
+            const int s = 1 + task % 5, t = (task / 5) * 32 + lane;
+            if (t < nact) {
+                const int k = d.hb_active[hb0 + t], kl = k - hb0;
+                int br;
+                const Rl v = six_term<D>(P, d.hb_idx + 6 * k, d.hb_nat + 6 * k, s, Rl(0), br);
+                w.term[6 * kl + s] = (double)v;
+                if (s >= 3) w.br[3 * kl + s - 3] = br;
+            }
         }
         __syncthreads();
-        if (threadIdx.x < 32) {  // valence-limited Monte Carlo (E:2239-2315), one warp
-            const int lane = threadIdx.x;
+        for (int t = tid; t < nact; t += bd) {
+            const int k = d.hb_active[hb0 + t], kl = k - hb0;
+            if (w.st[kl] == 1) continue;
+            Rl q = Rl(0);
+            for (int s = 0; s < 6; ++s) q += (Rl)w.term[6 * kl + s];
+            w.en[kl] = (double)((Rl)d.hb_E[k] * exp_(-q));
+            w.code[kl] = (w.br[3 * kl] + 1) + 3 * (w.br[3 * kl + 1] + 1) + 9 * (w.br[3 * kl + 2] + 1);
+        }
+        __syncthreads();
+        if (tid < 32) {  // valence-limited Monte Carlo (E:2239-2315), one warp
             const unsigned lt = (1u << lane) - 1u;
             unsigned long long ctr = s_ctr;
             const double T = R->T;
@@ -789,11 +869,11 @@ __global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int ma
                 __syncwarp();
                 const int atom = w.al[pick_index(s_v[0], nA) - 1];
                 // K: the atom's candidates still formed, in candidate order
-                const int c0 = d.ca_coff[ca0 + atom], nc = d.ca_coff[ca0 + atom + 1] - c0;
+                const int c0 = w.ca_off[atom], nc = w.ca_off[atom + 1] - c0;
                 int nK = 0;
                 for (int base = 0; base < nc; base += 32) {
                     const int t = base + lane;
-                    const int k = t < nc ? d.ca_cidx[c0 + t] : 0;
+                    const int k = t < nc ? w.ca_idx[c0 + t] : 0;
                     const bool ok = t < nc && w.st[k] == 0;
                     const unsigned m = __ballot_sync(kFull, ok);
                     if (ok) w.kl[nK + __popc(m & lt)] = k;
@@ -833,7 +913,7 @@ __global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int ma
                 if (lane == 0) {
                     const int k = w.kl[kc];
                     w.st[k] = 1;
-                    for (int u = d.hb_coff[hb0 + k]; u < d.hb_coff[hb0 + k + 1]; ++u) w.exc[d.hb_cpos[u]] -= 1;
+                    for (int u = w.hb_off[k]; u < w.hb_off[k + 1]; ++u) w.exc[w.hb_pos[u]] -= 1;
                 }
                 ctr += 2 * nK;
                 __syncwarp();
@@ -841,16 +921,25 @@ __global__ void __launch_bounds__(kTopoThreads) k_hbond(Dev d, int do_hb, int ma
             if (lane == 0) s_ctr = ctr;
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < nact; t += blockDim.x) {
-            const int k = d.hb_active[hb0 + t];
-            if (w.st[k - hb0] == 1) {
-                w.st[k - hb0] = 0;
-                continue;
+        // forces of the bonds still formed: warp task (chunk of 32 live bonds, term 0..5)
+        for (int task = warp; task < 6 * nchunk; task += nwarp) {
+            const int s = task % 6, t = (task / 6) * 32 + lane;
+            if (t < nact) {
+                const int k = d.hb_active[hb0 + t], kl = k - hb0;
+                if (w.st[kl] != 1) {
+                    const Rl wk = -(Rl)w.en[kl];
+                    if (s == 0) {
+                        if (d.hb_dode[k]) e3hb -= (double)wk;
+                        else e2hb -= (double)wk;
+                    }
+                    six_force_term<D>(P, A, d.hb_idx + 6 * k, d.hb_nat + 6 * k, w.code[kl], wk, s);
+                }
             }
-            const Rl wk = -(Rl)w.en[k - hb0];
-            if (d.hb_dode[k]) e3hb -= (double)wk;
-            else e2hb -= (double)wk;
-            six_force<D>(P, A, d.hb_idx + 6 * k, d.hb_nat + 6 * k, w.code[k - hb0], wk);
+        }
+        __syncthreads();
+        for (int t = tid; t < nact; t += bd) {  // every live bond is formed again for the next step
+            const int kl = d.hb_active[hb0 + t] - hb0;
+            if (w.st[kl] == 1) w.st[kl] = 0;
         }
     }
     __syncthreads();
@@ -1024,6 +1113,21 @@ __device__ inline int cell_axis(double v, double side, double l)
     return (int)ceil(__ddiv_rn(t, l));
 }
 
+// cell_axis decided in FP32 from the fixed-point coordinate q = floor(v 2^32 / side)
+// mod 2^32, for v in [0, side] (no wrap): c = q m / 2^32 approximates v / l (l = side
+// / m) within 2e-7 m; when c lies farther than 4e-7 m + 1e-6 from an integer, ceil(c)
+// is the FP64 result, else the FP64 form decides.
+__device__ inline int cell_axis_q(double v, unsigned q, double side, double l, int m)
+{
+    const long long b = __double_as_longlong(v);
+    if (b >= 0 && b <= __double_as_longlong(side)) {
+        const float c = (float)q * ((float)m * 2.3283064365386963e-10f);
+        const float fr = c - floorf(c), band = 4.0e-7f * (float)m + 1.0e-6f;
+        if (fr > band && fr < 1.0f - band) return (int)c + 1;
+    }
+    return cell_axis(v, side, l);
+}
+
 // Work items of the replicas that rebuild this step, laid end to end (`per`: 0 =
 // padded particles, 1 = cells).  Warp-collective: maps item i to its replica r and
 // the offset within it; returns false past the end.
@@ -1086,10 +1190,11 @@ __global__ void __launch_bounds__(kCellThreads) k_cells(Dev d)
     for (int i = tid; i < R->npad; i += bd) {
         const int p = R->p0 + i;
         int c = -1;
-        if ((d.q[p].w >> 16) & 1) {
-            const int i1 = cell_axis(d.x[p], R->box[0], R->lcell[0]);
-            const int i2 = cell_axis(d.y[p], R->box[1], R->lcell[1]);
-            const int i3 = cell_axis(d.z[p], R->box[2], R->lcell[2]);
+        const int4 qp = d.q[p];
+        if ((qp.w >> 16) & 1) {
+            const int i1 = cell_axis_q(d.x[p], (unsigned)qp.x, R->box[0], R->lcell[0], R->mc[0]);
+            const int i2 = cell_axis_q(d.y[p], (unsigned)qp.y, R->box[1], R->lcell[1], R->mc[1]);
+            const int i3 = cell_axis_q(d.z[p], (unsigned)qp.z, R->box[2], R->lcell[2], R->mc[2]);
             if (i1 < 1 || i1 > R->mc[0] || i2 < 1 || i2 > R->mc[1] || i3 < 1 || i3 > R->mc[2]) {
                 atomicOr(&S->err, kErrRange);
             } else {
@@ -1286,31 +1391,41 @@ __global__ void __launch_bounds__(128) k_pair_search(Dev d)
             if (lane == 0) pre[nseg] = total;
             __syncwarp();
             int nsr = 0, nlr = 0, seg = 0;
-            for (int t0 = 0; t0 < total; t0 += 32) {
-                const int t = t0 + lane;
-                int cls = 0, j = -1;  // 0 none, 1 SR, 2 LR
-                if (t < total) {
-                    while (t >= pre[seg + 1]) ++seg;
-                    const int slot = beg[seg] + (t - pre[seg]);
-                    j = d.cell_list[slot];
-                    if (j != p) {
-                        const int4 qj = d.qs[slot];
+            constexpr int kU = 4;  // candidate chunks of 32 whose loads are issued together
+            for (int t0 = 0; t0 < total; t0 += 32 * kU) {
+                int jv[kU];
+                int4 qv[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int t = t0 + 32 * u + lane;
+                    jv[u] = -1;
+                    qv[u] = make_int4(0, 0, 0, 0);
+                    if (t < total) {
+                        while (t >= pre[seg + 1]) ++seg;
+                        const int slot = beg[seg] + (t - pre[seg]);
+                        jv[u] = d.cell_list[slot];
+                        qv[u] = d.qs[slot];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    if (t0 + 32 * u >= total) break;
+                    const int j = jv[u];
+                    const int4 qj = qv[u];
+                    int cls = 0;  // 0 none, 1 SR, 2 LR
+                    if (j >= 0 && j != p) {
                         const bool ch = chp && is_charged((qj.w >> 8) & 0xff);
-                        float r2f;
-                        {
-                            const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
-                            const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
-                            const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
-                            r2f = dx * dx + dy * dy + dz * dz;
-                        }
+                        const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
+                        const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
+                        const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
+                        const float r2f = dx * dx + dy * dy + dz * dz;
                         if (D) {
                             const double r2 = exact_r2(d, R, p, j);
                             cls = r2 <= R->r2sr ? 1 : ((ch && r2 <= R->r2lr) ? 2 : 0);
                         } else {
-                            const float r2 = r2f;
-                            if (r2 < sr_lo) cls = 1;
-                            else if (r2 > sr_hi && (!ch || r2 > lr_hi)) cls = 0;
-                            else if (r2 > sr_hi && r2 < lr_lo) cls = 2;
+                            if (r2f < sr_lo) cls = 1;
+                            else if (r2f > sr_hi && (!ch || r2f > lr_hi)) cls = 0;
+                            else if (r2f > sr_hi && r2f < lr_lo) cls = 2;
                             else {
                                 const double e2 = exact_r2(d, R, p, j);
                                 cls = e2 <= R->r2sr ? 1 : ((ch && e2 <= R->r2lr) ? 2 : 0);
@@ -1318,23 +1433,22 @@ __global__ void __launch_bounds__(128) k_pair_search(Dev d)
                         }
                         // pruned list: a pair with an uncharged bead can only exert LJ, which
                         // vanishes beyond D_LJ; the skin keeps it exact until the next rebuild
-                        if (cls == 1 && !d.full_lists && !ch &&
-                            r2f > R->ljkeep2[jn12(qp.w & 0xff, qj.w & 0xff)])
+                        if (cls == 1 && !d.full_lists && !ch && r2f > R->ljkeep2[jn12(qp.w & 0xff, qj.w & 0xff)])
                             cls = 0;
                     }
+                    const unsigned bs = __ballot_sync(kFull, cls == 1), bl = __ballot_sync(kFull, cls == 2);
+                    if (cls == 1) {
+                        int m = 0;  // how often the reference subtracts this pair's LJ again
+                        for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
+                        const int pos = nsr + __popc(bs & lt);
+                        if (pos < d.cap_sr) d.nbr_sr[nb_idx(pos, p, P)] = j | (m << kExclShift);
+                    } else if (cls == 2) {
+                        const int pos = nlr + __popc(bl & lt);
+                        if (pos < d.cap_lr) d.nbr_lr[nb_idx(pos, p, P)] = j;
+                    }
+                    nsr += __popc(bs);
+                    nlr += __popc(bl);
                 }
-                const unsigned bs = __ballot_sync(kFull, cls == 1), bl = __ballot_sync(kFull, cls == 2);
-                if (cls == 1) {
-                    int m = 0;  // how often the reference subtracts this pair's LJ again
-                    for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
-                    const int pos = nsr + __popc(bs & lt);
-                    if (pos < d.cap_sr) d.nbr_sr[nb_idx(pos, p, P)] = j | (m << kExclShift);
-                } else if (cls == 2) {
-                    const int pos = nlr + __popc(bl & lt);
-                    if (pos < d.cap_lr) d.nbr_lr[nb_idx(pos, p, P)] = j;
-                }
-                nsr += __popc(bs);
-                nlr += __popc(bl);
             }
             if (lane == 0) {
                 if (nsr > d.cap_sr || nlr > d.cap_lr) atomicOr(&d.rs[r].err, kErrCapacity);
@@ -1420,11 +1534,11 @@ void launch_topology(const Dev &d, cudaStream_t s, int mask, bool en, bool make_
     const size_t sm = hb ? (size_t)d.hb_smem : 0;
     if (hb || mn) {
         if (d.fp64) {
-            if (en) k_hbond<true, true><<<d.R, kTopoThreads, sm, s>>>(d, hb, mn);
-            else k_hbond<true, false><<<d.R, kTopoThreads, sm, s>>>(d, hb, mn);
+            if (en) k_hbond<true, true><<<d.R, kHbThreads, sm, s>>>(d, hb, mn);
+            else k_hbond<true, false><<<d.R, kHbThreads, sm, s>>>(d, hb, mn);
         } else {
-            if (en) k_hbond<false, true><<<d.R, kTopoThreads, sm, s>>>(d, hb, mn);
-            else k_hbond<false, false><<<d.R, kTopoThreads, sm, s>>>(d, hb, mn);
+            if (en) k_hbond<false, true><<<d.R, kHbThreads, sm, s>>>(d, hb, mn);
+            else k_hbond<false, false><<<d.R, kHbThreads, sm, s>>>(d, hb, mn);
         }
     }
 }

@@ -50,12 +50,40 @@ struct Dev {
     int *hb_status, *hb_excess, *hb_active, *hb_K, *hb_A, *ca_exc;
     double *hb_energy;
     int *hb_code;               // imaging branch of the three native dihedrals
+    double *hb_term;            // six restraint terms per candidate (global scratch)
+    int *hb_br;                 // three dihedral branches per candidate (global scratch)
     int hb_nmax, ca_nmax, k_nmax;   // largest per-replica candidate, over-valence atom and K counts
+    int cidx_max, cpos_max;         // largest per-replica ca_cidx and hb_cpos lengths
     int hb_smem;                // dynamic shared bytes of the H-bond kernel (0: its arrays stay in global scratch)
     double *eterm;              // R x kNE (per-term energies, compute_forces only)
     double *shift;              // R x 3, recentring shift of the current step (adjust_box)
     const int *cell_rep;        // replica of every cell
 };
+
+// Byte offsets of the H-bond kernel's shared-memory arrays (one replica's working
+// set; the kernel and the engine's size check both use this layout).
+struct HbLayout {
+    size_t en, term, st, code, br, exc, al, kl, ca_off, ca_idx, hb_off, hb_pos, total;
+};
+__host__ __device__ inline HbLayout hb_layout(int hb_nmax, int ca_nmax, int k_nmax, int cidx_max, int cpos_max)
+{
+    HbLayout L;
+    size_t o = 0;
+    L.en = o; o += 8 * (size_t)hb_nmax;              // double per candidate
+    L.term = o; o += 48 * (size_t)hb_nmax;           // six doubles per candidate
+    L.st = o; o += 4 * (size_t)hb_nmax;
+    L.code = o; o += 4 * (size_t)hb_nmax;
+    L.br = o; o += 12 * (size_t)hb_nmax;             // three ints per candidate
+    L.exc = o; o += 4 * (size_t)ca_nmax;
+    L.al = o; o += 4 * (size_t)ca_nmax;
+    L.kl = o; o += 4 * (size_t)k_nmax;
+    L.ca_off = o; o += 4 * ((size_t)ca_nmax + 1);
+    L.ca_idx = o; o += 4 * (size_t)cidx_max;
+    L.hb_off = o; o += 4 * ((size_t)hb_nmax + 1);
+    L.hb_pos = o; o += 4 * (size_t)cpos_max;
+    L.total = (o + 15) / 16 * 16;
+    return L;
+}
 
 // Launchers (stream-ordered; gated per replica on device flags where noted).
 void launch_quantize(const Dev &d, cudaStream_t s);

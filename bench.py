@@ -28,6 +28,10 @@ import threading
 import time
 from concurrent.futures import ThreadPoolExecutor
 
+# each replica group's graph runs on its own streams; enough hardware work queues
+# keep queued graphs of different groups from waiting on one another
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "16s-central-folding_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
