@@ -133,10 +133,14 @@ __host__ __device__ inline double u31_ratio(uint32_t v)
 // ceil(u n) clamped to [1, n] as the reference picks a list entry, for u = v / (2^31 - 1)
 // and 1 <= n < 2^20: v n / (2^31 - 1) is never an integer for v < 2^31 - 1 (the divisor
 // is prime) and lies at least 2^-31 from one, far beyond the FP64 rounding of u and u n.
+// The quotient floor(x / (2^31 - 1)) for x < 2^62 is (x + (x >> 31) + 1) >> 31: with
+// x = q (2^31 - 1) + r, x >> 31 is q when r >= q and q - 1 when r < q, and either way
+// the sum is q 2^31 plus a remainder below 2^31.
 __host__ __device__ inline int pick_index(uint32_t v, int n)
 {
     if (v >= 2147483647u) return n;
-    return (int)(((unsigned long long)v * (unsigned)n) / 2147483647ull) + 1;
+    const unsigned long long x = (unsigned long long)v * (unsigned)n;
+    return (int)((x + (x >> 31) + 1ull) >> 31) + 1;
 }
 
 #ifdef __CUDACC__

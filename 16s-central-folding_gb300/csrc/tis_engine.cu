@@ -579,7 +579,7 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
     {
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, prm.device);
-        d.search_warps = std::max(4, sms * 8 * 4);  // 8 blocks of 4 warps per SM
+        d.search_warps = std::max(4, sms * 4);  // one block of 4 warps per SM: rebuilds are rare
         d.sm_count = std::max(1, sms);
         int nc_max = 1;
         for (auto &Q : rp) nc_max = std::max(nc_max, Q.nc);

@@ -751,15 +751,35 @@ struct HbWork {
 
 constexpr int kHbThreads = 512;
 
+// rand() draws vbase .. vbase + 63 of a replica into v[], by 17 lanes of one warp
+// (one Philox block of four draws each; the same words rand_value returns)
+__device__ inline void fill_draws(uint32_t *v, unsigned long long seed, unsigned long long vbase, int lane)
+{
+    const unsigned long long b = (vbase >> 2) + (unsigned long long)lane;
+    if (lane < 17) {
+        uint32_t c[4] = {(uint32_t)b, (uint32_t)(b >> 32), 0u, 0u};
+        philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        for (int w = 0; w < 4; ++w) {
+            const long long idx = (long long)(4 * b + (unsigned long long)w) - (long long)vbase;
+            if (idx >= 0 && idx < 64) {
+                const uint32_t x = c[w] >> 1;
+                v[idx] = x ? x : 1u;
+            }
+        }
+    }
+    __syncwarp();
+}
+
 // One block per replica.  The restraint energies and forces of the live bonds run
 // as (chunk of 32 bonds, term) warp tasks, so that the lanes of a warp evaluate
-// the same term; the Monte Carlo runs on one warp; then the step's Gaussians.
+// the same term; the Monte Carlo runs on one warp; then the step's Gaussians,
+// drawn by the block while its warps finish the force tasks.
 template <bool D, bool EN>
 __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make_noise)
 {
     using Rl = Real<D>;
     extern __shared__ __align__(16) unsigned char s_dyn[];
-    __shared__ uint32_t s_v[32];  // the next 32 draws of the replica's rand() stream
+    __shared__ uint32_t s_v[64];  // draws vbase .. vbase + 63 of the replica's rand() stream
     __shared__ unsigned long long s_ctr;
     __shared__ double s_red[2 * 32];
     const int r = blockIdx.x;
@@ -774,10 +794,12 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
     double e2hb = 0, e3hb = 0;
     const int hb0 = R->hb0, nhb = R->hb1 - R->hb0, ca0 = R->ca0, nca = R->ca1 - R->ca0;
     const int tid = threadIdx.x, bd = blockDim.x, warp = tid >> 5, nwarp = bd >> 5, lane = tid & 31;
+    HbWork w;
+    const int nact = do_hb ? S->n_active : 0;
+    __syncthreads();
 
     // ---- hydrogen_bonds_interactions (E:2145-2350) ----
     if (do_hb) {
-        HbWork w;
         const int c_base = d.ca_coff[ca0], n_cidx = d.ca_coff[R->ca1] - c_base;
         const int h_base = d.hb_coff[hb0], n_cpos = d.hb_coff[R->hb1] - h_base;
         if (d.hb_smem) {
@@ -812,7 +834,6 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
         }
         for (int i = tid; i < nca; i += bd) w.exc[i] = d.hb_excess[d.ca_list[ca0 + i]];
         __syncthreads();
-        const int nact = S->n_active;
         // a live bond whose central distance strays more than 2 A from native breaks (E:2165-2175)
         for (int t = tid; t < nact; t += bd) {
             const int k = d.hb_active[hb0 + t], kl = k - hb0;
@@ -849,7 +870,8 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
         __syncthreads();
         if (tid < 32) {  // valence-limited Monte Carlo (E:2239-2315), one warp
             const unsigned lt = (1u << lane) - 1u;
-            unsigned long long ctr = s_ctr;
+            unsigned long long ctr = s_ctr, vbase = ctr;
+            fill_draws(s_v, R->seed, vbase, lane);
             const double T = R->T;
             const float inv_t = 1.0f / R->Tf;
             int guard = nact + 2;
@@ -864,10 +886,14 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
                     nA += __popc(m);
                 }
                 if (nA == 0) break;
-                // draws ctr, ctr+1, ...: the atom, the K shuffle, the acceptances
-                s_v[lane] = rand_value(R->seed, ctr + lane);
-                __syncwarp();
-                const int atom = w.al[pick_index(s_v[0], nA) - 1];
+                // draws ctr, ctr+1, ...: the atom, the K shuffle, the acceptances; u[i] is draw ctr + i
+                if (ctr - vbase > 32) {
+                    vbase = ctr;
+                    fill_draws(s_v, R->seed, vbase, lane);
+                }
+                const uint32_t *u = s_v + (ctr - vbase);
+                const int nu = 64 - (int)(ctr - vbase);  // draws held from u[0] on (at least 32)
+                const int atom = w.al[pick_index(u[0], nA) - 1];
                 // K: the atom's candidates still formed, in candidate order
                 const int c0 = w.ca_off[atom], nc = w.ca_off[atom + 1] - c0;
                 int nK = 0;
@@ -887,7 +913,7 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
                 }
                 if (lane == 0)
                     for (int i = 1; i <= nK; ++i) {
-                        const int jj = pick_index(i < 32 ? s_v[i] : rand_value(R->seed, ctr + i), nK);
+                        const int jj = pick_index(i < nu ? u[i] : rand_value(R->seed, ctr + i), nK);
                         const int tmp = w.kl[i - 1];
                         w.kl[i - 1] = w.kl[jj - 1];
                         w.kl[jj - 1] = tmp;
@@ -899,14 +925,14 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
                 if (nK * nK <= 32) {
                     const int a = lane / nK, b = lane - a * nK;
                     const bool acc = lane < nK * nK && a >= 1 &&
-                                     accept_move(s_v[nK + a], w.en[w.kl[a]], w.en[w.kl[b]], T, inv_t);
+                                     accept_move(u[nK + a], w.en[w.kl[a]], w.en[w.kl[b]], T, inv_t);
                     const unsigned dm = __ballot_sync(kFull, acc);
                     for (int a2 = 1; a2 < nK; ++a2)
                         if ((dm >> (a2 * nK + kc)) & 1u) kc = a2;
                 } else if (lane == 0) {
                     for (int i = 2; i <= nK; ++i) {
                         const int di = nK + i - 1;
-                        const uint32_t v = di < 32 ? s_v[di] : rand_value(R->seed, ctr + di);
+                        const uint32_t v = di < nu ? u[di] : rand_value(R->seed, ctr + di);
                         if (accept_move(v, w.en[w.kl[i - 1]], w.en[w.kl[kc]], T, inv_t)) kc = i - 1;
                     }
                 }
@@ -936,19 +962,18 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
                 }
             }
         }
-        __syncthreads();
-        for (int t = tid; t < nact; t += bd) {  // every live bond is formed again for the next step
-            const int kl = d.hb_active[hb0 + t] - hb0;
-            if (w.st[kl] == 1) w.st[kl] = 0;
-        }
     }
-    __syncthreads();
     // ---- full_forces: the step's Gaussians follow the Monte Carlo draws ----
     const unsigned long long c1 = s_ctr;
     if (make_noise) gen_noise<D>(d, r, c1);
 
     double v[2] = {e2hb, e3hb};
     block_sum<2>(v, s_red);
+    if (do_hb)
+        for (int t = tid; t < nact; t += bd) {  // every live bond is formed again for the next step
+            const int kl = d.hb_active[hb0 + t] - hb0;
+            if (w.st[kl] == 1) w.st[kl] = 0;
+        }
     if (threadIdx.x == 0) {
         S->ctr = make_noise ? c1 + kNoise : c1;
         if (do_hb) { S->e2hb = v[0]; S->e3hb = v[1]; }

@@ -95,7 +95,8 @@ void launch_pair_sr(const Dev &d, cudaStream_t s, bool energies, bool excl_in_li
 void launch_pair_lr(const Dev &d, cudaStream_t s, bool energies, bool force_all);
 void launch_topology(const Dev &d, cudaStream_t s, int mask, bool energies, bool make_noise, bool excl_in_list);
 void launch_noise(const Dev &d, cudaStream_t s);  // the step's Gaussians only
-int configure_kernels(const Dev &d);              // kernel attributes (shared-memory limits); cudaError_t
+int configure_kernels(const Dev &d);
+              // kernel attributes (shared-memory limits); cudaError_t
 void launch_integrate(const Dev &d, cudaStream_t s);  // recentring shift, then the particles
 void launch_rebuild(const Dev &d, cudaStream_t s);  // gated on RepState::rebuild
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s);
