@@ -25,7 +25,10 @@ constexpr float kFixLimit = 1.0e9f;  // |contribution| clamp (int64 range / 2^32
 constexpr int kExcl = 8;             // bonded (1-2, 1-3) partners stored per particle
 constexpr int kExclShift = 30;       // SR list entry: partner | (exclusion multiplicity << 30)
 constexpr int kIdxMask = (1 << kExclShift) - 1;
-constexpr int kLanes = 4;            // threads per particle in the pair kernels
+constexpr int kLanes = 4;            // neighbour-list slots per chunk (nb_idx)
+constexpr int kLanesSR = 1;          // threads per particle in the SR pair kernel (lists of a few pairs)
+constexpr int kLanesLR = 4;          // threads per particle in the LR pair kernel
+constexpr int kIntPer = 1;           // particles per thread in the integrator
 
 // neighbour slot k of particle p: chunks of four slots per particle, chunk-major,
 // so the four threads of a particle read 16 contiguous bytes and a warp 128

@@ -232,7 +232,7 @@ int populate(Group *h)
 
 // deterministic_forces_MPI (E:2524-2586): the four force kernels are independent
 // (fixed-point atomics into one sum, the LR sum kept apart), so they run as
-// concurrent branches joined before the noise
+// concurrent branches joined before the integrator
 void enqueue_forces(Group *h, bool make_noise)
 {
     cudaEventRecord(h->fork, h->stream);

@@ -337,10 +337,12 @@ __global__ void __launch_bounds__(kBlock) k_quantize(Dev d)
 // ---------------------------------------------------------------------------
 // pair forces over the full (both-direction) neighbour lists
 // ---------------------------------------------------------------------------
-template <bool D, bool LR, bool EN, bool EX>
-__global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
+// Particle block b (kBlock particles) with L threads per particle: slot k of a
+// particle's list goes to its thread k % L.
+template <bool D, bool LR, bool EN, bool EX, int L>
+__device__ void pair_block(const Dev &d, int b, int force_all)
 {
-    const int r = d.blk_rep[blockIdx.x];
+    const int r = d.blk_rep[b];
     const RepParams *R = d.rp + r;
     if (LR && !force_all && !d.rs[r].lr_now) return;
     __shared__ float s_dlj2[46], s_dm[46], s_flj[46], s_qclb[46];
@@ -353,9 +355,8 @@ __global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
         }
         __syncthreads();
     }
-    // four threads per particle: slot k of the list goes to thread k % 4
-    const int lane4 = threadIdx.x & (kLanes - 1);
-    const int p = blockIdx.x * kBlock + (threadIdx.x >> 2);
+    const int lane4 = threadIdx.x & (L - 1);
+    const int p = b * kBlock + threadIdx.x / L;
     const int P = d.P;
     const int4 qp = d.q[p];
     const int tp = qp.w & 0xff, kp = (qp.w >> 8) & 0xff, act = (qp.w >> 16) & 1;
@@ -368,7 +369,7 @@ __global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
         long long ax = 0, ay = 0, az = 0;
         const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
         const float rc2 = R->rc2f, lo = rc2 * (1.0f - kBand), hi = rc2 * (1.0f + kBand);
-        for (int k = lane4; k < cnt; k += kLanes) {
+        for (int k = lane4; k < cnt; k += L) {
             const int raw = __ldg(nbr + nb_idx(k, p, P));
             const int j = raw & kIdxMask;
             const float ljw = EX ? (float)(1 - (raw >> kExclShift)) : 1.0f;
@@ -410,7 +411,7 @@ __global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
                 az += to_fix(F * dz, err);
             }
         }
-        for (int o = 1; o < kLanes; o <<= 1) {
+        for (int o = 1; o < L; o <<= 1) {
             ax += __shfl_xor_sync(kFull, ax, o);
             ay += __shfl_xor_sync(kFull, ay, o);
             az += __shfl_xor_sync(kFull, az, o);
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
         }
     } else {
         double ax = 0, ay = 0, az = 0;
-        for (int k = lane4; k < cnt; k += kLanes) {
+        for (int k = lane4; k < cnt; k += L) {
             const int raw = __ldg(nbr + nb_idx(k, p, P));
             const int j = raw & kIdxMask;
             const double ljw = EX ? (double)(1 - (raw >> kExclShift)) : 1.0;
@@ -463,7 +464,7 @@ __global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
             ay += v[1] * F;
             az += v[2] * F;
         }
-        for (int o = 1; o < kLanes; o <<= 1) {
+        for (int o = 1; o < L; o <<= 1) {
             ax += __shfl_xor_sync(kFull, ax, o);
             ay += __shfl_xor_sync(kFull, ay, o);
             az += __shfl_xor_sync(kFull, az, o);
@@ -487,6 +488,12 @@ __global__ void __launch_bounds__(kBlock * kLanes) k_pair(Dev d, int force_all)
         atomicAdd(d.eterm + r * kNE + (LR ? 2 : 1), e_c);
     }
     if (err) atomicOr(&d.rs[r].err, err);
+}
+
+template <bool D, bool LR, bool EN, bool EX, int L>
+__global__ void __launch_bounds__(kBlock * L) k_pair(Dev d, int force_all)
+{
+    pair_block<D, LR, EN, EX, L>(d, blockIdx.x, force_all);
 }
 
 // ---------------------------------------------------------------------------
@@ -1019,8 +1026,9 @@ __global__ void k_shift(Dev d)
 // move_rigid_units (E:2660-2731) of one particle per thread: leap-frog, the
 // recentring shift, the periodic wrap of the ions; the replica's last block to
 // finish runs the skin check
+// kIntPer particles per thread, kBlock / kIntPer threads per block of kBlock particles
 template <bool D>
-__global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
+__global__ void __launch_bounds__(kBlock / kIntPer) k_integrate(Dev d)
 {
     const int r = d.blk_rep[blockIdx.x];
     const RepParams *R = d.rp + r;
@@ -1028,10 +1036,12 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
     if (threadIdx.x == 0) s_max = 0ull;
     __syncthreads();
     const double sh[3] = {d.shift[3 * r], d.shift[3 * r + 1], d.shift[3 * r + 2]};
-    const int p = blockIdx.x * kBlock + threadIdx.x;
-    const int4 qp = d.q[p];
-    double d2 = 0.0;
+    unsigned long long bits = 0ull;  // max |x - x_old|^2 of the thread's particles (non-negative doubles order as integers)
     int err = 0;
+#pragma unroll
+    for (int j = 0; j < kIntPer; ++j) {
+    const int p = blockIdx.x * kBlock + j * (kBlock / kIntPer) + threadIdx.x;
+    const int4 qp = d.q[p];
     if ((qp.w >> 16) & 1) {
         double xn[3], vn[3];
         leap_frog<D>(d, R, r, p, xn, vn);
@@ -1046,10 +1056,12 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
                 if (above(xn[c], R->box[c])) { xn[c] -= R->box[c]; xo[c] -= R->box[c]; }
             }
         }
+        double e2 = 0.0;
         for (int c = 0; c < 3; ++c) {
             const double e = xn[c] - xo[c];
-            d2 += e * e;
+            e2 += e * e;
         }
+        bits = max(bits, (unsigned long long)__double_as_longlong(e2));
         // a runaway or non-finite particle (|x| or |v| component >= 2^20) stops the run
         bool ok = true;
         for (int c = 0; c < 3; ++c) ok = ok && bounded(xn[c]) && bounded(vn[c]);
@@ -1066,8 +1078,8 @@ __global__ void __launch_bounds__(kBlock) k_integrate(Dev d)
         q.z = (int)(unsigned)__double2ll_rd(xn[2] * R->qinv[2]);
         d.q[p] = q;
     }
-    // check_shifts (E:1745-1762): max |x - x_old|^2; non-negative doubles order as integers
-    unsigned long long bits = (unsigned long long)__double_as_longlong(d2);
+    }
+    // check_shifts (E:1745-1762): max |x - x_old|^2 over the block
     for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long b = __shfl_down_sync(kFull, bits, o);
         bits = b > bits ? b : bits;
@@ -1518,26 +1530,28 @@ void launch_quantize(const Dev &d, cudaStream_t s) { k_quantize<<<d.nblk, kBlock
 
 void launch_pair_sr(const Dev &d, cudaStream_t s, bool en, bool ex)
 {
+    constexpr int L = kLanesSR;
     if (d.fp64) {
-        if (en) k_pair<true, false, true, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
-        else if (ex) k_pair<true, false, false, true><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
-        else k_pair<true, false, false, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
+        if (en) k_pair<true, false, true, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
+        else if (ex) k_pair<true, false, false, true, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
+        else k_pair<true, false, false, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
     } else {
-        if (en) k_pair<false, false, true, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
-        else if (ex) k_pair<false, false, false, true><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
-        else k_pair<false, false, false, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, 1);
+        if (en) k_pair<false, false, true, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
+        else if (ex) k_pair<false, false, false, true, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
+        else k_pair<false, false, false, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
     }
 }
 
 void launch_pair_lr(const Dev &d, cudaStream_t s, bool en, bool force_all)
 {
+    constexpr int L = kLanesLR;
     const int fa = force_all ? 1 : 0;
     if (d.fp64) {
-        if (en) k_pair<true, true, true, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, fa);
-        else k_pair<true, true, false, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, fa);
+        if (en) k_pair<true, true, true, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, fa);
+        else k_pair<true, true, false, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, fa);
     } else {
-        if (en) k_pair<false, true, true, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, fa);
-        else k_pair<false, true, false, false><<<d.nblk, kBlock * kLanes, 0, s>>>(d, fa);
+        if (en) k_pair<false, true, true, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, fa);
+        else k_pair<false, true, false, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, fa);
     }
 }
 
@@ -1596,10 +1610,10 @@ void launch_integrate(const Dev &d, cudaStream_t s)
 {
     if (d.fp64) {
         k_shift<true><<<d.R, 32, 0, s>>>(d);
-        k_integrate<true><<<d.nblk, kBlock, 0, s>>>(d);
+        k_integrate<true><<<d.nblk, kBlock / kIntPer, 0, s>>>(d);
     } else {
         k_shift<false><<<d.R, 32, 0, s>>>(d);
-        k_integrate<false><<<d.nblk, kBlock, 0, s>>>(d);
+        k_integrate<false><<<d.nblk, kBlock / kIntPer, 0, s>>>(d);
     }
 }
 
