@@ -28,6 +28,7 @@ constexpr int kIdxMask = (1 << kExclShift) - 1;
 constexpr int kLanes = 4;            // neighbour-list slots per chunk (nb_idx)
 constexpr int kLanesSR = 1;          // threads per particle in the SR pair kernel (lists of a few pairs)
 constexpr int kLanesLR = 4;          // threads per particle in the LR pair kernel
+constexpr int kThreadsLR = 512;      // threads per LR block (its kBlock particles in kBlock * 4 / 512 passes)
 constexpr int kIntPer = 1;           // particles per thread in the integrator
 
 // neighbour slot k of particle p: chunks of four slots per particle, chunk-major,

@@ -337,9 +337,9 @@ __global__ void __launch_bounds__(kBlock) k_quantize(Dev d)
 // ---------------------------------------------------------------------------
 // pair forces over the full (both-direction) neighbour lists
 // ---------------------------------------------------------------------------
-// Particle block b (kBlock particles) with L threads per particle: slot k of a
-// particle's list goes to its thread k % L.
-template <bool D, bool LR, bool EN, bool EX, int L>
+// Particle block b (kBlock particles) by T threads, L per particle: slot k of a
+// particle's list goes to its thread k % L; the block's particles in kBlock L / T passes.
+template <bool D, bool LR, bool EN, bool EX, int L, int T>
 __device__ void pair_block(const Dev &d, int b, int force_all)
 {
     const int r = d.blk_rep[b];
@@ -356,130 +356,134 @@ __device__ void pair_block(const Dev &d, int b, int force_all)
         __syncthreads();
     }
     const int lane4 = threadIdx.x & (L - 1);
-    const int p = b * kBlock + threadIdx.x / L;
     const int P = d.P;
-    const int4 qp = d.q[p];
-    const int tp = qp.w & 0xff, kp = (qp.w >> 8) & 0xff, act = (qp.w >> 16) & 1;
-    const bool chp = is_charged(kp);
-    const int cnt = act ? (LR ? d.n_lr[p] : d.n_sr[p]) : 0;
-    const int *nbr = LR ? d.nbr_lr : d.nbr_sr;
     int err = 0;
     double e_lj = 0, e_c = 0;
-    if (!D) {
-        long long ax = 0, ay = 0, az = 0;
-        const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
-        const float rc2 = R->rc2f, lo = rc2 * (1.0f - kBand), hi = rc2 * (1.0f + kBand);
-        for (int k = lane4; k < cnt; k += L) {
-            const int raw = __ldg(nbr + nb_idx(k, p, P));
-            const int j = raw & kIdxMask;
-            const float ljw = EX ? (float)(1 - (raw >> kExclShift)) : 1.0f;
-            const int4 qj = __ldg(d.q + j);
-            const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
-            const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
-            const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            const int tj = qj.w & 0xff, kj = (qj.w >> 8) & 0xff;
-            const int J = jn12(tp, tj);
-            float F = 0.0f;
-            if (!LR && ljw != 0.0f && r2 <= s_dlj2[J]) {  // LJ_FORCE (E:801-821)
-                const float rr = sqrtf(r2);
-                const float dr = rr - s_dm[J];
-                const float s = 1.5852f / dr;
-                const float s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
-                F = ljw * (s_flj[J] * (s14 - s8) * dr / rr);
-                if (EN) {
-                    double e;
-                    if ((double)r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
-                    else {
-                        const float s6 = s4 * s2, s12 = s6 * s6;
-                        e = (double)(R->elj[J] * (s12 - 2.0f * s6 + 1.0f));
-                    }
-                    e_lj += 0.5 * (double)ljw * e;
-                }
-            }
-            if ((LR || (chp && is_charged(kj))) && r2 <= hi) {  // COULOMB_TRUNCATED_FORCE (E:841-855)
-                bool in = r2 <= lo || exact_r2(d, R, p, j) <= R->rc2;
-                if (in) {
+    constexpr int kPasses = kBlock * L / T;
+#pragma unroll
+    for (int pass = 0; pass < kPasses; ++pass) {
+        const int p = b * kBlock + pass * (T / L) + (int)threadIdx.x / L;
+        const int4 qp = d.q[p];
+        const int tp = qp.w & 0xff, kp = (qp.w >> 8) & 0xff, act = (qp.w >> 16) & 1;
+        const bool chp = is_charged(kp);
+        const int cnt = act ? (LR ? d.n_lr[p] : d.n_sr[p]) : 0;
+        const int *nbr = LR ? d.nbr_lr : d.nbr_sr;
+        if (!D) {
+            long long ax = 0, ay = 0, az = 0;
+            const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
+            const float rc2 = R->rc2f, lo = rc2 * (1.0f - kBand), hi = rc2 * (1.0f + kBand);
+            for (int k = lane4; k < cnt; k += L) {
+                const int raw = __ldg(nbr + nb_idx(k, p, P));
+                const int j = raw & kIdxMask;
+                const float ljw = EX ? (float)(1 - (raw >> kExclShift)) : 1.0f;
+                const int4 qj = __ldg(d.q + j);
+                const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
+                const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
+                const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                const int tj = qj.w & 0xff, kj = (qj.w >> 8) & 0xff;
+                const int J = jn12(tp, tj);
+                float F = 0.0f;
+                if (!LR && ljw != 0.0f && r2 <= s_dlj2[J]) {  // LJ_FORCE (E:801-821)
                     const float rr = sqrtf(r2);
-                    F += s_qclb[J] / (r2 * rr);
-                    if (EN) e_c += 0.5 * (double)(s_qclb[J] / rr);
-                }
-            }
-            if (F != 0.0f) {
-                ax += to_fix(F * dx, err);
-                ay += to_fix(F * dy, err);
-                az += to_fix(F * dz, err);
-            }
-        }
-        for (int o = 1; o < L; o <<= 1) {
-            ax += __shfl_xor_sync(kFull, ax, o);
-            ay += __shfl_xor_sync(kFull, ay, o);
-            az += __shfl_xor_sync(kFull, az, o);
-        }
-        if (lane4 == 0) {
-            if (LR) {  // the LR force is kept for the MTS interval: overwrite
-                d.flr[p] = (unsigned long long)ax;
-                d.flr[P + p] = (unsigned long long)ay;
-                d.flr[2 * P + p] = (unsigned long long)az;
-            } else if (act) {  // other force kernels run concurrently: accumulate
-                atomic_add_fix(d.f + p, ax);
-                atomic_add_fix(d.f + P + p, ay);
-                atomic_add_fix(d.f + 2 * P + p, az);
-            }
-        }
-    } else {
-        double ax = 0, ay = 0, az = 0;
-        for (int k = lane4; k < cnt; k += L) {
-            const int raw = __ldg(nbr + nb_idx(k, p, P));
-            const int j = raw & kIdxMask;
-            const double ljw = EX ? (double)(1 - (raw >> kExclShift)) : 1.0;
-            const int tj = d.q[j].w & 0xff, kj = (d.q[j].w >> 8) & 0xff;
-            const int J = jn12(tp, tj);
-            double v[3];
-            exact_vec(d, R, p, j, v);
-            const double r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
-            double F = 0.0;
-            if (!LR && ljw != 0.0 && r2 <= R->dlj2_d[J]) {
-                const double rr = sqrt(r2);
-                const double dr = rr + kSig0 - R->dlj_d[J];
-                const double s = kSig0 / dr;
-                const double s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
-                F = ljw * (R->flj_d[J] * (s14 - s8) * dr / rr);
-                if (EN) {
-                    double e;
-                    if (r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
-                    else {
-                        const double s6 = s4 * s2, s12 = s6 * s6;
-                        e = R->elj_d[J] * (s12 - 2.0 * s6 + 1.0);
+                    const float dr = rr - s_dm[J];
+                    const float s = 1.5852f / dr;
+                    const float s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+                    F = ljw * (s_flj[J] * (s14 - s8) * dr / rr);
+                    if (EN) {
+                        double e;
+                        if ((double)r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
+                        else {
+                            const float s6 = s4 * s2, s12 = s6 * s6;
+                            e = (double)(R->elj[J] * (s12 - 2.0f * s6 + 1.0f));
+                        }
+                        e_lj += 0.5 * (double)ljw * e;
                     }
-                    e_lj += 0.5 * ljw * e;
+                }
+                if ((LR || (chp && is_charged(kj))) && r2 <= hi) {  // COULOMB_TRUNCATED_FORCE (E:841-855)
+                    bool in = r2 <= lo || exact_r2(d, R, p, j) <= R->rc2;
+                    if (in) {
+                        const float rr = sqrtf(r2);
+                        F += s_qclb[J] / (r2 * rr);
+                        if (EN) e_c += 0.5 * (double)(s_qclb[J] / rr);
+                    }
+                }
+                if (F != 0.0f) {
+                    ax += to_fix(F * dx, err);
+                    ay += to_fix(F * dy, err);
+                    az += to_fix(F * dz, err);
                 }
             }
-            if ((LR || (chp && is_charged(kj))) && r2 <= R->rc2) {
-                const double rr = sqrt(r2);
-                F += R->qclb_d[J] / (rr * r2);
-                if (EN) e_c += 0.5 * R->qclb_d[J] / rr;
+            for (int o = 1; o < L; o <<= 1) {
+                ax += __shfl_xor_sync(kFull, ax, o);
+                ay += __shfl_xor_sync(kFull, ay, o);
+                az += __shfl_xor_sync(kFull, az, o);
             }
-            ax += v[0] * F;
-            ay += v[1] * F;
-            az += v[2] * F;
-        }
-        for (int o = 1; o < L; o <<= 1) {
-            ax += __shfl_xor_sync(kFull, ax, o);
-            ay += __shfl_xor_sync(kFull, ay, o);
-            az += __shfl_xor_sync(kFull, az, o);
-        }
-        if (lane4 == 0) {
-            if (LR) {
-                double *out = (double *)d.flr;
-                out[p] = ax;
-                out[P + p] = ay;
-                out[2 * P + p] = az;
-            } else if (act) {
-                double *out = (double *)d.f;
-                atomicAdd(out + p, ax);
-                atomicAdd(out + P + p, ay);
-                atomicAdd(out + 2 * P + p, az);
+            if (lane4 == 0) {
+                if (LR) {  // the LR force is kept for the MTS interval: overwrite
+                    d.flr[p] = (unsigned long long)ax;
+                    d.flr[P + p] = (unsigned long long)ay;
+                    d.flr[2 * P + p] = (unsigned long long)az;
+                } else if (act) {  // other force kernels run concurrently: accumulate
+                    atomic_add_fix(d.f + p, ax);
+                    atomic_add_fix(d.f + P + p, ay);
+                    atomic_add_fix(d.f + 2 * P + p, az);
+                }
+            }
+        } else {
+            double ax = 0, ay = 0, az = 0;
+            for (int k = lane4; k < cnt; k += L) {
+                const int raw = __ldg(nbr + nb_idx(k, p, P));
+                const int j = raw & kIdxMask;
+                const double ljw = EX ? (double)(1 - (raw >> kExclShift)) : 1.0;
+                const int tj = d.q[j].w & 0xff, kj = (d.q[j].w >> 8) & 0xff;
+                const int J = jn12(tp, tj);
+                double v[3];
+                exact_vec(d, R, p, j, v);
+                const double r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+                double F = 0.0;
+                if (!LR && ljw != 0.0 && r2 <= R->dlj2_d[J]) {
+                    const double rr = sqrt(r2);
+                    const double dr = rr + kSig0 - R->dlj_d[J];
+                    const double s = kSig0 / dr;
+                    const double s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+                    F = ljw * (R->flj_d[J] * (s14 - s8) * dr / rr);
+                    if (EN) {
+                        double e;
+                        if (r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
+                        else {
+                            const double s6 = s4 * s2, s12 = s6 * s6;
+                            e = R->elj_d[J] * (s12 - 2.0 * s6 + 1.0);
+                        }
+                        e_lj += 0.5 * ljw * e;
+                    }
+                }
+                if ((LR || (chp && is_charged(kj))) && r2 <= R->rc2) {
+                    const double rr = sqrt(r2);
+                    F += R->qclb_d[J] / (rr * r2);
+                    if (EN) e_c += 0.5 * R->qclb_d[J] / rr;
+                }
+                ax += v[0] * F;
+                ay += v[1] * F;
+                az += v[2] * F;
+            }
+            for (int o = 1; o < L; o <<= 1) {
+                ax += __shfl_xor_sync(kFull, ax, o);
+                ay += __shfl_xor_sync(kFull, ay, o);
+                az += __shfl_xor_sync(kFull, az, o);
+            }
+            if (lane4 == 0) {
+                if (LR) {
+                    double *out = (double *)d.flr;
+                    out[p] = ax;
+                    out[P + p] = ay;
+                    out[2 * P + p] = az;
+                } else if (act) {
+                    double *out = (double *)d.f;
+                    atomicAdd(out + p, ax);
+                    atomicAdd(out + P + p, ay);
+                    atomicAdd(out + 2 * P + p, az);
+                }
             }
         }
     }
@@ -490,10 +494,10 @@ __device__ void pair_block(const Dev &d, int b, int force_all)
     if (err) atomicOr(&d.rs[r].err, err);
 }
 
-template <bool D, bool LR, bool EN, bool EX, int L>
-__global__ void __launch_bounds__(kBlock * L) k_pair(Dev d, int force_all)
+template <bool D, bool LR, bool EN, bool EX, int L, int T>
+__global__ void __launch_bounds__(T) k_pair(Dev d, int force_all)
 {
-    pair_block<D, LR, EN, EX, L>(d, blockIdx.x, force_all);
+    pair_block<D, LR, EN, EX, L, T>(d, blockIdx.x, force_all);
 }
 
 // ---------------------------------------------------------------------------
@@ -1530,28 +1534,28 @@ void launch_quantize(const Dev &d, cudaStream_t s) { k_quantize<<<d.nblk, kBlock
 
 void launch_pair_sr(const Dev &d, cudaStream_t s, bool en, bool ex)
 {
-    constexpr int L = kLanesSR;
+    constexpr int L = kLanesSR, T = kBlock * kLanesSR;
     if (d.fp64) {
-        if (en) k_pair<true, false, true, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
-        else if (ex) k_pair<true, false, false, true, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
-        else k_pair<true, false, false, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
+        if (en) k_pair<true, false, true, false, L, T><<<d.nblk, T, 0, s>>>(d, 1);
+        else if (ex) k_pair<true, false, false, true, L, T><<<d.nblk, T, 0, s>>>(d, 1);
+        else k_pair<true, false, false, false, L, T><<<d.nblk, T, 0, s>>>(d, 1);
     } else {
-        if (en) k_pair<false, false, true, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
-        else if (ex) k_pair<false, false, false, true, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
-        else k_pair<false, false, false, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, 1);
+        if (en) k_pair<false, false, true, false, L, T><<<d.nblk, T, 0, s>>>(d, 1);
+        else if (ex) k_pair<false, false, false, true, L, T><<<d.nblk, T, 0, s>>>(d, 1);
+        else k_pair<false, false, false, false, L, T><<<d.nblk, T, 0, s>>>(d, 1);
     }
 }
 
 void launch_pair_lr(const Dev &d, cudaStream_t s, bool en, bool force_all)
 {
-    constexpr int L = kLanesLR;
+    constexpr int L = kLanesLR, T = kThreadsLR;
     const int fa = force_all ? 1 : 0;
     if (d.fp64) {
-        if (en) k_pair<true, true, true, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, fa);
-        else k_pair<true, true, false, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, fa);
+        if (en) k_pair<true, true, true, false, L, T><<<d.nblk, T, 0, s>>>(d, fa);
+        else k_pair<true, true, false, false, L, T><<<d.nblk, T, 0, s>>>(d, fa);
     } else {
-        if (en) k_pair<false, true, true, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, fa);
-        else k_pair<false, true, false, false, L><<<d.nblk, kBlock * L, 0, s>>>(d, fa);
+        if (en) k_pair<false, true, true, false, L, T><<<d.nblk, T, 0, s>>>(d, fa);
+        else k_pair<false, true, false, false, L, T><<<d.nblk, T, 0, s>>>(d, fa);
     }
 }
 
