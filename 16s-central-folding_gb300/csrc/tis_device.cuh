@@ -60,6 +60,7 @@ struct RepParams {
     unsigned long long seed;
     int bt0, bt1, s30, s31, s20, s21, hb0, hb1, hba0, hba1, ca0, ca1;
     int kscr0, maxk;             // hb_K scratch offset and size
+    int pk0;                     // first value of the replica in the group's packed (unpadded) host arrays
 };
 
 // Per-replica dynamic state.

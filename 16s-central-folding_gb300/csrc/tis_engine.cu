@@ -109,6 +109,9 @@ struct Group {
     int base = 0;  // handle-wide index of the group's first replica
     long long launches = 0;
     double *d_scalar = nullptr;
+    int npk = 0;              // particles of the group's replicas (unpadded)
+    double *stage = nullptr;  // nine packed state arrays of npk values (tis_set_states / tis_get_states)
+    double *d_e5 = nullptr;   // five energies per replica (tis_get_all_energies)
 
     ~Group()
     {
@@ -547,6 +550,8 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         R.bt0 = hr.bt0; R.bt1 = hr.bt1; R.s30 = hr.s30; R.s31 = hr.s31; R.s20 = hr.s20; R.s21 = hr.s21;
         R.hb0 = hr.hb0; R.hb1 = hr.hb1; R.hba0 = hr.hba0; R.hba1 = hr.hba1;
         R.kscr0 = kscr;
+        R.pk0 = h->npk;
+        h->npk += n;
         R.maxk = maxk;
         kscr += maxk;
         h->rep.push_back(hr);
@@ -623,7 +628,8 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         (rc = dalloc(O, &d.n_sr, h->P)) || (rc = dalloc(O, &d.n_lr, h->P)) ||
         (rc = dalloc(O, &d.nbr_sr, (size_t)cap_sr * h->P)) || (rc = dalloc(O, &d.nbr_lr, (size_t)cap_lr * h->P)) ||
         (rc = dalloc(O, &d.eterm, (size_t)h->R * tis::kNE)) || (rc = dalloc(O, &d.shift, (size_t)h->R * 3)) || 
-        (rc = dalloc(O, &h->d_scalar, 4)))
+        (rc = dalloc(O, &h->d_scalar, 4)) || (rc = dalloc(O, &h->stage, 9 * (size_t)h->npk)) ||
+        (rc = dalloc(O, &h->d_e5, 5 * (size_t)h->R)))
         return bail(rc);
     int4 *d_bti = nullptr;
     double2 *d_btp = nullptr;
@@ -759,6 +765,39 @@ static int grp_get_state(Group *h, int r, double *x, double *y, double *z, doubl
     for (int c = 0; c < 9; ++c)
         if (dst[c]) TIS_CUDA(cudaMemcpyAsync(dst[c], src[c] + hr.p0, sizeof(double) * hr.n, cudaMemcpyDeviceToHost, h->stream));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return TIS_OK;
+}
+
+// the group's part of packed host arrays: nine arrays, the group's values from offset `off`
+static int grp_set_states(Group *h, const double *const *src, int64_t off)
+{
+    for (int c = 0; c < 9; ++c)
+        TIS_CUDA(cudaMemcpyAsync(h->stage + (size_t)c * h->npk, src[c] + off, sizeof(double) * h->npk,
+                                 cudaMemcpyHostToDevice, h->stream));
+    tis::launch_put_state(h->dev, h->stream, h->stage, h->npk);
+    TIS_CUDA(cudaGetLastError());
+    h->lists_built = false;
+    return TIS_OK;
+}
+
+static int grp_get_states(Group *h, double *const *dst, int64_t off)
+{
+    unsigned mask = 0;
+    for (int c = 0; c < 9; ++c) mask |= dst[c] ? (1u << c) : 0u;
+    tis::launch_get_state(h->dev, h->stream, h->stage, h->npk, mask);
+    TIS_CUDA(cudaGetLastError());
+    for (int c = 0; c < 9; ++c)
+        if (dst[c])
+            TIS_CUDA(cudaMemcpyAsync(dst[c] + off, h->stage + (size_t)c * h->npk, sizeof(double) * h->npk,
+                                     cudaMemcpyDeviceToHost, h->stream));
+    return TIS_OK;
+}
+
+static int grp_get_all_energies(Group *h, double *out)
+{
+    tis::launch_energies(h->dev, h->stream, h->d_e5);
+    TIS_CUDA(cudaGetLastError());
+    TIS_CUDA(cudaMemcpyAsync(out, h->d_e5, sizeof(double) * 5 * h->R, cudaMemcpyDeviceToHost, h->stream));
     return TIS_OK;
 }
 
@@ -974,31 +1013,38 @@ static int grp_profile_stages(Group *h, int64_t n, double *ms)
     if (!h || n < 1 || !ms) return fail(TIS_ERR_ARG, "tis_profile_stages: bad argument");
     int rc;
     if (!h->lists_built && (rc = populate(h))) return rc;
-    cudaEvent_t ev[7];
+    constexpr int kS = TIS_N_STAGES;
+    cudaEvent_t ev[kS + 1];
     for (auto &e : ev) TIS_CUDA(cudaEventCreate(&e));
-    double acc[6] = {0, 0, 0, 0, 0, 0};
+    double acc[kS] = {};
+    const tis::Dev &d = h->dev;
     for (int64_t s = 0; s < n; ++s) {
         TIS_CUDA(cudaEventRecord(ev[0], h->stream));
-        tis::launch_pair_sr(h->dev, h->stream, false, true);
+        tis::launch_pair_sr(d, h->stream, false, true);
         TIS_CUDA(cudaEventRecord(ev[1], h->stream));
-        tis::launch_pair_lr(h->dev, h->stream, false, false);
+        tis::launch_pair_lr(d, h->stream, false, false);
         TIS_CUDA(cudaEventRecord(ev[2], h->stream));
-        tis::launch_topology(h->dev, h->stream, 4 | 8 | 16, false, true, true);
+        tis::launch_topology(d, h->stream, 4 | 8, false, false, true);
         TIS_CUDA(cudaEventRecord(ev[3], h->stream));
-        tis::launch_integrate(h->dev, h->stream);
+        tis::launch_topology(d, h->stream, 16, false, true, true);
         TIS_CUDA(cudaEventRecord(ev[4], h->stream));
-        TIS_CUDA(cudaEventRecord(ev[5], h->stream));  // skin check: fused into the integrator
-        tis::launch_rebuild(h->dev, h->stream);
+        tis::launch_shift(d, h->stream);
+        TIS_CUDA(cudaEventRecord(ev[5], h->stream));
+        tis::launch_move(d, h->stream);  // the skin check runs in its last blocks
         TIS_CUDA(cudaEventRecord(ev[6], h->stream));
-        TIS_CUDA(cudaEventSynchronize(ev[6]));
-        for (int k = 0; k < 6; ++k) {
+        tis::launch_cells(d, h->stream);
+        TIS_CUDA(cudaEventRecord(ev[7], h->stream));
+        tis::launch_search(d, h->stream);
+        TIS_CUDA(cudaEventRecord(ev[8], h->stream));
+        TIS_CUDA(cudaEventSynchronize(ev[kS]));
+        for (int k = 0; k < kS; ++k) {
             float t = 0;
             TIS_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
             acc[k] += t;
         }
     }
     for (auto &e : ev) cudaEventDestroy(e);
-    for (int k = 0; k < 6; ++k) ms[k] = acc[k] / (double)n;
+    for (int k = 0; k < kS; ++k) ms[k] = acc[k] / (double)n;
     h->launches += n * tis::kernel_launches_per_step();
     return check_flags(h);
 }
@@ -1233,6 +1279,54 @@ int tis_get_state(tis_handle *h, int r, double *x, double *y, double *z, double 
     return grp_get_state(g, loc, x, y, z, xo, yo, zo, vx, vy, vz);
 }
 
+int tis_set_states(tis_handle *h, const double *x, const double *y, const double *z, const double *xo,
+                   const double *yo, const double *zo, const double *vx, const double *vy, const double *vz)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    const double *src[9] = {x, y, z, xo, yo, zo, vx, vy, vz};
+    for (int c = 0; c < 9; ++c)
+        if (!src[c]) return fail(TIS_ERR_ARG, "tis_set_states: null array %d", c);
+    int64_t off = 0;
+    int rc = each_group(h, [&](Group *g) {
+        const int r = grp_set_states(g, src, off);
+        off += g->npk;
+        return r;
+    });
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return TIS_OK;
+}
+
+int tis_get_states(tis_handle *h, double *x, double *y, double *z, double *xo, double *yo, double *zo, double *vx,
+                   double *vy, double *vz)
+{
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    double *dst[9] = {x, y, z, xo, yo, zo, vx, vy, vz};
+    int64_t off = 0;
+    int rc = each_group(h, [&](Group *g) {
+        const int r = grp_get_states(g, dst, off);
+        off += g->npk;
+        return r;
+    });
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return TIS_OK;
+}
+
+int tis_get_all_energies(tis_handle *h, double *out)
+{
+    if (!h || !out) return fail(TIS_ERR_ARG, "tis_get_all_energies: bad argument");
+    int64_t off = 0;
+    int rc = each_group(h, [&](Group *g) {
+        const int r = grp_get_all_energies(g, out + 5 * off);
+        off += g->R;
+        return r;
+    });
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return TIS_OK;
+}
+
 int tis_populate_lists(tis_handle *h)
 {
     return each_group(h, [](Group *g) { return grp_populate_lists(g); });
@@ -1314,12 +1408,12 @@ int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
     // stage times of the groups run one after another, summed over the groups
     if (!h || n < 1 || !ms) return fail(TIS_ERR_ARG, "tis_profile_stages: bad argument");
     TIS_CUDA(cudaStreamSynchronize(h->stream));
-    for (int k = 0; k < 6; ++k) ms[k] = 0;
+    for (int k = 0; k < TIS_N_STAGES; ++k) ms[k] = 0;
     for (Group *g : h->groups) {
-        double part[6];
+        double part[TIS_N_STAGES];
         const int rc = grp_profile_stages(g, n, part);
         if (rc) return rc;
-        for (int k = 0; k < 6; ++k) ms[k] += part[k];
+        for (int k = 0; k < TIS_N_STAGES; ++k) ms[k] += part[k];
     }
     return TIS_OK;
 }

@@ -334,6 +334,34 @@ __global__ void __launch_bounds__(kBlock) k_quantize(Dev d)
     d.q[p] = q;
 }
 
+// packed (unpadded, replicas end to end) state <-> the padded device arrays; N is
+// the group's particle count, stage holds the nine arrays of N values each
+__global__ void __launch_bounds__(kBlock) k_put_state(Dev d, const double *stage, int N)
+{
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const RepParams *R = d.rp + d.blk_rep[blockIdx.x];
+    const int i = p - R->p0;
+    if (i >= R->n) return;
+    double *dst[9] = {d.x, d.y, d.z, d.xo, d.yo, d.zo, d.vx, d.vy, d.vz};
+    for (int c = 0; c < 9; ++c) dst[c][p] = stage[(size_t)c * N + R->pk0 + i];
+    int4 q = d.q[p];
+    q.x = (int)(unsigned)(long long)floor(d.x[p] * R->qinv[0]);
+    q.y = (int)(unsigned)(long long)floor(d.y[p] * R->qinv[1]);
+    q.z = (int)(unsigned)(long long)floor(d.z[p] * R->qinv[2]);
+    d.q[p] = q;
+}
+
+__global__ void __launch_bounds__(kBlock) k_get_state(Dev d, double *stage, int N, unsigned mask)
+{
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const RepParams *R = d.rp + d.blk_rep[blockIdx.x];
+    const int i = p - R->p0;
+    if (i >= R->n) return;
+    const double *src[9] = {d.x, d.y, d.z, d.xo, d.yo, d.zo, d.vx, d.vy, d.vz};
+    for (int c = 0; c < 9; ++c)
+        if ((mask >> c) & 1u) stage[(size_t)c * N + R->pk0 + i] = src[c][p];
+}
+
 // ---------------------------------------------------------------------------
 // pair forces over the full (both-direction) neighbour lists
 // ---------------------------------------------------------------------------
@@ -1525,12 +1553,57 @@ __global__ void k_rg(Dev d, int r, double *out)
     if (threadIdx.x == 0) *out = sqrt(s[0] / R->nrna);
 }
 
+// E2_HB, E3_HB, E2_STACK, E3_STACK and Rg of every replica (one block each)
+__global__ void k_energies(Dev d, double *out)
+{
+    const int r = blockIdx.x;
+    const RepParams *R = d.rp + r;
+    __shared__ double s_red[3 * 32];
+    double c[3] = {0, 0, 0};
+    for (int i = threadIdx.x; i < R->nrna; i += blockDim.x) {
+        c[0] += d.x[R->p0 + i];
+        c[1] += d.y[R->p0 + i];
+        c[2] += d.z[R->p0 + i];
+    }
+    block_sum<3>(c, s_red);
+    __shared__ double s_c[3];
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; ++k) s_c[k] = c[k] / R->nrna;
+    __syncthreads();
+    double sq[1] = {0};
+    for (int i = threadIdx.x; i < R->nrna; i += blockDim.x) {
+        const double a = d.x[R->p0 + i] - s_c[0], b = d.y[R->p0 + i] - s_c[1], e = d.z[R->p0 + i] - s_c[2];
+        sq[0] += a * a + b * b + e * e;
+    }
+    block_sum<1>(sq, s_red);
+    if (threadIdx.x == 0) {
+        const RepState *S = d.rs + r;
+        out[5 * r] = S->e2hb;
+        out[5 * r + 1] = S->e3hb;
+        out[5 * r + 2] = S->e2st;
+        out[5 * r + 3] = S->e3st;
+        out[5 * r + 4] = sqrt(sq[0] / R->nrna);
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 void launch_quantize(const Dev &d, cudaStream_t s) { k_quantize<<<d.nblk, kBlock, 0, s>>>(d); }
+
+void launch_put_state(const Dev &d, cudaStream_t s, const double *stage, int n)
+{
+    k_put_state<<<d.nblk, kBlock, 0, s>>>(d, stage, n);
+}
+
+void launch_get_state(const Dev &d, cudaStream_t s, double *stage, int n, unsigned mask)
+{
+    k_get_state<<<d.nblk, kBlock, 0, s>>>(d, stage, n, mask);
+}
+
+void launch_energies(const Dev &d, cudaStream_t s, double *out) { k_energies<<<d.R, 256, 0, s>>>(d, out); }
 
 void launch_pair_sr(const Dev &d, cudaStream_t s, bool en, bool ex)
 {
@@ -1610,23 +1683,40 @@ void launch_noise(const Dev &d, cudaStream_t s)
     else k_noise<false><<<d.R, kTopoThreads, 0, s>>>(d);
 }
 
+void launch_shift(const Dev &d, cudaStream_t s)
+{
+    if (d.fp64) k_shift<true><<<d.R, 32, 0, s>>>(d);
+    else k_shift<false><<<d.R, 32, 0, s>>>(d);
+}
+
+void launch_move(const Dev &d, cudaStream_t s)
+{
+    if (d.fp64) k_integrate<true><<<d.nblk, kBlock / kIntPer, 0, s>>>(d);
+    else k_integrate<false><<<d.nblk, kBlock / kIntPer, 0, s>>>(d);
+}
+
 void launch_integrate(const Dev &d, cudaStream_t s)
 {
-    if (d.fp64) {
-        k_shift<true><<<d.R, 32, 0, s>>>(d);
-        k_integrate<true><<<d.nblk, kBlock / kIntPer, 0, s>>>(d);
-    } else {
-        k_shift<false><<<d.R, 32, 0, s>>>(d);
-        k_integrate<false><<<d.nblk, kBlock / kIntPer, 0, s>>>(d);
-    }
+    launch_shift(d, s);
+    launch_move(d, s);
+}
+
+void launch_cells(const Dev &d, cudaStream_t s)
+{
+    if (d.fp64) k_cells<true><<<d.R, kCellThreads, d.cell_smem, s>>>(d);
+    else k_cells<false><<<d.R, kCellThreads, d.cell_smem, s>>>(d);
+}
+
+void launch_search(const Dev &d, cudaStream_t s)
+{
+    if (d.fp64) k_pair_search<true><<<d.search_warps / 4, 128, 0, s>>>(d);
+    else k_pair_search<false><<<d.search_warps / 4, 128, 0, s>>>(d);
 }
 
 void launch_rebuild(const Dev &d, cudaStream_t s)
 {
-    if (d.fp64) k_cells<true><<<d.R, kCellThreads, d.cell_smem, s>>>(d);
-    else k_cells<false><<<d.R, kCellThreads, d.cell_smem, s>>>(d);
-    if (d.fp64) k_pair_search<true><<<d.search_warps / 4, 128, 0, s>>>(d);
-    else k_pair_search<false><<<d.search_warps / 4, 128, 0, s>>>(d);
+    launch_cells(d, s);
+    launch_search(d, s);
 }
 
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s) { k_force_rebuild<<<d.R, 128, 0, s>>>(d); }

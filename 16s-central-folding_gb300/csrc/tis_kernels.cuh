@@ -87,6 +87,10 @@ __host__ __device__ inline HbLayout hb_layout(int hb_nmax, int ca_nmax, int k_nm
 
 // Launchers (stream-ordered; gated per replica on device flags where noted).
 void launch_quantize(const Dev &d, cudaStream_t s);
+// the group's state packed (replicas end to end, n values per array, nine arrays) <-> device
+void launch_put_state(const Dev &d, cudaStream_t s, const double *stage, int n);
+void launch_get_state(const Dev &d, cudaStream_t s, double *stage, int n, unsigned mask);
+void launch_energies(const Dev &d, cudaStream_t s, double *out);  // 5 values per replica
 // excl_in_list: the hot path skips the LJ of bonded pairs in the SR kernel and
 // does not subtract it in the bonded kernel (the reference's net force, without
 // the cancellation of two large equal terms); false gives the reference's
@@ -98,7 +102,12 @@ void launch_noise(const Dev &d, cudaStream_t s);  // the step's Gaussians only
 int configure_kernels(const Dev &d);
               // kernel attributes (shared-memory limits); cudaError_t
 void launch_integrate(const Dev &d, cudaStream_t s);  // recentring shift, then the particles
-void launch_rebuild(const Dev &d, cudaStream_t s);  // gated on RepState::rebuild
+void launch_rebuild(const Dev &d, cudaStream_t s);  // gated on RepState::rebuild: cells, then pair search
+// the parts of launch_integrate and launch_rebuild, for stage timing
+void launch_shift(const Dev &d, cudaStream_t s);
+void launch_move(const Dev &d, cudaStream_t s);
+void launch_cells(const Dev &d, cudaStream_t s);
+void launch_search(const Dev &d, cudaStream_t s);
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s);
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out);
 int kernel_launches_per_step();

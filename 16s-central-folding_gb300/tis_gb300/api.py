@@ -74,6 +74,9 @@ def _declare(L):
         "tis_destroy": [vp],
         "tis_set_state": [vp, i32] + [dp] * 9,
         "tis_get_state": [vp, i32] + [dp] * 9,
+        "tis_set_states": [vp] + [dp] * 9,
+        "tis_get_states": [vp] + [dp] * 9,
+        "tis_get_all_energies": [vp, dp],
         "tis_populate_lists": [vp],
         "tis_get_cells": [vp, i32, ip, ip],
         "tis_get_pairs": [vp, i32, i32, ip, i64, C.POINTER(C.c_int64)],
@@ -108,7 +111,8 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_pairs", "tis_get_hb_status", "tis_compute_forces", "tis_deterministic_forces", "tis_full_forces",
             "tis_move_rigid_units", "tis_check_shifts", "tis_step", "tis_sync", "tis_get_energies",
             "tis_get_stack_energies", "tis_get_counters", "tis_get_info", "tis_replica_size", "tis_get_launch_count",
-            "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc"]
+            "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc", "tis_set_states",
+            "tis_get_states", "tis_get_all_energies"]
 
 
 def pair_lists_noalloc(d_x, d_y, d_z, d_kind, n, box, sr_radius, lr_radius, d_sr, sr_cap, d_lr, lr_cap, d_counts,
@@ -254,6 +258,33 @@ class Engine:
         _check(lib().tis_get_state(self.h, r, *[_dp(a) for a in arrs]))
         return dict(zip(STATE_NAMES, arrs))
 
+    def set_states(self, states):
+        """Every replica's state in one call: `states` maps each of STATE_NAMES to one
+        array holding the replicas' particles end to end (or is a list of per-replica dicts)."""
+        if isinstance(states, (list, tuple)):
+            states = {k: np.concatenate([st[k] for st in states]) for k in STATE_NAMES}
+        arrs = [np.ascontiguousarray(states[k], dtype=np.float64) for k in STATE_NAMES]
+        for a in arrs:
+            if a.size != sum(self.n):
+                raise ValueError(f"expected {sum(self.n)} values per array, got {a.size}")
+        _check(lib().tis_set_states(self.h, *[_dp(a) for a in arrs]))
+
+    def get_states(self, names=STATE_NAMES, out=None):
+        """Every replica's state in one call: {name: array of all particles, replicas end to end}."""
+        out = {} if out is None else out
+        for k in names:
+            if k not in out:
+                out[k] = np.zeros(sum(self.n))
+        ptrs = [(_dp(out[k]) if k in names else None) for k in STATE_NAMES]
+        _check(lib().tis_get_states(self.h, *ptrs))
+        return {k: out[k] for k in names}
+
+    def all_energies(self, out=None):
+        """(replicas, 5) array of tis_get_energies' five values for every replica."""
+        out = np.zeros((len(self.n), 5)) if out is None else out
+        _check(lib().tis_get_all_energies(self.h, _dp(out)))
+        return out
+
     def populate_lists(self):
         _check(lib().tis_populate_lists(self.h))
 
@@ -323,11 +354,15 @@ class Engine:
         _check(lib().tis_get_counters(self.h, r, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
 
+    STAGES = ["pair_sr", "pair_lr", "bonded", "hbond", "shift", "integrate", "cells", "search"]
+
     def profile_stages(self, n):
-        """Mean ms per step of: pair_sr, pair_lr, topology, integrate, control, rebuild."""
-        ms = np.zeros(6)
+        """Mean ms per step of each stage run alone (kernels one after another, summed
+        over the replica groups): SR pairs, LR pairs, bonded + stacking, H-bonds +
+        Gaussians, shift, integrator, cell binning, pair search."""
+        ms = np.zeros(len(self.STAGES))
         _check(lib().tis_profile_stages(self.h, n, _dp(ms)))
-        return dict(zip(["pair_sr", "pair_lr", "topology", "integrate", "control", "rebuild"], ms))
+        return dict(zip(self.STAGES, ms))
 
     def launches(self):
         n = C.c_int64()

@@ -127,17 +127,45 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-# Algorithmic (compulsory) HBM bytes per unit of each stage:
-#   integrate: per particle-step, read x, x_old, v (72 B), the SR and LR fixed-point force
-#     sums (48 B) and the packed position (16 B); write x, x_old, v (72 B) and the packed
-#     position (16 B): 224 B
-#   pair_sr / pair_lr: per particle-step (LR: per particle of a replica whose LR is due),
-#     the particle's packed position (16 B) and its force write (24 B): 40 B
-#   topology: per bonded term or stack, its index/parameter record (32 B); per H-bond
-#     candidate (48 B)
-#   rebuild: per particle of a replica that rebuilds, ~50 B (position read, cell id,
-#     cell-ordered copy, list counts)
-ALG_BYTES_PER_PARTICLE = {"integrate": 224, "pair_sr": 40, "pair_lr": 40, "rebuild": 50}
+# Algorithmic (compulsory) HBM bytes of each stage per step of the whole batch:
+# every array the stage must read or write once, gathers through cache not counted
+# again.  n: particles; sr, lr: mean SR / LR neighbours per particle; lr_frac: share
+# of particles whose LR sum is refreshed in a step; nreb: particles of the replicas
+# that rebuild in a step; nrna: RNA beads; items: bonded terms + stacks; nhb: H-bond
+# candidates (all summed over the replicas).
+#   pair_sr:   q (16) + count (4) + list (4 sr) + force sum read-modify-write (48)
+#   pair_lr:   (q 16 + count 4 + list 4 lr + LR force store 24) x lr_frac
+#   bonded:    index/parameter record per item (32) + force RMW per RNA bead (48) + its q (16)
+#   hbond:     per candidate index/natives record (96) + its six beads' q (96) and force
+#              RMW (288); the step's 3000 Gaussians per replica (8 each)
+#   shift:     per replica the centre bead's state (about 200)
+#   integrate: read x, x_old, v (72), force sums (48), q (16); write x, x_old, v (72),
+#              zeroed force sum (24), q (16): 248
+#   cells:     per rebuilt particle x, y, z, q (40), cell id (4, written and read), slot
+#              (4, written and read), cell-ordered copy of q (16 written)
+#   search:    per rebuilt particle its cell-ordered q (16), cell id (4), the list
+#              entries written (4 (sr + lr)) and counts (8)
+def stage_bytes(n, sr, lr, lr_frac, nreb, nrna, items, nhb, nrep):
+    return {
+        "pair_sr": (16 + 4 + 4 * sr + 48) * n,
+        "pair_lr": (16 + 4 + 4 * lr + 24) * n * lr_frac,
+        "bonded": 32 * items + (48 + 16) * nrna,
+        "hbond": (96 + 96 + 288) * nhb + 3000 * 8 * nrep,
+        "shift": 200 * nrep,
+        "integrate": 248 * n,
+        "cells": (40 + 8 + 8 + 16) * nreb,
+        "search": (16 + 4 + 4 * (sr + lr) + 8) * nreb,
+    }
+
+
+# DRAM bytes per launch of each step kernel for one group of 8 replicas (43k
+# particles), from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum,
+# cold L2, serialised launches) of the command
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+#       --clock-control none -s 400 -c 64 python bench.py --steps 40 --warmup 3 --no-extras
+# (None: not captured).  Scaled to the batch by the number of groups.
+NCU_DRAM_BYTES_PER_GROUP = {"pair_sr": 3.12e6, "pair_lr": None, "bonded": 1.24e6, "hbond": 0.48e6,
+                            "shift": 0.04e6, "integrate": 5.51e6, "cells": 0.03e6, "search": 0.04e6}
 
 
 def cpu_sample(files, specs, steps, workers):
@@ -258,55 +286,66 @@ def gpu_arm(args):
                                   "ms_per_step": ms_per_step, "note": "timed loop only (--no-extras)"}), flush=True)
             return
 
-        # end to end through the C ABI with host buffers: every 100 steps a state
-        # upload from pinned host memory and a frame (positions + energies) read back
+        # end to end through the C ABI with host buffers: every 100 steps every
+        # replica's state is uploaded from pinned host memory (one call), the lists
+        # are rebuilt, 100 steps run, and a frame (positions + the five energies of
+        # every replica) is read back into pinned host memory
         e2e = None
         if rank == 0:
             E2E_STEPS = 100
             n_it = max(1, min(10, K // E2E_STEPS))
-            states = [eng.get_state(r) for r in range(N_REPLICAS)]
-            pinned = []
-            for st in states:
-                pinned.append({k: torch.from_numpy(v).pin_memory().numpy() for k, v in st.items()})
-            h2d = sum(v.nbytes for st in pinned for v in st.values())
+            state = eng.get_states()
+            pinned = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in state.items()}
+            frame = {k: torch.zeros(v.size, dtype=torch.float64).pin_memory().numpy() for k, v in state.items()
+                     if k in ("x", "y", "z")}
+            energies = torch.zeros((N_REPLICAS, 5), dtype=torch.float64).pin_memory().numpy()
+            h2d = sum(v.nbytes for v in pinned.values())
+            d2h = sum(v.nbytes for v in frame.values()) + energies.nbytes
             t0 = time.perf_counter()
-            d2h = 0
             for _ in range(n_it):
-                for r in range(N_REPLICAS):
-                    eng.set_state(r, pinned[r])
+                eng.set_states(pinned)
                 eng.populate_lists()
                 eng.step(E2E_STEPS)
-                for r in range(N_REPLICAS):
-                    st = eng.get_state(r)
-                    en = eng.energies(r)
-                    d2h += 3 * st["x"].nbytes + en.nbytes
+                eng.get_states(("x", "y", "z"), out=frame)
+                eng.all_energies(out=energies)
             eng.sync()
             dt = time.perf_counter() - t0
             e2e = {"value": N_REPLICAS * E2E_STEPS * n_it / dt, "unit": UNIT,
-                   "h2d_bytes_per_step": h2d // E2E_STEPS, "d2h_bytes_per_step": d2h // (E2E_STEPS * n_it),
+                   "h2d_bytes_per_step": h2d // E2E_STEPS, "d2h_bytes_per_step": d2h // E2E_STEPS,
                    "frame_every_steps": E2E_STEPS}
 
-        # per-stage device time (CUDA events between the stage launches)
+        # per-stage device time: each stage's kernels alone, CUDA events between them on
+        # the group streams, ms per step summed over the replica groups
         stages = eng.profile_stages(50)
-        dom = max(stages, key=stages.get)
         peak, peak_kind = measured_peaks()
         n_part = sum(eng.n)
         cnt = [eng.counters(r) for r in range(N_REPLICAS)]
-        rebuild_rate = sum(eng.n[r] * c[1] / max(1, c[0]) for r, c in enumerate(cnt))  # particles rebuilt / step
-        lr_rate = sum(eng.n[r] / 10.0 for r in range(N_REPLICAS))  # LR refresh every 10 steps (plus rebuilds)
-        units = {"integrate": n_part, "pair_sr": n_part, "pair_lr": lr_rate, "rebuild": rebuild_rate}
-        roofline = {"bound": "hbm", "kernel": dom, "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
-                    "traffic": None}
-        if dom in ALG_BYTES_PER_PARTICLE:
-            alg = ALG_BYTES_PER_PARTICLE[dom] * units[dom]
-            achieved = alg / (stages[dom] * 1e-3) / 1e9
-            roofline.update({"achieved": achieved, "frac": achieved / peak, "alg_bytes_per_launch": alg})
-        else:
-            roofline.update({"achieved": None, "frac": None})
-        integ_alg = ALG_BYTES_PER_PARTICLE["integrate"] * n_part
-        integ_gbs = integ_alg / (stages["integrate"] * 1e-3) / 1e9
-        roofline["integrate"] = {"achieved": integ_gbs, "frac": integ_gbs / peak, "alg_bytes_per_launch": integ_alg,
-                                 "note": "FP64-pipe bound (ncu: 81.6% FP64 pipe active)"}
+        reb_rep = sum(c[1] / max(1, c[0]) for c in cnt)  # replicas rebuilt per step
+        nreb = reb_rep * n_part / N_REPLICAS
+        sampled = [0, N_REPLICAS - 1]  # mean list lengths from two replicas (0 and 20 mM Mg)
+        sr = sum(2 * len(eng.pairs(r, 0)) for r in sampled) / sum(eng.n[r] for r in sampled)
+        lr = sum(2 * len(eng.pairs(r, 1)) for r in sampled) / sum(eng.n[r] for r in sampled)
+        sd = systems[0].to_dict()
+        nrna = int(np.asarray(sd["n_rna"]).ravel()[0]) * N_REPLICAS
+        items = (len(sd["bt_kind"]) + len(sd["st3_E"]) + len(sd["st2_E"])) * N_REPLICAS
+        nhb = len(sd["hb_E"]) * N_REPLICAS
+        alg = stage_bytes(n_part, sr, lr, 0.1 + reb_rep / N_REPLICAS, nreb, nrna, items, nhb, N_REPLICAS)
+        groups = eng.params.groups or (N_REPLICAS + 7) // 8
+        per_stage = {}
+        for k, ms_k in stages.items():
+            gbs = alg[k] / (ms_k * 1e-3) / 1e9 if ms_k > 0 else None
+            per_stage[k] = {"ms": ms_k, "alg_bytes": alg[k], "achieved_gbs": gbs,
+                            "frac": gbs / peak if gbs is not None else None}
+        dom = max(stages, key=stages.get)
+        traffic = NCU_DRAM_BYTES_PER_GROUP.get(dom)
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": per_stage[dom]["achieved_gbs"], "peak": peak,
+                    "unit": "GB/s", "frac": per_stage[dom]["frac"],
+                    "traffic": traffic * groups if traffic is not None else None,
+                    "alg_bytes_per_launch": alg[dom], "peak_source": peak_kind,
+                    "mean_neighbours": {"sr": sr, "lr": lr}, "stages": per_stage,
+                    "note": "stage = its kernels over all replica groups run alone; launch = one step of "
+                            "the batch; the integrator is FP64-pipe bound, the H-bond kernel latency bound "
+                            "(serial Monte Carlo per replica)"}
 
         # the plain single-replica FP64 GPU path (the denominator of the batching target)
         plain = Engine([systems[len(systems) // 2]], precision=PREC_FP64, device=local, use_graph=0)

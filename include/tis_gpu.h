@@ -139,6 +139,17 @@ int tis_set_state(tis_handle *h, int replica, const double *x, const double *y, 
 int tis_get_state(tis_handle *h, int replica, double *x, double *y, double *z,
                   double *xo, double *yo, double *zo, double *vx, double *vy, double *vz);
 
+/* The state of every replica in one call: each array holds the replicas' particles
+ * end to end (replica 0's n_0 values, then replica 1's, ...; total the sum of
+ * tis_replica_size), one host-device copy per array and replica group.  Null
+ * arrays are skipped by tis_get_states; tis_set_states needs all nine.  No
+ * counterpart in the reference, which holds one system per process. */
+int tis_set_states(tis_handle *h, const double *x, const double *y, const double *z,
+                   const double *xo, const double *yo, const double *zo,
+                   const double *vx, const double *vy, const double *vz);
+int tis_get_states(tis_handle *h, double *x, double *y, double *z,
+                   double *xo, double *yo, double *zo, double *vx, double *vy, double *vz);
+
 /* populate_lists (E:1546-1737) for every replica: cell binning, SR/LR neighbour
  * lists, hydrogen-bond candidate status; resets PROGRESS (E:6238). */
 int tis_populate_lists(tis_handle *h);
@@ -188,6 +199,8 @@ int tis_sync(tis_handle *h);
 /* E2_HB, E3_HB, E2_STACK, E3_STACK of the last step and Rg of the RNA
  * (the five columns of the Energies file, E:6312). */
 int tis_get_energies(tis_handle *h, int replica, double *out5);
+/* The same five values for every replica: out[5 * replica + k]. */
+int tis_get_all_energies(tis_handle *h, double *out);
 /* Energies of the tertiary stacks of the last step (the Contacts file, E:6290). */
 int tis_get_stack_energies(tis_handle *h, int replica, double *out, int64_t cap, int64_t *n);
 /* Step counter (klok), rebuild count and rand() draws consumed by one replica. */
@@ -197,10 +210,12 @@ int tis_get_counters(tis_handle *h, int replica, int64_t *klok, int64_t *rebuild
 int tis_get_info(tis_handle *h, int *n_replicas, int *device, void **stream);
 int tis_replica_size(tis_handle *h, int replica, int *n_particles);
 
-/* Runs n steps with direct launches and CUDA events between the stages, on the
- * handle's stream; ms[6] receives the mean duration per step of: SR pair forces,
- * LR pair forces, topology terms (bonded/stacking/H-bond + noise), integrator,
- * skin check, list rebuild (all six rebuild kernels). */
+/* Runs n steps with direct launches, one kernel after another, and CUDA events
+ * between them, on each group's stream; ms[TIS_N_STAGES] receives the mean
+ * duration per step, summed over the replica groups, of: SR pair forces, LR pair
+ * forces, bonded + stacking terms, H-bonds + the step's Gaussians, recentring
+ * shift, integrator (+ skin check), cell binning, pair search. */
+#define TIS_N_STAGES 8
 int tis_profile_stages(tis_handle *h, int64_t n, double *ms);
 
 /* Kernel launches enqueued by tis_step since the handle was created. */

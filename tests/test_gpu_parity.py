@@ -287,6 +287,42 @@ def test_replica_groups_equal_one_group_bitwise(synth_dir):
                 assert np.array_equal(states[r][k], runs[0][0][r][k]), (r, k)
 
 
+def test_batched_state_calls_equal_per_replica_calls(synth_dir):
+    """tis_set_states / tis_get_states / tis_get_all_energies (all replicas, packed
+    end to end, one copy per array and group) equal the per-replica calls."""
+    f = synth_dir["small"]
+    specs = [dict(seed=3 + 2 * k, n_mg=10 + 2 * k, n_cl=261 + 4 * k, n_k=317) for k in range(5)]
+    sys_ = [load(f, "small", **sp) for sp in specs]
+    e = Engine(sys_, groups=2)
+    e.populate_lists()
+    e.step(60)
+    e.sync()
+    packed = e.get_states()
+    per = [e.get_state(r) for r in range(len(sys_))]
+    for k in per[0]:
+        assert np.array_equal(packed[k], np.concatenate([p[k] for p in per])), k
+    en = e.all_energies()
+    for r in range(len(sys_)):
+        assert np.array_equal(en[r], e.energies(r)), r
+    mod = {k: v.copy() for k, v in packed.items()}
+    mod["vx"] *= 0.5
+    batched = Engine(sys_, groups=3)
+    batched.set_states(mod)
+    single = Engine(sys_, groups=1)
+    off = 0
+    for r in range(len(sys_)):
+        n = single.n[r]
+        single.set_state(r, {k: mod[k][off:off + n] for k in mod})
+        off += n
+    for eng in (batched, single):
+        eng.populate_lists()
+        eng.step(40)
+        eng.sync()
+    a, b = batched.get_states(), single.get_states()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
 def test_split_calls_and_graph_equal_fused_step(systems):
     """The four drop-in calls (deterministic_forces, full_forces, move_rigid_units,
     check_shifts), the fused step and the captured graph give identical states."""
