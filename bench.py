@@ -158,14 +158,13 @@ def stage_bytes(n, sr, lr, lr_frac, nreb, nrna, items, nhb, nrep):
     }
 
 
-# DRAM bytes per launch of each step kernel for one group of 8 replicas (43k
-# particles), from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum,
-# cold L2, serialised launches) of the command
-#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
-#       --clock-control none -s 400 -c 64 python bench.py --steps 40 --warmup 3 --no-extras
-# (None: not captured).  Scaled to the batch by the number of groups.
-NCU_DRAM_BYTES_PER_GROUP = {"pair_sr": 3.12e6, "pair_lr": None, "bonded": 1.24e6, "hbond": 0.48e6,
-                            "shift": 0.04e6, "integrate": 5.51e6, "cells": 0.03e6, "search": 0.04e6}
+# DRAM bytes per launch of each step kernel for one group of 8 replicas (about 43k
+# particles), dram__bytes_read.sum + dram__bytes_write.sum of one launch (cold L2,
+# serialised) from ncu captures of `python bench.py --steps 40 --warmup 3 --no-extras`
+# with --clock-control none, --kernel-name-base mangled and -k set to the kernel
+# (None: no capture of a stepping launch).  Scaled to the batch by the number of groups.
+NCU_DRAM_BYTES_PER_GROUP = {"pair_sr": 3.04e6, "pair_lr": None, "bonded": 1.24e6, "hbond": 0.48e6,
+                            "shift": 0.04e6, "integrate": 5.35e6, "cells": 0.03e6, "search": None}
 
 
 def cpu_sample(files, specs, steps, workers):
