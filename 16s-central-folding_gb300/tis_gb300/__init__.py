@@ -6,7 +6,8 @@ from tis_gb300 import System, Engine
     eng.step(1000); eng.sync()
 """
 from .api import (ENERGY_NAMES, NOISE_OFF, NOISE_REFERENCE, PREC_FP64, PREC_MIXED, STATE_NAMES, TERM_BONDED,
-                  TERM_HB, TERM_LR, TERM_SR, TERM_STACK, Engine, System, TisError, lib)
+                  TERM_HB, TERM_LR, TERM_SR, TERM_STACK, Engine, System, TisError, lib, read_last_frame)
 
 __all__ = ["System", "Engine", "TisError", "lib", "STATE_NAMES", "ENERGY_NAMES", "TERM_SR", "TERM_LR",
-           "TERM_BONDED", "TERM_STACK", "TERM_HB", "PREC_MIXED", "PREC_FP64", "NOISE_REFERENCE", "NOISE_OFF"]
+           "TERM_BONDED", "TERM_STACK", "TERM_HB", "PREC_MIXED", "PREC_FP64", "NOISE_REFERENCE", "NOISE_OFF",
+           "read_last_frame"]

@@ -77,6 +77,8 @@ def _declare(L):
         "tis_set_states": [vp] + [dp] * 9,
         "tis_get_states": [vp] + [dp] * 9,
         "tis_get_all_energies": [vp, dp],
+        "tis_write_frame": [vp, i32, cp, cp, cp],
+        "tis_read_last_frame": [cp, i32, dp, dp, dp, C.POINTER(C.c_int64)],
         "tis_populate_lists": [vp],
         "tis_get_cells": [vp, i32, ip, ip],
         "tis_get_pairs": [vp, i32, i32, ip, i64, C.POINTER(C.c_int64)],
@@ -112,7 +114,15 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_move_rigid_units", "tis_check_shifts", "tis_step", "tis_sync", "tis_get_energies",
             "tis_get_stack_energies", "tis_get_counters", "tis_get_info", "tis_replica_size", "tis_get_launch_count",
             "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc", "tis_set_states",
-            "tis_get_states", "tis_get_all_energies"]
+            "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame"]
+
+
+def read_last_frame(path, n):
+    """(x, y, z, frames): the last frame of a reference Coordinates file of n particles."""
+    x, y, z = np.zeros(n), np.zeros(n), np.zeros(n)
+    frames = C.c_int64()
+    _check(lib().tis_read_last_frame(path.encode(), n, _dp(x), _dp(y), _dp(z), C.byref(frames)))
+    return x, y, z, frames.value
 
 
 def pair_lists_noalloc(d_x, d_y, d_z, d_kind, n, box, sr_radius, lr_radius, d_sr, sr_cap, d_lr, lr_cap, d_counts,
@@ -284,6 +294,11 @@ class Engine:
         out = np.zeros((len(self.n), 5)) if out is None else out
         _check(lib().tis_get_all_energies(self.h, _dp(out)))
         return out
+
+    def write_frame(self, r, contacts=None, coordinates=None, energies=None):
+        """Appends replica r's frame to the reference's Contacts / Coordinates / Energies files."""
+        enc = lambda p: p.encode() if p is not None else None
+        _check(lib().tis_write_frame(self.h, r, enc(contacts), enc(coordinates), enc(energies)))
 
     def populate_lists(self):
         _check(lib().tis_populate_lists(self.h))

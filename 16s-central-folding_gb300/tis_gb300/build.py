@@ -9,7 +9,8 @@ OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libtis_gpu.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["tis_kernels.cu", "tis_engine.cu", "tis_system.cpp", "tis_loader.cpp", "tis_noalloc.cu"]
+SOURCES = ["tis_kernels.cu", "tis_engine.cu", "tis_system.cpp", "tis_loader.cpp", "tis_noalloc.cu", "tis_output.cpp"]
+RUN = os.path.join(OUT, "tis_run")  # the command-line program (csrc/tis_run.cpp) over the library
 
 
 def _flags():
@@ -28,14 +29,21 @@ def _compile(src):
 
 def build(verbose=False, force=False):
     os.makedirs(OUT, exist_ok=True)
-    srcs = [os.path.join(CSRC, s) for s in SOURCES] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    srcs = [os.path.join(CSRC, s) for s in SOURCES + ["tis_run.cpp"]] + \
+        [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     srcs.append(os.path.join(PKG, "..", "include", "tis_gpu.h"))
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > max(os.path.getmtime(s) for s in srcs):
+    if not force and os.path.exists(LIB) and os.path.exists(RUN) and \
+            min(os.path.getmtime(LIB), os.path.getmtime(RUN)) > max(os.path.getmtime(s) for s in srcs):
         return LIB
     try:
         with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
             objs = list(ex.map(_compile, SOURCES))
         cmd = [NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(NVCC))), "lib64")
+        cmd = [NVCC, "-std=c++17", "-O2", "-I", os.path.join(PKG, "..", "include"), "-x", "c++",
+               os.path.join(CSRC, "tis_run.cpp"), "-o", RUN, "-L", OUT, "-ltis_gpu",
+               "-Xlinker", "-rpath,$ORIGIN:" + cuda_lib]
         subprocess.run(cmd, check=True, capture_output=True, text=True)
     except subprocess.CalledProcessError as e:
         raise RuntimeError(f"building libtis_gpu.so failed:\n{' '.join(e.cmd)}\n{e.stdout}\n{e.stderr}") from None

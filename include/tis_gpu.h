@@ -201,6 +201,19 @@ int tis_sync(tis_handle *h);
 int tis_get_energies(tis_handle *h, int replica, double *out5);
 /* The same five values for every replica: out[5 * replica + k]. */
 int tis_get_all_energies(tis_handle *h, double *out);
+
+/* Appends one frame of a replica to the reference's three output files (any may
+ * be NULL): the Contacts file ("%+.3f " per tertiary stack energy, then a
+ * newline, E:6290-6294), the Coordinates file (x, y, z, each as the reference's
+ * 1-based array of n+1 doubles with the unused index 0 written as 0, E:6298-6304)
+ * and the Energies file ("%le %le %le %le %le\n": E2_HB, E3_HB, E2_STACK,
+ * E3_STACK as the sum of the stack energies, Rg, E:6308-6312). */
+int tis_write_frame(tis_handle *h, int replica, const char *contacts, const char *coordinates,
+                    const char *energies);
+/* The restart read of E:6181-6211: the last complete frame of a Coordinates file
+ * of n particles into x, y, z (n values each, any may be NULL) and the number of
+ * frames in *frames (the reference resumes at klok = frames * 10^6). */
+int tis_read_last_frame(const char *coordinates, int n, double *x, double *y, double *z, int64_t *frames);
 /* Energies of the tertiary stacks of the last step (the Contacts file, E:6290). */
 int tis_get_stack_energies(tis_handle *h, int replica, double *out, int64_t cap, int64_t *n);
 /* Step counter (klok), rebuild count and rand() draws consumed by one replica. */

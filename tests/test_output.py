@@ -1,0 +1,87 @@
+"""The reference's output files (Contacts / Coordinates / Energies, E:6276-6312),
+its restart read (E:6181-6211) and the tis_run command line."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from systems import golden_inputs, load
+from tis_gb300 import Engine, read_last_frame, TisError
+from tis_gb300 import build as _build
+
+
+def _write_frames(path, frames):
+    """Frames in the reference's Coordinates layout: x, y, z as 1-based arrays (n+1 doubles)."""
+    with open(path, "wb") as f:
+        for x, y, z in frames:
+            for a in (x, y, z):
+                np.concatenate([[0.0], a]).astype(np.float64).tofile(f)
+
+
+def test_read_last_frame(tmp_path):
+    n = 7
+    rng = np.random.default_rng(3)
+    frames = [tuple(rng.normal(size=n) for _ in range(3)) for _ in range(3)]
+    p = str(tmp_path / "coords.dat")
+    _write_frames(p, frames)
+    x, y, z, count = read_last_frame(p, n)
+    assert count == 3
+    assert np.array_equal(x, frames[-1][0]) and np.array_equal(y, frames[-1][1]) and np.array_equal(z, frames[-1][2])
+    with open(p, "ab") as f:
+        f.write(b"\0" * 16)
+    with pytest.raises(TisError) as err:
+        read_last_frame(p, n)
+    assert err.value.code == 3
+
+
+@pytest.mark.gpu
+def test_write_frame_matches_the_engine(tmp_path):
+    s = load(golden_inputs(), "small")
+    e = Engine([s])
+    e.populate_lists()
+    e.step(60)
+    e.sync()
+    paths = [str(tmp_path / k) for k in ("contacts.dat", "coordinates.dat", "energies.dat")]
+    for _ in range(2):
+        e.write_frame(0, *paths)
+    st = e.get_state(0)
+    en = e.energies(0)
+    stacks = e.stack_energies(0)
+    lines = open(paths[0]).read().splitlines()
+    assert len(lines) == 2
+    vals = lines[0].split()
+    assert len(vals) == len(stacks)
+    assert vals == [f"{v:+.3f}" for v in stacks]
+    x, y, z, count = read_last_frame(paths[1], e.n[0])
+    assert count == 2
+    assert np.array_equal(x, st["x"]) and np.array_equal(y, st["y"]) and np.array_equal(z, st["z"])
+    row = [float(v) for v in open(paths[2]).read().splitlines()[0].split()]
+    want = [en[0], en[1], en[2], float(np.sum(stacks)), en[4]]
+    np.testing.assert_allclose(row, want, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_cli_runs_writes_and_restarts(tmp_path):
+    _build.build()
+    g = golden_inputs()
+    for src, dst in [(g["pdb"], "16SCD.pdb"), (g["bonds"], "16SCD_16SCD_unprocessed_bonds.dat"),
+                     (g["stacks"], "16SCD_16SCD_unprocessed_stacks.dat"), (g["maxikey"], "MAXIKEY_Mg_Cl_K.dat")]:
+        shutil.copy(src, tmp_path / dst)
+    args = [_build.RUN, "-T0.59219", "-c0.005", "-f0.05", "-s3", "--box", "200", "--rc", "30", "--center", "100",
+            "--every", "50", "--snapshot-every", "100", "--replicas", "2"]
+    subprocess.run(args + ["--steps", "200"], cwd=tmp_path, check=True, capture_output=True, text=True, timeout=300)
+    tail = "D0.850_E3.975_d6.500_T0.592_cM0.0050_f0.050_s{}"
+    for seed in (3, 4):
+        base = tail.format(seed)
+        energies = (tmp_path / f"Energies_16SCD_EPS_Mg_Cl_K_{base}.dat").read_text().splitlines()
+        assert len(energies) == 4  # steps 50, 100, 150, 200
+        assert all(len(l.split()) == 5 for l in energies)
+        assert (tmp_path / f"Contacts_16SCD_EPS_Mg_Cl_K_{base}_2.dat").exists()  # snapshot at step 200
+        coords = tmp_path / f"Coordinates_16SCD_EPS_Mg_Cl_K_{base}.dat"
+        assert coords.stat().st_size % (3 * 8) == 0
+    subprocess.run(args + ["--steps", "400"], cwd=tmp_path, check=True, capture_output=True, text=True, timeout=300)
+    base = tail.format(3)
+    energies = (tmp_path / f"Energies_16SCD_EPS_Mg_Cl_K_{base}.dat").read_text().splitlines()
+    assert len(energies) == 8  # resumed at step 4 x 50 from the last frame, then frames at 250 .. 400
