@@ -849,6 +849,40 @@ static int grp_get_pairs(Group *h, int r, int which, int32_t *pairs, int64_t cap
     return TIS_OK;
 }
 
+static int grp_ion_counts(Group *h, int r, int kind, double radius, int32_t *counts, int64_t cap, int64_t *n_p,
+                          int32_t *total)
+{
+    int rc = valid_replica(h, r);
+    if (rc) return rc;
+    if (kind < 3 || kind > 5) return fail(TIS_ERR_ARG, "tis_ion_counts: ion kind %d is not 3 (Mg), 4 (Cl) or 5 (K)", kind);
+    if (!(radius > 0) || radius > h->prm.sr)
+        return fail(TIS_ERR_ARG, "tis_ion_counts: radius %g outside (0, %g] (the SR radius)", radius, h->prm.sr);
+    if (!h->lists_built && (rc = populate(h))) return rc;
+    const RepHost &hr = h->rep[r];
+    int *d_cnt = nullptr, *d_hit = nullptr;
+    TIS_CUDA(cudaMallocAsync((void **)&d_cnt, sizeof(int) * (hr.nrna + hr.n), h->stream));
+    d_hit = d_cnt + hr.nrna;
+    TIS_CUDA(cudaMemsetAsync(d_hit, 0, sizeof(int) * hr.n, h->stream));
+    tis::launch_ion_counts(h->dev, h->stream, r, hr.nrna, kind, radius * radius, d_cnt, d_hit);
+    std::vector<int> c(hr.nrna + hr.n);
+    TIS_CUDA(cudaMemcpyAsync(c.data(), d_cnt, sizeof(int) * c.size(), cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaFreeAsync(d_cnt, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    int64_t np = 0;
+    for (int i = 0; i < hr.nrna; ++i)
+        if (c[i] >= 0) {
+            if (counts && np < cap) counts[np] = c[i];
+            ++np;
+        }
+    if (n_p) *n_p = np;
+    if (total) {
+        int t = 0;
+        for (int j = 0; j < hr.n; ++j) t += c[hr.nrna + j];
+        *total = t;
+    }
+    return check_flags(h);
+}
+
 static int grp_get_hb_status(Group *h, int r, int32_t *status, int32_t *excess)
 {
     int rc = valid_replica(h, r);
@@ -1348,6 +1382,16 @@ int tis_get_pairs(tis_handle *h, int r, int which, int32_t *pairs, int64_t cap, 
     if (rc) return rc;
     TIS_CUDA(cudaStreamSynchronize(h->stream));
     return grp_get_pairs(g, loc, which, pairs, cap, n);
+}
+
+int tis_ion_counts(tis_handle *h, int r, int kind, double radius, int32_t *counts, int64_t cap, int64_t *n_p,
+                   int32_t *total)
+{
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return grp_ion_counts(g, loc, kind, radius, counts, cap, n_p, total);
 }
 
 int tis_get_hb_status(tis_handle *h, int r, int32_t *status, int32_t *excess)

@@ -1553,6 +1553,30 @@ __global__ void k_rg(Dev d, int r, double *out)
     if (threadIdx.x == 0) *out = sqrt(s[0] / R->nrna);
 }
 
+// Ions of one kind within sqrt(r2cut) of each phosphate of replica r, from the SR
+// lists (complete within the SR radius between rebuilds): count[i] for RNA bead i
+// (-1 for sugars and bases), hit[j] = 1 for every ion j within range of some P.
+__global__ void k_ion_counts(Dev d, int r, int kind, double r2cut, int *count, int *hit)
+{
+    const RepParams *R = d.rp + r;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R->nrna) return;
+    const int p = R->p0 + i;
+    if (((d.q[p].w >> 8) & 0xff) != 0) {
+        count[i] = -1;
+        return;
+    }
+    int c = 0;
+    for (int k = 0; k < d.n_sr[p]; ++k) {
+        const int j = d.nbr_sr[nb_idx(k, p, d.P)] & kIdxMask;
+        if (((d.q[j].w >> 8) & 0xff) == kind && exact_r2(d, R, p, j) <= r2cut) {
+            ++c;
+            hit[j - R->p0] = 1;
+        }
+    }
+    count[i] = c;
+}
+
 // E2_HB, E3_HB, E2_STACK, E3_STACK and Rg of every replica (one block each)
 __global__ void k_energies(Dev d, double *out)
 {
@@ -1604,6 +1628,11 @@ void launch_get_state(const Dev &d, cudaStream_t s, double *stage, int n, unsign
 }
 
 void launch_energies(const Dev &d, cudaStream_t s, double *out) { k_energies<<<d.R, 256, 0, s>>>(d, out); }
+
+void launch_ion_counts(const Dev &d, cudaStream_t s, int r, int nrna, int kind, double r2cut, int *count, int *hit)
+{
+    k_ion_counts<<<(nrna + 127) / 128, 128, 0, s>>>(d, r, kind, r2cut, count, hit);
+}
 
 void launch_pair_sr(const Dev &d, cudaStream_t s, bool en, bool ex)
 {

@@ -91,6 +91,9 @@ void launch_quantize(const Dev &d, cudaStream_t s);
 void launch_put_state(const Dev &d, cudaStream_t s, const double *stage, int n);
 void launch_get_state(const Dev &d, cudaStream_t s, double *stage, int n, unsigned mask);
 void launch_energies(const Dev &d, cudaStream_t s, double *out);  // 5 values per replica
+// per RNA bead of replica r: ions of `kind` within sqrt(r2cut) of it if it is a P (-1 otherwise);
+// hit[j] set for each such ion (replica-local index)
+void launch_ion_counts(const Dev &d, cudaStream_t s, int r, int nrna, int kind, double r2cut, int *count, int *hit);
 // excl_in_list: the hot path skips the LJ of bonded pairs in the SR kernel and
 // does not subtract it in the bonded kernel (the reference's net force, without
 // the cancellation of two large equal terms); false gives the reference's

@@ -78,6 +78,7 @@ def _declare(L):
         "tis_get_states": [vp] + [dp] * 9,
         "tis_get_all_energies": [vp, dp],
         "tis_write_frame": [vp, i32, cp, cp, cp],
+        "tis_ion_counts": [vp, i32, i32, C.c_double, ip, i64, C.POINTER(C.c_int64), ip],
         "tis_read_last_frame": [cp, i32, dp, dp, dp, C.POINTER(C.c_int64)],
         "tis_populate_lists": [vp],
         "tis_get_cells": [vp, i32, ip, ip],
@@ -114,7 +115,7 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_move_rigid_units", "tis_check_shifts", "tis_step", "tis_sync", "tis_get_energies",
             "tis_get_stack_energies", "tis_get_counters", "tis_get_info", "tis_replica_size", "tis_get_launch_count",
             "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc", "tis_set_states",
-            "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame"]
+            "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts"]
 
 
 def read_last_frame(path, n):
@@ -299,6 +300,15 @@ class Engine:
         """Appends replica r's frame to the reference's Contacts / Coordinates / Energies files."""
         enc = lambda p: p.encode() if p is not None else None
         _check(lib().tis_write_frame(self.h, r, enc(contacts), enc(coordinates), enc(energies)))
+
+    def ion_counts(self, r, kind, radius):
+        """(counts per phosphate, distinct ions bound): ions of `kind` (3 Mg, 4 Cl, 5 K)
+        within `radius` of each phosphate of replica r."""
+        n = C.c_int64()
+        tot = C.c_int32()
+        out = np.zeros(self.n[r], dtype=np.int32)
+        _check(lib().tis_ion_counts(self.h, r, kind, radius, _ip(out), out.size, C.byref(n), C.byref(tot)))
+        return out[: n.value], tot.value
 
     def populate_lists(self):
         _check(lib().tis_populate_lists(self.h))

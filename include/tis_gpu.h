@@ -202,6 +202,17 @@ int tis_get_energies(tis_handle *h, int replica, double *out5);
 /* The same five values for every replica: out[5 * replica + k]. */
 int tis_get_all_energies(tis_handle *h, double *out);
 
+/* Bound-ion counts on the device (the reference's analysis/mg_correlation/
+ * mg_bound.F90:94-116 and analysis/salt_nt/dcd_traj_SaltCount_Kinetics_PBC.py:
+ * 42-70, which read them back from trajectory files): for every phosphate of the
+ * replica, in bead order, the number of ions of `kind` (3 Mg, 4 Cl, 5 K, the
+ * reference's part_key) whose minimum-image FP64 distance is at most `radius`
+ * (at most the SR radius, e.g. 4.4, 5 or 7.2684 A); *n_p receives the number of
+ * phosphates (at most cap counts are written) and *total the number of distinct
+ * ions within range of some phosphate. */
+int tis_ion_counts(tis_handle *h, int replica, int kind, double radius, int32_t *counts, int64_t cap,
+                   int64_t *n_p, int32_t *total);
+
 /* Appends one frame of a replica to the reference's three output files (any may
  * be NULL): the Contacts file ("%+.3f " per tertiary stack energy, then a
  * newline, E:6290-6294), the Coordinates file (x, y, z, each as the reference's

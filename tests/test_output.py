@@ -85,3 +85,31 @@ def test_cli_runs_writes_and_restarts(tmp_path):
     base = tail.format(3)
     energies = (tmp_path / f"Energies_16SCD_EPS_Mg_Cl_K_{base}.dat").read_text().splitlines()
     assert len(energies) == 8  # resumed at step 4 x 50 from the last frame, then frames at 250 .. 400
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,radius", [(3, 4.4), (3, 7.2684), (5, 5.0), (5, 7.2684), (4, 7.2684)])
+def test_ion_counts_match_a_direct_count(kind, radius):
+    """Ions of one kind within a radius of each phosphate (the reference's bound-ion
+    analyses), counted on the device from the SR lists, equal a direct count over
+    all ions with the engine's image rule."""
+    s = load(golden_inputs(), "small")
+    e = Engine([s])
+    e.populate_lists()
+    e.step(150)
+    e.sync()
+    counts, total = e.ion_counts(0, kind, radius)
+    st = e.get_state(0)
+    sd = s.to_dict()
+    kinds = np.asarray(sd["kind"])
+    L = np.asarray(sd["box"], dtype=np.float64)
+    X = np.stack([st["x"], st["y"], st["z"]], 1)
+    P = np.nonzero(kinds == 0)[0]
+    ions = np.nonzero(kinds == kind)[0]
+    d = X[P][:, None, :] - X[ions][None, :, :]
+    d = np.where(d > 0.5 * L, d - L, d)
+    d = np.where(d < -0.5 * L, d + L, d)
+    r2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+    within = r2 <= radius * radius
+    assert np.array_equal(counts, within.sum(1))
+    assert total == int(within.any(0).sum())
