@@ -1242,7 +1242,7 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     if (prm.sr <= 0) prm.sr = 12.0;
     if (prm.skin <= 0) prm.skin = 3.0;
     if (prm.groups < 0) return fail(TIS_ERR_ARG, "tis_create: negative group count");
-    int G = prm.groups > 0 ? prm.groups : (n_replicas + 7) / 8;
+    int G = prm.groups > 0 ? prm.groups : (3 * n_replicas + 15) / 16;  // about 5 1/3 replicas per group
     G = std::min(G, n_replicas);
     prm.groups = G;
 

@@ -45,7 +45,7 @@ T_298 = 0.59219
 GEN_SEED = 2000
 METRIC = "aggregate Langevin steps/s, batched mixed-prec vs plain GPU, force rel-err <=1e-5"
 UNIT = "replica-steps/s"
-GRAPH_STEPS = 20
+GRAPH_STEPS = 100
 
 
 def replica_specs(n=N_REPLICAS):
@@ -158,13 +158,14 @@ def stage_bytes(n, sr, lr, lr_frac, nreb, nrna, items, nhb, nrep):
     }
 
 
-# DRAM bytes per launch of each step kernel for one group of 8 replicas (about 43k
-# particles), dram__bytes_read.sum + dram__bytes_write.sum of one launch (cold L2,
-# serialised) from ncu captures of `python bench.py --steps 40 --warmup 3 --no-extras`
-# with --clock-control none, --kernel-name-base mangled and -k set to the kernel
-# (None: no capture of a stepping launch).  Scaled to the batch by the number of groups.
-NCU_DRAM_BYTES_PER_GROUP = {"pair_sr": 3.04e6, "pair_lr": None, "bonded": 1.24e6, "hbond": 0.48e6,
-                            "shift": 0.04e6, "integrate": 5.35e6, "cells": 0.03e6, "search": None}
+# DRAM bytes per replica of each step kernel's launch: dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch over a group of 8 replicas (about 43k
+# particles; cold L2, serialised) divided by 8, from ncu captures of
+# `python bench.py --steps 40 --warmup 3 --no-extras --groups 8` with --clock-control
+# none, --kernel-name-base mangled and -k set to the kernel (None: no capture of a
+# stepping launch).  Scaled to the batch by the number of replicas.
+NCU_DRAM_BYTES_PER_REPLICA = {"pair_sr": 3.04e6 / 8, "pair_lr": None, "bonded": 1.24e6 / 8, "hbond": 0.48e6 / 8,
+                              "shift": 0.04e6 / 8, "integrate": 5.35e6 / 8, "cells": 0.03e6 / 8, "search": None}
 
 
 def cpu_sample(files, specs, steps, workers):
@@ -329,17 +330,16 @@ def gpu_arm(args):
         items = (len(sd["bt_kind"]) + len(sd["st3_E"]) + len(sd["st2_E"])) * N_REPLICAS
         nhb = len(sd["hb_E"]) * N_REPLICAS
         alg = stage_bytes(n_part, sr, lr, 0.1 + reb_rep / N_REPLICAS, nreb, nrna, items, nhb, N_REPLICAS)
-        groups = eng.params.groups or (N_REPLICAS + 7) // 8
         per_stage = {}
         for k, ms_k in stages.items():
             gbs = alg[k] / (ms_k * 1e-3) / 1e9 if ms_k > 0 else None
             per_stage[k] = {"ms": ms_k, "alg_bytes": alg[k], "achieved_gbs": gbs,
                             "frac": gbs / peak if gbs is not None else None}
         dom = max(stages, key=stages.get)
-        traffic = NCU_DRAM_BYTES_PER_GROUP.get(dom)
+        traffic = NCU_DRAM_BYTES_PER_REPLICA.get(dom)
         roofline = {"bound": "hbm", "kernel": dom, "achieved": per_stage[dom]["achieved_gbs"], "peak": peak,
                     "unit": "GB/s", "frac": per_stage[dom]["frac"],
-                    "traffic": traffic * groups if traffic is not None else None,
+                    "traffic": traffic * N_REPLICAS if traffic is not None else None,
                     "alg_bytes_per_launch": alg[dom], "peak_source": peak_kind,
                     "mean_neighbours": {"sr": sr, "lr": lr}, "stages": per_stage,
                     "note": "stage = its kernels over all replica groups run alone; launch = one step of "
@@ -373,7 +373,7 @@ def gpu_arm(args):
             "config": {"workload": "64 replicas x 346-nt TIS chain (1037 beads) + Mg 0-20 mM sweep, 76 mM KCl, "
                                    "350 A box, T 298 K, rc 30 A",
                        "replicas_per_gpu": N_REPLICAS, "particles_per_gpu": n_part, "precision": "mixed",
-                       "graph_steps": GRAPH_STEPS, "replica_groups": eng.params.groups or (N_REPLICAS + 7) // 8,
+                       "graph_steps": GRAPH_STEPS, "replica_groups": eng.params.groups or (3 * N_REPLICAS + 15) // 16,
                        "l2": "flushed (256 MB write) between timed iterations of "
                                                          f"{GRAPH_STEPS} steps", "parallelism": f"replicas x{world}"},
             "plain_fp64_single_replica_steps_per_s": plain_sps,

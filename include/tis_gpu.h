@@ -120,7 +120,7 @@ typedef struct tis_run_params {
                               LJ range plus the skin, the only pairs that can exert a force before
                               the next rebuild */
     int32_t groups;        /* replica groups whose step graphs run concurrently on the GPU
-                              (0: one group per 8 replicas); results do not depend on it */
+                              (0: (3 n + 15) / 16 for n replicas, 12 for 64); results do not depend on it */
     int32_t reserved[4];
 } tis_run_params;
 
