@@ -112,11 +112,16 @@ struct Group {
     int npk = 0;              // particles of the group's replicas (unpadded)
     double *stage = nullptr;  // nine packed state arrays of npk values (tis_set_states / tis_get_states)
     double *d_e5 = nullptr;   // five energies per replica (tis_get_all_energies)
+    tis::RepState *h_rs = nullptr;  // pinned host copy of the replicas' state (list build checks)
+    int *h_peaks = nullptr;         // pinned: largest SR and LR neighbour counts of the last list build
+    int *d_peaks = nullptr;
 
     ~Group()
     {
         if (graph) cudaGraphExecDestroy(graph);
         for (void *p : owned) cudaFree(p);
+        if (h_rs) cudaFreeHost(h_rs);
+        if (h_peaks) cudaFreeHost(h_peaks);
         for (int k = 0; k < 3; ++k) {
             if (side[k]) cudaStreamDestroy(side[k]);
             if (join[k]) cudaEventDestroy(join[k]);
@@ -190,47 +195,63 @@ int uncount_rebuilds(Group *h, int n)
     return TIS_OK;
 }
 
-// largest SR and LR neighbour counts of the lists just built
-int list_peaks(Group *h, int *max_sr, int *max_lr)
+// populate_lists for the group, in two halves around a stream synchronisation so
+// that several groups' builds can run at once: the launch (flags cleared, every
+// replica rebuilt, the largest neighbour counts reduced, flags and counts copied to
+// pinned host memory) and the check.  The lists grow until they hold twice the
+// largest neighbour count found, so that later rebuilds (ions gathering at the
+// RNA, the chain compacting) have room; a step that still overflows reports
+// TIS_ERR_CAPACITY.
+int populate_launch(Group *h)
 {
-    std::vector<int> a(h->P), b(h->P);
-    TIS_CUDA(cudaMemcpyAsync(a.data(), h->dev.n_sr, sizeof(int) * h->P, cudaMemcpyDeviceToHost, h->stream));
-    TIS_CUDA(cudaMemcpyAsync(b.data(), h->dev.n_lr, sizeof(int) * h->P, cudaMemcpyDeviceToHost, h->stream));
-    TIS_CUDA(cudaStreamSynchronize(h->stream));
-    *max_sr = *std::max_element(a.begin(), a.end());
-    *max_lr = *std::max_element(b.begin(), b.end());
+    tis::launch_clear_err(h->dev, h->stream);
+    tis::launch_force_all_rebuild(h->dev, h->stream);
+    tis::launch_rebuild(h->dev, h->stream);
+    TIS_CUDA(cudaMemsetAsync(h->d_peaks, 0, 2 * sizeof(int), h->stream));
+    tis::launch_list_peaks(h->dev, h->stream, h->d_peaks);
+    TIS_CUDA(cudaGetLastError());
+    TIS_CUDA(cudaMemcpyAsync(h->h_rs, h->dev.rs, sizeof(tis::RepState) * h->R, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaMemcpyAsync(h->h_peaks, h->d_peaks, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     return TIS_OK;
 }
 
-// populate_lists for the group.  The lists grow until they hold twice the largest
-// neighbour count found, so that later rebuilds (ions gathering at the RNA, the
-// chain compacting) have room; a step that still overflows reports TIS_ERR_CAPACITY.
+// after the group's stream is synchronised: *again when the lists must grow and be
+// built once more
+int populate_check(Group *h, int attempt, bool *again)
+{
+    *again = false;
+    bool overflow = false;
+    for (int r = 0; r < h->R; ++r) {
+        const int e = h->h_rs[r].err;
+        if (e & tis::kErrRange) return fail(TIS_ERR_RANGE, "replica %d: a particle left the cell grid's range", h->base + r);
+        if (e & tis::kErrNonFinite) return fail(TIS_ERR_NONFINITE, "replica %d: non-finite or runaway force/state", h->base + r);
+        overflow = overflow || (e & tis::kErrCapacity);
+    }
+    const int want_sr = std::max(h->dev.cap_sr, round_up(2 * h->h_peaks[0], 32));
+    const int want_lr = std::max(h->dev.cap_lr, round_up(2 * h->h_peaks[1], 32));
+    if (!overflow && want_sr == h->dev.cap_sr && want_lr == h->dev.cap_lr) {
+        h->lists_built = true;
+        // the builds discarded for capacity do not count as list rebuilds
+        return attempt ? uncount_rebuilds(h, attempt) : TIS_OK;
+    }
+    if (attempt >= 7) return fail(TIS_ERR_CAPACITY, "neighbour lists keep overflowing");
+    // an overflowing list reports its capacity as its count: grow by half at least
+    const int rc = grow_lists(h, overflow ? std::max(want_sr, round_up(h->dev.cap_sr * 3 / 2, 32)) : want_sr,
+                              overflow ? std::max(want_lr, round_up(h->dev.cap_lr * 3 / 2, 32)) : want_lr);
+    if (rc) return rc;
+    *again = true;
+    return TIS_OK;
+}
+
 int populate(Group *h)
 {
-    for (int attempt = 0; attempt < 8; ++attempt) {
-        int rc = clear_flags(h);
+    for (int attempt = 0;; ++attempt) {
+        int rc = populate_launch(h);
         if (rc) return rc;
-        tis::launch_force_all_rebuild(h->dev, h->stream);
-        tis::launch_rebuild(h->dev, h->stream);
-        TIS_CUDA(cudaGetLastError());
-        rc = check_flags(h);
-        if (rc != TIS_OK && rc != TIS_ERR_CAPACITY) return rc;
-        int msr = 0, mlr = 0;
-        const int rp = list_peaks(h, &msr, &mlr);
-        if (rp) return rp;
-        const int want_sr = std::max(h->dev.cap_sr, round_up(2 * msr, 32));
-        const int want_lr = std::max(h->dev.cap_lr, round_up(2 * mlr, 32));
-        if (rc == TIS_OK && want_sr == h->dev.cap_sr && want_lr == h->dev.cap_lr) {
-            h->lists_built = true;
-            // the builds discarded for capacity do not count as list rebuilds
-            return attempt ? uncount_rebuilds(h, attempt) : TIS_OK;
-        }
-        // an overflowing list reports its capacity as its count: grow by half at least
-        rc = grow_lists(h, rc ? std::max(want_sr, round_up(h->dev.cap_sr * 3 / 2, 32)) : want_sr,
-                        rc ? std::max(want_lr, round_up(h->dev.cap_lr * 3 / 2, 32)) : want_lr);
-        if (rc) return rc;
+        TIS_CUDA(cudaStreamSynchronize(h->stream));
+        bool again = false;
+        if ((rc = populate_check(h, attempt, &again)) || !again) return rc;
     }
-    return fail(TIS_ERR_CAPACITY, "neighbour lists keep overflowing");
 }
 
 // deterministic_forces_MPI (E:2524-2586): the four force kernels are independent
@@ -629,7 +650,7 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         (rc = dalloc(O, &d.nbr_sr, (size_t)cap_sr * h->P)) || (rc = dalloc(O, &d.nbr_lr, (size_t)cap_lr * h->P)) ||
         (rc = dalloc(O, &d.eterm, (size_t)h->R * tis::kNE)) || (rc = dalloc(O, &d.shift, (size_t)h->R * 3)) || 
         (rc = dalloc(O, &h->d_scalar, 4)) || (rc = dalloc(O, &h->stage, 9 * (size_t)h->npk)) ||
-        (rc = dalloc(O, &h->d_e5, 5 * (size_t)h->R)))
+        (rc = dalloc(O, &h->d_e5, 5 * (size_t)h->R)) || (rc = dalloc(O, &h->d_peaks, 2)))
         return bail(rc);
     int4 *d_bti = nullptr;
     double2 *d_btp = nullptr;
@@ -718,6 +739,9 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         d.hb_smem = smem <= 160 * 1024 ? (int)smem : 0;
     }
     if (tis::configure_kernels(d) != 0) return bail(fail(TIS_ERR_CUDA, "cudaFuncSetAttribute failed"));
+    if (cudaMallocHost((void **)&h->h_rs, sizeof(tis::RepState) * h->R) != cudaSuccess ||
+        cudaMallocHost((void **)&h->h_peaks, 2 * sizeof(int)) != cudaSuccess)
+        return bail(fail(TIS_ERR_NOMEM, "cudaMallocHost failed"));
     tis::launch_quantize(h->dev, h->stream);
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess)
         return bail(fail(TIS_ERR_CUDA, "quantisation kernel failed"));
@@ -801,11 +825,6 @@ static int grp_get_all_energies(Group *h, double *out)
     return TIS_OK;
 }
 
-static int grp_populate_lists(Group *h)
-{
-    if (!h) return fail(TIS_ERR_ARG, "null handle");
-    return populate(h);
-}
 
 static int grp_get_cells(Group *h, int r, int32_t *cell, int32_t *dims)
 {
@@ -1363,7 +1382,24 @@ int tis_get_all_energies(tis_handle *h, double *out)
 
 int tis_populate_lists(tis_handle *h)
 {
-    return each_group(h, [](Group *g) { return grp_populate_lists(g); });
+    // every group's build is launched before any is checked, so the builds overlap
+    if (!h) return fail(TIS_ERR_ARG, "null handle");
+    int rc = fork_groups(h);
+    if (rc) return rc;
+    std::vector<Group *> pending(h->groups);
+    for (int attempt = 0; !pending.empty(); ++attempt) {
+        for (Group *g : pending)
+            if ((rc = populate_launch(g))) return rc;
+        std::vector<Group *> again_list;
+        for (Group *g : pending) {
+            TIS_CUDA(cudaStreamSynchronize(g->stream));
+            bool again = false;
+            if ((rc = populate_check(g, attempt, &again))) return rc;
+            if (again) again_list.push_back(g);
+        }
+        pending.swap(again_list);
+    }
+    return join_groups(h);
 }
 
 int tis_get_cells(tis_handle *h, int r, int32_t *cell, int32_t *dims)

@@ -1577,6 +1577,30 @@ __global__ void k_ion_counts(Dev d, int r, int kind, double r2cut, int *count, i
     count[i] = c;
 }
 
+// clears every replica's device-side error flags
+__global__ void k_clear_err(Dev d)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < d.R; r += gridDim.x * blockDim.x) d.rs[r].err = 0;
+}
+
+// the largest SR and LR neighbour counts of the group (out[0], out[1]; zero on entry)
+__global__ void k_list_peaks(Dev d, int *out)
+{
+    int a = 0, b = 0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < d.P; p += gridDim.x * blockDim.x) {
+        a = max(a, d.n_sr[p]);
+        b = max(b, d.n_lr[p]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a = max(a, __shfl_down_sync(kFull, a, o));
+        b = max(b, __shfl_down_sync(kFull, b, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, a);
+        atomicMax(out + 1, b);
+    }
+}
+
 // E2_HB, E3_HB, E2_STACK, E3_STACK and Rg of every replica (one block each)
 __global__ void k_energies(Dev d, double *out)
 {
@@ -1628,6 +1652,10 @@ void launch_get_state(const Dev &d, cudaStream_t s, double *stage, int n, unsign
 }
 
 void launch_energies(const Dev &d, cudaStream_t s, double *out) { k_energies<<<d.R, 256, 0, s>>>(d, out); }
+
+void launch_clear_err(const Dev &d, cudaStream_t s) { k_clear_err<<<1, 256, 0, s>>>(d); }
+
+void launch_list_peaks(const Dev &d, cudaStream_t s, int *out) { k_list_peaks<<<d.sm_count, 256, 0, s>>>(d, out); }
 
 void launch_ion_counts(const Dev &d, cudaStream_t s, int r, int nrna, int kind, double r2cut, int *count, int *hit)
 {

@@ -91,6 +91,8 @@ void launch_quantize(const Dev &d, cudaStream_t s);
 void launch_put_state(const Dev &d, cudaStream_t s, const double *stage, int n);
 void launch_get_state(const Dev &d, cudaStream_t s, double *stage, int n, unsigned mask);
 void launch_energies(const Dev &d, cudaStream_t s, double *out);  // 5 values per replica
+void launch_clear_err(const Dev &d, cudaStream_t s);              // RepState::err = 0 for every replica
+void launch_list_peaks(const Dev &d, cudaStream_t s, int *out);   // max n_sr, max n_lr (out zeroed first)
 // per RNA bead of replica r: ions of `kind` within sqrt(r2cut) of it if it is a P (-1 otherwise);
 // hit[j] set for each such ion (replica-local index)
 void launch_ion_counts(const Dev &d, cudaStream_t s, int r, int nrna, int kind, double r2cut, int *count, int *hit);
