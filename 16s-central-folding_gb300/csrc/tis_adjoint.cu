@@ -1,0 +1,620 @@
+// Adjoint kernels of the TIS step (no counterpart in the reference, which has no
+// derivatives): dU/dtheta of the potential at a state, and the reverse pass of one
+// step of the fused Langevin update.
+//
+// The forces' Jacobian enters the reverse pass as J^T lambda.  Every force term is
+// the exact negative gradient of its energy (LJ_FORCE of WCA_ENERGY, E:749-821;
+// COULOMB_TRUNCATED_FORCE of its energy, E:825-855; the bonded, stacking and
+// H-bond forces of their restraint energies, E:924-1454), so J is symmetric and
+// J^T lambda = J lambda, the directional derivative of the force along lambda.
+// It is evaluated by forward-mode differentiation: the force code of each term is
+// written once more here over dual numbers (value, derivative along lambda), in
+// FP64, with the discrete choices (cutoffs, Monte Carlo outcome, stack switching,
+// dihedral imaging branch) taken from the values as the forward pass takes them.
+//
+// Parameter derivatives use that every parameter but the ion radii enters its
+// terms as a factor (E_LJ = sqrt(ELJ_i ELJ_j); Q_C lB; st_E; hb_E), so
+// lambda . dF/dtheta is lambda . F_term / theta times the factor's derivative;
+// a radius moves the LJ contact distance D = R_i + R_j (dF/dD in closed form) and
+// the ion's friction (K1, K2, sigma of E:2897-2903).
+#include <cstdio>
+
+#include "tis_kernels.cuh"
+
+namespace tis {
+namespace {
+
+constexpr unsigned kFullMask = 0xffffffffu;
+constexpr int kNP = kNParams;
+
+// ---------------------------------------------------------------------------
+// dual numbers: value and derivative along the tangent direction
+// ---------------------------------------------------------------------------
+struct Dual {
+    double v, d;
+};
+__device__ inline Dual cst(double v) { return {v, 0.0}; }
+__device__ inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+__device__ inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
+__device__ inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+__device__ inline Dual operator/(Dual a, Dual b)
+{
+    const double q = a.v / b.v;
+    return {q, (a.d - q * b.d) / b.v};
+}
+__device__ inline Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
+__device__ inline Dual operator+(double a, Dual b) { return {a + b.v, b.d}; }
+__device__ inline Dual operator-(Dual a, double b) { return {a.v - b, a.d}; }
+__device__ inline Dual operator-(double a, Dual b) { return {a - b.v, -b.d}; }
+__device__ inline Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
+__device__ inline Dual operator/(double a, Dual b)
+{
+    const double q = a / b.v;
+    return {q, -q * b.d / b.v};
+}
+__device__ inline Dual dsqrt(Dual a)
+{
+    const double s = sqrt(a.v);
+    return {s, s > 0.0 ? 0.5 * a.d / s : 0.0};
+}
+__device__ inline Dual dexp(Dual a)
+{
+    const double e = exp(a.v);
+    return {e, e * a.d};
+}
+__device__ inline Dual datan2(Dual y, Dual x)
+{
+    const double n = x.v * x.v + y.v * y.v;
+    return {atan2(y.v, x.v), n > 0.0 ? (x.v * y.d - y.v * x.d) / n : 0.0};
+}
+
+using DV = V3<Dual>;
+
+// positions (FP64 arrays) with the tangent (3P, component-major) as derivative
+struct APos {
+    const double *x, *y, *z, *t;
+    int P;
+    __device__ DV at(int i) const
+    {
+        if (!t) return {cst(x[i]), cst(y[i]), cst(z[i])};
+        return {{x[i], t[i]}, {y[i], t[P + i]}, {z[i], t[2 * P + i]}};
+    }
+    // position(b) - position(a), raw difference (the bonded terms' convention)
+    __device__ DV vec(int a, int b) const { return at(b) - at(a); }
+};
+
+// Force contributions of one term evaluated at unit strength: the derivative
+// part, times the term's strength, goes to jv; lambda . value is summed in w
+// (lambda = the tangent direction).
+struct AAcc {
+    double *jv;
+    const double *lam;
+    int P;
+    double scale;
+    double w;
+    __device__ void add(int i, DV g)
+    {
+        if (jv) {
+            atomicAdd(jv + i, scale * g.x.d);
+            atomicAdd(jv + P + i, scale * g.y.d);
+            atomicAdd(jv + 2 * P + i, scale * g.z.d);
+        }
+        if (lam) w += lam[i] * g.x.v + lam[P + i] * g.y.v + lam[2 * P + i] * g.z.v;
+    }
+};
+
+__device__ inline DV neg(DV a) { return {-a.x, -a.y, -a.z}; }
+
+// ---------------------------------------------------------------------------
+// the restraint terms (E:924-1454) over dual numbers
+// ---------------------------------------------------------------------------
+__device__ Dual angle_of(const APos &P, int i1, int i2, int i3)
+{
+    const DV a = P.vec(i2, i1), b = P.vec(i2, i3);
+    const DV w = cross(a, b);
+    return datan2(dsqrt(dot(w, w)), dot(a, b));
+}
+
+__device__ Dual dihedral_of(const APos &P, int i1, int i2, int i3, int i4)
+{
+    const DV v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
+    const DV m = cross(v1, v2), n = cross(v2, v3);
+    return datan2(dot(v1, n) * dsqrt(dot(v2, v2)), dot(m, n));
+}
+
+// force of V = k0 (r0 - r)^2 on i1, i2
+__device__ void bond_force(const APos &P, AAcc &A, int i1, int i2, Dual k0, double r0)
+{
+    const DV v = P.vec(i1, i2);
+    const Dual r = dsqrt(dot(v, v));
+    const Dual t = 2.0 * k0 * (r0 - r) / r;
+    const DV g = t * v;
+    A.add(i1, neg(g));
+    A.add(i2, g);
+}
+
+// force of V = k0 (th0 - theta)^2 at i2; clamp: none once cos theta < -0.99995 (E:1138-1251)
+__device__ void angle_force(const APos &P, AAcc &A, int i1, int i2, int i3, Dual k0, double th0, bool clamp)
+{
+    const DV a = P.vec(i2, i1), b = P.vec(i2, i3);
+    const Dual aa = dot(a, a), bb = dot(b, b), ab = dot(a, b);
+    if (clamp && ab.v / sqrt(aa.v * bb.v) < -0.99995) return;
+    const DV w = cross(a, b);
+    const Dual ww = dsqrt(dot(w, w));
+    if (ww.v == 0.0) return;
+    const Dual th = datan2(ww, ab);
+    const Dual s = 2.0 * k0 * (th0 - th) / ww;
+    const DV g1 = (s / aa) * cross(a, w);
+    const DV g3 = (-s / bb) * cross(b, w);
+    A.add(i1, g1);
+    A.add(i2, neg(g1 + g3));
+    A.add(i3, g3);
+}
+
+// force of V = k0 (psi0 - psi)^2 of the dihedral i1-i2-i3-i4 (E:1306-1454)
+__device__ void dihedral_force(const APos &P, AAcc &A, int i1, int i2, int i3, int i4, Dual k0, double psi0)
+{
+    const DV v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
+    const DV m = cross(v1, v2), n = cross(v2, v3);
+    const Dual mm = dot(m, m), nn = dot(n, n), v22 = dot(v2, v2);
+    if (mm.v == 0.0 || nn.v == 0.0) return;
+    const Dual l2 = dsqrt(v22);
+    const Dual psi = datan2(dot(v1, n) * l2, dot(m, n));
+    const Dual c = 2.0 * k0 * (psi0 - psi);
+    const DV g1 = (-c * l2 / mm) * m;
+    const DV g4 = (c * l2 / nn) * n;
+    const Dual p = dot(v1, v2) / v22, q = dot(v3, v2) / v22;
+    const DV g2 = (-1.0 - p) * g1 + q * g4;
+    A.add(i1, g1);
+    A.add(i2, g2);
+    A.add(i3, neg(g1 + g2 + g4));
+    A.add(i4, g4);
+}
+
+// native dihedral imaged to within pi of the current one (E:1999-2019)
+__device__ inline int branch_of(double psi, double nat)
+{
+    const double pi = 3.14159265358979323846;
+    if (fabs(psi - nat) <= pi) return 0;
+    return (psi - nat > pi) ? 1 : -1;
+}
+__device__ inline double shifted(double nat, int br) { return nat + 2.0 * 3.14159265358979323846 * br; }
+
+// the six-term native-geometry restraint sum q (E:1983-2056, E:2177-2231)
+__device__ Dual six_q(const APos &P, const int *k, const double *nat, Dual rdev, double init, int br[3])
+{
+    const Dual t1 = angle_of(P, k[0], k[1], k[4]);
+    const Dual t2 = angle_of(P, k[3], k[4], k[1]);
+    const Dual p0 = dihedral_of(P, k[0], k[1], k[4], k[3]);
+    const Dual p1 = dihedral_of(P, k[4], k[1], k[0], k[2]);
+    const Dual p2 = dihedral_of(P, k[1], k[4], k[3], k[5]);
+    br[0] = branch_of(p0.v, nat[3]);
+    br[1] = branch_of(p1.v, nat[4]);
+    br[2] = branch_of(p2.v, nat[5]);
+    const Dual d0 = p0 - shifted(nat[3], br[0]), d1 = p1 - shifted(nat[4], br[1]), d2 = p2 - shifted(nat[5], br[2]);
+    Dual q = init + 5.0 * rdev * rdev;
+    q = q + 1.5 * (t1 - nat[1]) * (t1 - nat[1]);
+    q = q + 1.5 * (t2 - nat[2]) * (t2 - nat[2]);
+    q = q + 0.15 * d0 * d0 + 0.15 * d1 * d1 + 0.15 * d2 * d2;
+    return q;
+}
+
+// force of V = w q for the six-term restraint
+__device__ void six_force(const APos &P, AAcc &A, const int *k, const double *nat, const int br[3], Dual w)
+{
+    bond_force(P, A, k[1], k[4], 5.0 * w, nat[0]);
+    angle_force(P, A, k[0], k[1], k[4], 1.5 * w, nat[1], true);
+    angle_force(P, A, k[3], k[4], k[1], 1.5 * w, nat[2], true);
+    dihedral_force(P, A, k[0], k[1], k[4], k[3], 0.15 * w, shifted(nat[3], br[0]));
+    dihedral_force(P, A, k[4], k[1], k[0], k[2], 0.15 * w, shifted(nat[4], br[1]));
+    dihedral_force(P, A, k[1], k[4], k[3], k[5], 0.15 * w, shifted(nat[5], br[2]));
+}
+
+__device__ inline Dual distance(const APos &P, int a, int b)
+{
+    const DV v = P.vec(a, b);
+    return dsqrt(dot(v, v));
+}
+
+// ---------------------------------------------------------------------------
+// parameter bookkeeping
+// ---------------------------------------------------------------------------
+// LJ epsilon class of a particle type (MAXIKEY order: 1 P, 2 S, 3-6 bases, 7 Mg, 8 Cl, 9 K)
+__device__ inline int eps_param(int t)
+{
+    if (t == 1) return 6;
+    if (t == 2) return 7;
+    if (t <= 6) return 8;
+    if (t == 7) return 9;
+    if (t == 8) return 10;
+    return 11;
+}
+__device__ inline int radius_param(int t) { return t == 7 ? 12 : t == 9 ? 13 : -1; }
+
+// sum of NV doubles over a block of blockDim.x threads (multiple of 32) into thread 0
+template <int NV>
+__device__ void block_reduce(double (&v)[NV], double *smem /* NV * 32 */)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(kFullMask, v[k], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) smem[k * 32 + warp] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            v[k] = lane < nw ? smem[k * 32 + lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(kFullMask, v[k], o);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pair terms over the neighbour lists (SR_interactions_lists, LR_interactions_lists)
+// ---------------------------------------------------------------------------
+// One thread per particle over its full list (every pair appears in both
+// partners' lists).  mode 0: dU/dtheta (each pair half from each side); mode 1:
+// jv[p] += (J tan)_p and the parameter terms of lambda = tan.  The LR kernel in
+// mode 1 runs only for replicas whose LR force was refreshed in the step.
+template <bool LR>
+__global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const double *tan, int mode)
+{
+    __shared__ double s_red[9 * 32];
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int r = d.blk_rep[blockIdx.x];
+    const RepParams *R = d.rp + r;
+    if (LR && mode == 1 && !a.rlr[r]) return;  // block-uniform
+    const int P = d.P;
+    const int4 qp = d.q[p];
+    const int tp = qp.w & 0xff, kp = (qp.w >> 8) & 0xff, act = (qp.w >> 16) & 1;
+    const bool chp = kp != 1 && kp != 2;
+    double g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // parameters 6 .. 14
+    double jx = 0, jy = 0, jz = 0;
+    if (act) {
+        const int cnt = LR ? d.n_lr[p] : d.n_sr[p];
+        const int *nbr = LR ? d.nbr_lr : d.nbr_sr;
+        const double lx = tan ? tan[p] : 0.0, ly = tan ? tan[P + p] : 0.0, lz = tan ? tan[2 * P + p] : 0.0;
+        const double eps_p = R->elj_d[jn12(tp, tp)];
+        for (int k = 0; k < cnt; ++k) {
+            const int raw = nbr[nb_idx(k, p, P)];
+            const int j = raw & kIdxMask;
+            const double ljw = LR ? 0.0 : (double)(1 - (raw >> kExclShift));
+            const int4 qj = d.q[j];
+            const int tj = qj.w & 0xff, kj = (qj.w >> 8) & 0xff;
+            const int J = jn12(tp, tj);
+            double v[3] = {a.px[p] - a.px[j], a.py[p] - a.py[j], a.pz[p] - a.pz[j]};
+            for (int c = 0; c < 3; ++c) {
+                if (v[c] > R->hbox[c]) v[c] -= R->box[c];
+                if (v[c] < -R->hbox[c]) v[c] += R->box[c];
+            }
+            const double r2e = __dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2]));
+            const bool lj = !LR && ljw != 0.0 && r2e <= R->dlj2_d[J];
+            const bool cou = (LR || (chp && kj != 1 && kj != 2)) && r2e <= R->rc2;
+            if (!lj && !cou) continue;
+            const DV dv = {{v[0], tan ? lx - tan[j] : 0.0}, {v[1], tan ? ly - tan[P + j] : 0.0},
+                           {v[2], tan ? lz - tan[2 * P + j] : 0.0}};
+            const Dual r2 = dot(dv, dv);
+            const Dual rr = dsqrt(r2);
+            Dual F = cst(0.0);
+            const double wl = lx * v[0] + ly * v[1] + lz * v[2];  // lambda_p . (x_p - x_j)
+            if (lj) {
+                const Dual dr = rr + (kSig0 - R->dlj_d[J]);
+                const Dual s = kSig0 / dr;
+                const Dual s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+                const double c0 = ljw * R->flj_d[J];
+                const Dual phi = c0 * (s14 - s8) * dr / rr;
+                F = F + phi;
+                const double eps_j = R->elj_d[jn12(tj, tj)];
+                const bool radius = !(tp <= 6 && tj <= 6);
+                if (mode == 0) {
+                    const double s6 = s4.v * s2.v, s12 = s6 * s6;
+                    const double u = ljw * R->elj_d[J] * (s12 - 2.0 * s6 + 1.0);
+                    if (eps_p > 0.0) g[eps_param(tp) - 6] += 0.25 * u / eps_p;
+                    if (eps_j > 0.0) g[eps_param(tj) - 6] += 0.25 * u / eps_j;
+                    if (radius) {
+                        const double dud = 0.5 * ljw * 12.0 * R->elj_d[J] * (s12 - s6) / dr.v;
+                        const int ip = radius_param(tp), ij = radius_param(tj);
+                        if (ip >= 0) g[ip - 6] += dud;
+                        if (ij >= 0) g[ij - 6] += dud;
+                    }
+                } else {
+                    if (eps_p > 0.0) g[eps_param(tp) - 6] += wl * phi.v / (2.0 * eps_p);
+                    if (eps_j > 0.0) g[eps_param(tj) - 6] += wl * phi.v / (2.0 * eps_j);
+                    if (radius) {
+                        const double dphi = c0 * (13.0 * s14.v - 7.0 * s8.v) / rr.v;
+                        const int ip = radius_param(tp), ij = radius_param(tj);
+                        if (ip >= 0) g[ip - 6] += wl * dphi;
+                        if (ij >= 0) g[ij - 6] += wl * dphi;
+                    }
+                }
+            }
+            if (cou) {
+                const Dual psi = R->qclb_d[J] / (rr * r2);
+                F = F + psi;
+                if (R->lB != 0.0) {
+                    if (mode == 0) g[8] += 0.5 * R->qclb_d[J] / rr.v / R->lB;
+                    else g[8] += wl * psi.v / R->lB;
+                }
+            }
+            if (mode == 1) {  // d/dtan of F (x_p - x_j)
+                jx += F.d * v[0] + F.v * dv.x.d;
+                jy += F.d * v[1] + F.v * dv.y.d;
+                jz += F.d * v[2] + F.v * dv.z.d;
+            }
+        }
+        if (mode == 1) {
+            a.jv[p] += jx;
+            a.jv[P + p] += jy;
+            a.jv[2 * P + p] += jz;
+        }
+    }
+    block_reduce<9>(g, s_red);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 9; ++k)
+            if (g[k] != 0.0) atomicAdd(a.dth + r * kNP + 6 + k, g[k]);
+}
+
+// ---------------------------------------------------------------------------
+// bonded terms, stacks and formed H-bonds, one thread per term
+// ---------------------------------------------------------------------------
+constexpr int kAdjTopoThreads = 256;
+
+__global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, const double *tan, int mode)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int kind, item;
+    if (t < d.nbt) { kind = 0; item = t; }
+    else if (t < d.nbt + d.nst3) { kind = 1; item = t - d.nbt; }
+    else if (t < d.nbt + d.nst3 + d.nst2) { kind = 2; item = t - d.nbt - d.nst3; }
+    else if (t < d.nbt + d.nst3 + d.nst2 + a.nhb) { kind = 3; item = t - d.nbt - d.nst3 - d.nst2; }
+    else return;
+    if (kind == 0 && mode == 0) return;  // no parameter of this set enters the bonded terms
+    if (kind == 3 && !a.rhb[item]) return;
+    const APos P{a.px, a.py, a.pz, mode == 1 ? tan : nullptr, d.P};
+    AAcc A{mode == 1 ? a.jv : nullptr, mode == 1 ? tan : nullptr, d.P, 1.0, 0.0};
+    int r = 0, param = -1;
+    double dE = 0.0, u1 = 0.0;
+    if (kind == 0) {
+        const int4 id = d.bt_idx[item];
+        const double2 par = d.bt_par[item];
+        if (id.w == 0) bond_force(P, A, id.x, id.y, cst(par.x), par.y);
+        else angle_force(P, A, id.x, id.y, id.z, cst(par.x), par.y, false);
+        return;
+    } else if (kind == 1) {  // tertiary: U = st_E / (1 + q), st_E = -st_D
+        const int *id = d.st3_idx + 6 * item;
+        const double *nat = d.st3_nat + 6 * item;
+        r = d.rep_of[id[0]];
+        int br[3];
+        const Dual rdev = distance(P, id[1], id[4]) - nat[0];
+        const Dual Dn = six_q(P, id, nat, rdev, 1.0, br);
+        u1 = 1.0 / Dn.v;
+        param = 4;
+        dE = -1.0;
+        if (mode == 1) {
+            A.scale = d.st3_E[item];
+            six_force(P, A, id, nat, br, -1.0 / (Dn * Dn));
+        }
+    } else if (kind == 2) {  // secondary: U = st_E / (1 + 1.4 dr^2 + 4 dpsi1^2 + 4 dpsi2^2)
+        const int *id = d.st2_idx + 7 * item;
+        r = d.rep_of[id[0]];
+        for (int u = d.st2_offby_off[item]; u < d.st2_offby_off[item + 1]; ++u) {  // E:1960-1981
+            const int k = d.st2_offby_idx[u];
+            const int *tid = d.st3_idx + 6 * k;
+            if (distance(P, tid[1], tid[4]).v - d.st3_nat[6 * k] < 10.0) return;
+        }
+        const Dual rr = distance(P, id[2], id[5]);
+        const Dual p1 = dihedral_of(P, id[0], id[1], id[3], id[4]);
+        const Dual p2 = dihedral_of(P, id[6], id[4], id[3], id[1]);
+        const double p10 = shifted(-2.58684, branch_of(p1.v, -2.58684));
+        const double p20 = shifted(3.07135, branch_of(p2.v, 3.07135));
+        const double r0 = d.st2_r0[item];
+        const Dual Dn = 1.0 + 1.4 * (rr - r0) * (rr - r0) + 4.0 * (p1 - p10) * (p1 - p10) + 4.0 * (p2 - p20) * (p2 - p20);
+        u1 = 1.0 / Dn.v;
+        param = a.st2_cls[item];
+        dE = a.st2_dss[item];
+        if (mode == 1) {
+            A.scale = d.st2_E[item];
+            const Dual w = -1.0 / (Dn * Dn);
+            bond_force(P, A, id[2], id[5], 1.4 * w, r0);
+            dihedral_force(P, A, id[0], id[1], id[3], id[4], 4.0 * w, p10);
+            dihedral_force(P, A, id[6], id[4], id[3], id[1], 4.0 * w, p20);
+        }
+    } else {  // formed H-bond: U = hb_E exp(-q)
+        const int *id = d.hb_idx + 6 * item;
+        const double *nat = d.hb_nat + 6 * item;
+        r = d.rep_of[id[0]];
+        int br[3];
+        const Dual rdev = distance(P, id[1], id[4]) - nat[0];
+        const Dual q = six_q(P, id, nat, rdev, 0.0, br);
+        const Dual e = dexp(-q);
+        u1 = e.v;
+        param = 5;
+        dE = a.hb_dhs[item];
+        if (mode == 1) {
+            A.scale = d.hb_E[item];
+            six_force(P, A, id, nat, br, -e);
+        }
+    }
+    if (param < 0 || dE == 0.0) return;
+    const double gval = mode == 0 ? u1 * dE : A.w * dE;
+    if (gval != 0.0) atomicAdd(a.dth + r * kNP + param, gval);
+}
+
+// ---------------------------------------------------------------------------
+// reverse pass of move_rigid_units (E:2660-2732, leap_frog_move_atom E:570-642,
+// adjust_box E:2632-2656) with full_forces' noise (E:2612-2622)
+// ---------------------------------------------------------------------------
+// per replica: S = sum over particles of (lambda_x' + lambda_xo'), the adjoint of
+// the recentring shift sh = box/2 - x'_centre that moves every x' and x_old'
+__global__ void __launch_bounds__(kBlock) k_adj_center(Dev d, AdjDev a)
+{
+    __shared__ double s_red[3 * 32];
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int r = d.blk_rep[blockIdx.x];
+    const int P = d.P;
+    double v[3] = {0, 0, 0};
+    if ((d.q[p].w >> 16) & 1)
+        for (int c = 0; c < 3; ++c) v[c] = a.lam[c * P + p] + a.lam[(3 + c) * P + p];
+    block_reduce<3>(v, s_red);
+    if (threadIdx.x == 0)
+        for (int c = 0; c < 3; ++c) atomicAdd(a.cen + 3 * r + c, v[c]);
+}
+
+// lambda of (x', x_old', v') after the step -> lambda of (x, x_old, v) before it,
+// less the force path: lamf = K2 lambda_v' (the force's adjoint), mu += lamf
+// (the LR force's adjoint since its refresh), jv = 0; the friction's dependence
+// on the ion radii goes to dth
+__global__ void __launch_bounds__(kBlock) k_adj_move(Dev d, AdjDev a)
+{
+    __shared__ double s_red[2 * 32];
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int r = d.blk_rep[blockIdx.x];
+    const RepParams *R = d.rp + r;
+    const int P = d.P;
+    const int4 qp = d.q[p];
+    double g[2] = {0, 0};
+    if ((qp.w >> 16) & 1) {
+        const int t = qp.w & 0xff;
+        const double k1 = R->k1[t], k2 = R->k2[t], h = R->h;
+        const double sg = d.noise == 0 ? R->sigma[t] : 0.0;
+        const int kn = (p - R->p0 + 1) % 1000;
+        double v0[3], f[3], gn[3], vp[3], A[3], lvpp[3], lvp[3];
+        for (int c = 0; c < 3; ++c) {
+            v0[c] = a.rx[(6 + c) * P + p];
+            f[c] = a.rf[c * P + p];
+            gn[c] = a.rg[r * kNoise + kn + 1000 * c];
+            vp[c] = k1 * v0[c] + k2 * (f[c] + sg * gn[c]);
+            A[c] = a.lam[c * P + p] - (p == R->center ? a.cen[3 * r + c] : 0.0);
+            lvpp[c] = a.lam[(6 + c) * P + p] + h * A[c];
+        }
+        const double vv = vp[0] * vp[0] + vp[1] * vp[1] + vp[2] * vp[2];
+        const double vsq = R->vcap[t] * vv;
+        if (vsq > 1.0) {  // v'' = v' / sqrt(vcap |v'|^2): Jacobian (I - u u^T) / sqrt(vsq)
+            const double inv = 1.0 / sqrt(vv), nrm = sqrt(vsq);
+            const double u[3] = {vp[0] * inv, vp[1] * inv, vp[2] * inv};
+            const double ul = u[0] * lvpp[0] + u[1] * lvpp[1] + u[2] * lvpp[2];
+            for (int c = 0; c < 3; ++c) lvp[c] = (lvpp[c] - u[c] * ul) / nrm;
+        } else {
+            for (int c = 0; c < 3; ++c) lvp[c] = lvpp[c];
+        }
+        for (int c = 0; c < 3; ++c) {
+            const double lxo = a.lam[(3 + c) * P + p];
+            a.lam[c * P + p] = 2.0 * A[c] + lxo;
+            a.lam[(3 + c) * P + p] = -A[c];
+            a.lam[(6 + c) * P + p] = k1 * lvp[c] - h * A[c];
+            const double lf = k2 * lvp[c];
+            a.lamf[c * P + p] = lf;
+            a.mu[c * P + p] += lf;
+            a.jv[c * P + p] = 0.0;
+        }
+        const int rp = radius_param(t);
+        if (rp >= 0) {  // VISC = 0.555 RLJ; K1 = exp(-VISC h / m); K2 = (1 - K1) / VISC; sigma = sqrt(2 VISC T / h)
+            const double visc = (1.0 - k1) / k2, m = R->mass[t];
+            const double dk1 = -k1 * h / m * 0.555;
+            const double dk2 = 0.555 * (k1 * h * visc / m - (1.0 - k1)) / (visc * visc);
+            const double dsg = sg > 0.0 ? 0.555 * sg / (2.0 * visc) : 0.0;
+            double s = 0.0;
+            for (int c = 0; c < 3; ++c) s += lvp[c] * (dk1 * v0[c] + dk2 * (f[c] + sg * gn[c]) + k2 * dsg * gn[c]);
+            g[rp - 12] = s;
+        }
+    }
+    block_reduce<2>(g, s_red);
+    if (threadIdx.x == 0) {
+        if (g[0] != 0.0) atomicAdd(a.dth + r * kNP + 12, g[0]);
+        if (g[1] != 0.0) atomicAdd(a.dth + r * kNP + 13, g[1]);
+    }
+}
+
+// lambda_x += J^T lamf (+ J_LR^T mu where the LR force was refreshed; mu then restarts)
+__global__ void __launch_bounds__(kBlock) k_adj_finish(Dev d, AdjDev a)
+{
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int r = d.blk_rep[blockIdx.x];
+    const int P = d.P;
+    for (int c = 0; c < 3; ++c) {
+        a.lam[c * P + p] += a.jv[c * P + p];
+        if (a.rlr[r]) a.mu[c * P + p] = 0.0;
+    }
+}
+
+// the step's inputs, after its forces and before its integrator: x .. v, the force
+// (f + the held LR force, without the noise) in FP64, the LR refresh flag
+__global__ void __launch_bounds__(kBlock) k_adj_record(Dev d, AdjDev a)
+{
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const int P = d.P;
+    const double *src[9] = {d.x, d.y, d.z, d.xo, d.yo, d.zo, d.vx, d.vy, d.vz};
+    for (int c = 0; c < 9; ++c) a.rx[c * P + p] = src[c][p];
+    for (int c = 0; c < 3; ++c) {
+        double v;
+        if (d.fp64) v = ((const double *)d.f)[c * P + p] + ((const double *)d.flr)[c * P + p];
+        else v = (double)(long long)(d.f[c * P + p] + d.flr[c * P + p]) * (1.0 / kFixScale);
+        a.rf[c * P + p] = v;
+    }
+    if (blockIdx.x == 0)
+        for (int r = threadIdx.x; r < d.R; r += blockDim.x) a.rlr[r] = d.rs[r].lr_now;
+}
+
+// nine packed host-order arrays (replicas end to end, n values each) <-> nine
+// component-major device arrays of P values (padding slots zero)
+__global__ void __launch_bounds__(kBlock) k_adj_unpack(Dev d, double *dst, const double *stage, int N, unsigned mask)
+{
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const RepParams *R = d.rp + d.blk_rep[blockIdx.x];
+    const int i = p - R->p0;
+    for (int c = 0; c < 9; ++c)
+        dst[(size_t)c * d.P + p] = (i < R->n && ((mask >> c) & 1u)) ? stage[(size_t)c * N + R->pk0 + i] : 0.0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_adj_pack(Dev d, const double *src, double *stage, int N)
+{
+    const int p = blockIdx.x * kBlock + threadIdx.x;
+    const RepParams *R = d.rp + d.blk_rep[blockIdx.x];
+    const int i = p - R->p0;
+    if (i >= R->n) return;
+    for (int c = 0; c < 9; ++c) stage[(size_t)c * N + R->pk0 + i] = src[(size_t)c * d.P + p];
+}
+
+}  // namespace
+
+void launch_adj_pair(const Dev &d, const AdjDev &a, cudaStream_t s, bool lr, const double *tan, int mode)
+{
+    if (lr) k_adj_pair<true><<<d.nblk, kBlock, 0, s>>>(d, a, tan, mode);
+    else k_adj_pair<false><<<d.nblk, kBlock, 0, s>>>(d, a, tan, mode);
+}
+
+void launch_adj_topo(const Dev &d, const AdjDev &a, cudaStream_t s, const double *tan, int mode)
+{
+    const int n = d.nbt + d.nst3 + d.nst2 + a.nhb;
+    if (n > 0) k_adj_topo<<<(n + kAdjTopoThreads - 1) / kAdjTopoThreads, kAdjTopoThreads, 0, s>>>(d, a, tan, mode);
+}
+
+void launch_adj_step(const Dev &d, const AdjDev &a, cudaStream_t s)
+{
+    cudaMemsetAsync(a.cen, 0, sizeof(double) * 3 * d.R, s);
+    k_adj_center<<<d.nblk, kBlock, 0, s>>>(d, a);
+    k_adj_move<<<d.nblk, kBlock, 0, s>>>(d, a);
+    launch_adj_pair(d, a, s, false, a.lamf, 1);
+    launch_adj_topo(d, a, s, a.lamf, 1);
+    launch_adj_pair(d, a, s, true, a.mu, 1);
+    k_adj_finish<<<d.nblk, kBlock, 0, s>>>(d, a);
+}
+
+void launch_adj_record(const Dev &d, const AdjDev &a, cudaStream_t s) { k_adj_record<<<d.nblk, kBlock, 0, s>>>(d, a); }
+
+void launch_adj_unpack(const Dev &d, cudaStream_t s, double *dst, const double *stage, int n, unsigned mask)
+{
+    k_adj_unpack<<<d.nblk, kBlock, 0, s>>>(d, dst, stage, n, mask);
+}
+
+void launch_adj_pack(const Dev &d, cudaStream_t s, const double *src, double *stage, int n)
+{
+    k_adj_pack<<<d.nblk, kBlock, 0, s>>>(d, src, stage, n);
+}
+
+}  // namespace tis

@@ -115,6 +115,10 @@ struct Group {
     tis::RepState *h_rs = nullptr;  // pinned host copy of the replicas' state (list build checks)
     int *h_peaks = nullptr;         // pinned: largest SR and LR neighbour counts of the last list build
     int *d_peaks = nullptr;
+    // parameter-derivative coefficients (tis_param_grad, tis_traj_grad)
+    double *a_st2_dss = nullptr, *a_hb_dhs = nullptr;
+    int *a_st2_cls = nullptr;
+    int nhb_all = 0, nhba_all = 0;  // H-bond candidates and H-bond atoms of all replicas
 
     ~Group()
     {
@@ -315,6 +319,8 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
     std::vector<int> st3_idx, st3_off, st2_idx, hb_idx, hb_dode, hb_aoff{0}, hb_aidx, hba_val, hba_coff{0}, hba_cidx,
         hba_n, ca_list;
     std::vector<double> st3_nat, st3_E, st2_r0, st2_E, hb_nat, hb_E;
+    std::vector<double> st2_dss, hb_dhs;  // parameter derivatives of st2_E (by ss_D) and hb_E (by hs_D)
+    std::vector<int> st2_cls;             // 5' base of each secondary stack (0-3 A C G U; -1 unknown)
     std::vector<std::vector<int>> excl_of;
     int p0 = 0, c0 = 0, kscr = 0;
     double max_rho = 0, max_rho_ch = 0;
@@ -508,7 +514,12 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         }
         hr.s31 = (int)st3_E.size();
         hr.s20 = (int)st2_E.size();
+        const tis::Array *s2d = s->get("st2_dss"), *s2c = s->get("st2_cls");
+        const bool have_dss = s2d && s2d->dtype == TIS_F64 && s2d->count() == n2 && s2c && s2c->dtype == TIS_I32 &&
+                              s2c->count() == n2;
         for (int64_t k = 0; k < n2; ++k) {
+            st2_dss.push_back(have_dss ? s2d->as<double>()[k] : 0.0);
+            st2_cls.push_back(have_dss ? s2c->as<int32_t>()[k] : -1);
             for (int c = 0; c < 7; ++c) {
                 const int v = s2i->as<int32_t>()[7 * k + c];
                 if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: secondary stack %lld bad index", base + r, (long long)k));
@@ -533,7 +544,12 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         if (!hai || !hci) return bail(TIS_ERR_ARG);
         hr.hb0 = (int)hb_E.size();
         hr.hba0 = (int)hba_val.size();
+        const tis::Array *hds = s->get("hb_dhs");
+        const bool have_dhs = hds && hds->dtype == TIS_F64 && hds->count() == nh;
+        const double hs_D = scalar_f64(s, "hs_D", 0.0);
         for (int64_t k = 0; k < nh; ++k) {
+            // hb_E = -0.73753 hs_D per bond of the candidate (E:3881, E:3963)
+            hb_dhs.push_back(have_dhs ? hds->as<double>()[k] : hs_D != 0.0 ? hE->as<double>()[k] / hs_D : 0.0);
             for (int c = 0; c < 6; ++c) {
                 const int v = hi->as<int32_t>()[6 * k + c];
                 if (v < 0 || v >= nrna) return bail(fail(TIS_ERR_ARG, "replica %d: H-bond candidate %lld bad index", base + r, (long long)k));
@@ -663,7 +679,9 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         (rc = dupload(O, &ih, hb_idx)) || (rc = dupload(O, &nh, hb_nat)) || (rc = dupload(O, &eh, hb_E)) ||
         (rc = dupload(O, &dh, hb_dode)) || (rc = dupload(O, &ao, hb_aoff)) || (rc = dupload(O, &ai, hb_aidx)) ||
         (rc = dupload(O, &hv, hba_val)) || (rc = dupload(O, &co, hba_coff)) || (rc = dupload(O, &ci, hba_cidx)) ||
-        (rc = dupload(O, &hn, hba_n)) || (rc = dupload(O, &ca, ca_list)))
+        (rc = dupload(O, &hn, hba_n)) || (rc = dupload(O, &ca, ca_list)) ||
+        (rc = dupload(O, &h->a_st2_dss, st2_dss)) || (rc = dupload(O, &h->a_st2_cls, st2_cls)) ||
+        (rc = dupload(O, &h->a_hb_dhs, hb_dhs)))
         return bail(rc);
     d.bt_idx = d_bti; d.bt_par = d_btp;
     d.st3_idx = i3; d.st3_nat = n3; d.st3_E = e3; d.st3_off = o3;
@@ -671,6 +689,8 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
     d.hb_idx = ih; d.hb_nat = nh; d.hb_E = eh; d.hb_dode = dh; d.hb_aoff = ao; d.hb_aidx = ai;
     d.hba_val = hv; d.hba_coff = co; d.hba_cidx = ci; d.hba_n = hn; d.ca_list = ca;
     const size_t nst2 = st2_E.size(), nst3 = st3_E.size(), nhb = hb_E.size(), nhba = hba_val.size();
+    h->nhb_all = (int)nhb;
+    h->nhba_all = (int)nhba;
     d.nbt = (int)bt_idx.size();
     d.nst3 = (int)nst3;
     d.nst2 = (int)nst2;
@@ -965,6 +985,216 @@ static int grp_compute_forces(Group *h, int r, int mask, double *forces, double 
         for (int k = 0; k < tis::kNE; ++k) energies[k] = et[k];
         energies[TIS_E_RG] = rg;
     }
+    return check_flags(h);
+}
+
+// ---------------------------------------------------------------------------
+// parameter derivatives and the reverse pass through steps (no counterpart in
+// the reference)
+// ---------------------------------------------------------------------------
+// device memory of one adjoint call, zeroed on the group's stream, freed with it
+struct AdjMem {
+    std::vector<void *> owned;
+    ~AdjMem()
+    {
+        for (void *p : owned) cudaFree(p);
+    }
+    template <class T>
+    int alloc(Group *h, T **p, size_t count)
+    {
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+        if (e != cudaSuccess)
+            return fail(TIS_ERR_NOMEM, "cudaMalloc(%zu bytes) for the adjoint: %s", count * sizeof(T), cudaGetErrorString(e));
+        owned.push_back((void *)*p);
+        e = cudaMemsetAsync(*p, 0, count * sizeof(T), h->stream);
+        if (e != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+        return TIS_OK;
+    }
+};
+
+static_assert(tis::kNParams == TIS_N_PARAMS, "parameter count");
+
+tis::AdjDev adj_base(const Group *h)
+{
+    tis::AdjDev a{};
+    a.st2_dss = h->a_st2_dss;
+    a.st2_cls = h->a_st2_cls;
+    a.hb_dhs = h->a_hb_dhs;
+    a.nhb = h->nhb_all;
+    return a;
+}
+
+static int grp_param_grad(Group *h, double *out)
+{
+    int rc;
+    if (!h->lists_built && (rc = populate(h))) return rc;
+    if ((rc = clear_flags(h))) return rc;
+    AdjMem M;
+    tis::AdjDev a = adj_base(h);
+    if ((rc = M.alloc(h, &a.dth, (size_t)h->R * tis::kNParams)) || (rc = M.alloc(h, &a.rhb, (size_t)h->nhb_all)))
+        return rc;
+    const size_t fbytes = sizeof(unsigned long long) * 3 * h->P;
+    // the valence-limited Monte Carlo of this state (as a force evaluation runs it),
+    // recording the bonds it leaves formed; its forces are dropped
+    tis::Dev dr = h->dev;
+    dr.hb_rec = a.rhb;
+    TIS_CUDA(cudaMemsetAsync(h->dev.f, 0, fbytes, h->stream));
+    tis::launch_topology(dr, h->stream, 16, false, false, true);
+    TIS_CUDA(cudaMemsetAsync(h->dev.f, 0, fbytes, h->stream));
+    a.px = h->dev.x;
+    a.py = h->dev.y;
+    a.pz = h->dev.z;
+    tis::launch_adj_pair(h->dev, a, h->stream, false, nullptr, 0);
+    tis::launch_adj_pair(h->dev, a, h->stream, true, nullptr, 0);
+    tis::launch_adj_topo(h->dev, a, h->stream, nullptr, 0);
+    TIS_CUDA(cudaGetLastError());
+    TIS_CUDA(cudaMemcpyAsync(out, a.dth, sizeof(double) * h->R * tis::kNParams, cudaMemcpyDeviceToHost, h->stream));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    return check_flags(h);
+}
+
+// the device arrays a step reads and leaves for the next one (the rest is rebuilt
+// or scratch): a checkpoint holds copies of these
+std::vector<std::pair<void *, size_t>> step_state(const Group *h)
+{
+    const tis::Dev &d = h->dev;
+    const size_t P = h->P;
+    std::vector<std::pair<void *, size_t>> v;
+    for (double *p : {d.x, d.y, d.z, d.xo, d.yo, d.zo, d.vx, d.vy, d.vz}) v.emplace_back(p, 8 * P);
+    v.emplace_back(d.q, sizeof(int4) * P);
+    v.emplace_back(d.flr, 24 * P);
+    v.emplace_back(d.rs, sizeof(tis::RepState) * h->R);
+    v.emplace_back(d.n_sr, 4 * P);
+    v.emplace_back(d.n_lr, 4 * P);
+    v.emplace_back(d.nbr_sr, 4 * (size_t)d.cap_sr * P);
+    v.emplace_back(d.nbr_lr, 4 * (size_t)d.cap_lr * P);
+    v.emplace_back(d.hb_status, 4 * (size_t)h->nhb_all);
+    v.emplace_back(d.hb_excess, 4 * (size_t)h->nhba_all);
+    v.emplace_back(d.hb_active, 4 * (size_t)h->nhb_all);
+    return v;
+}
+
+inline size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+// seed: the group's part of nine packed arrays from offset `off` (NULL entries zero);
+// dtheta: R x kNParams of the group; dstate0: packed like seed (NULL entries skipped)
+static int grp_traj_grad(Group *h, int64_t steps, int K, const double *const *seed, int64_t off, double *dtheta,
+                         double *const *dstate0)
+{
+    int rc;
+    if ((rc = clear_flags(h))) return rc;
+    if ((rc = populate(h))) return rc;  // the run starts with populate_lists (E:6237): lists and LR force fresh
+    const tis::Dev &d = h->dev;
+    const size_t P = h->P, R = h->R;
+    const auto st = step_state(h);
+    size_t sbytes = 0;
+    for (const auto &e : st) sbytes += align256(e.second);
+    const int64_t nseg = (steps + K - 1) / K;
+    AdjMem M;
+    char *arena = nullptr;
+    tis::AdjDev a = adj_base(h);
+    double *rx, *rf, *rg;
+    int *rhb, *rlr, *rnsr, *rnlr, *rbsr, *rblr;
+    const size_t Kz = (size_t)K, nhb = (size_t)h->nhb_all;
+    if ((rc = M.alloc(h, &arena, (size_t)(nseg + 1) * sbytes)) || (rc = M.alloc(h, &a.lam, 9 * P)) ||
+        (rc = M.alloc(h, &a.lamf, 3 * P)) || (rc = M.alloc(h, &a.mu, 3 * P)) || (rc = M.alloc(h, &a.jv, 3 * P)) ||
+        (rc = M.alloc(h, &a.cen, 3 * R)) || (rc = M.alloc(h, &a.dth, R * tis::kNParams)) ||
+        (rc = M.alloc(h, &rx, Kz * 9 * P)) || (rc = M.alloc(h, &rf, Kz * 3 * P)) ||
+        (rc = M.alloc(h, &rg, Kz * R * tis::kNoise)) || (rc = M.alloc(h, &rhb, Kz * std::max<size_t>(nhb, 1))) ||
+        (rc = M.alloc(h, &rlr, Kz * R)) || (rc = M.alloc(h, &rnsr, Kz * P)) || (rc = M.alloc(h, &rnlr, Kz * P)) ||
+        (rc = M.alloc(h, &rbsr, Kz * d.cap_sr * P)) || (rc = M.alloc(h, &rblr, Kz * d.cap_lr * P)))
+        return rc;
+    auto save = [&](int64_t slot) {
+        char *p = arena + slot * sbytes;
+        for (const auto &e : st) {
+            if (e.second) cudaMemcpyAsync(p, e.first, e.second, cudaMemcpyDeviceToDevice, h->stream);
+            p += align256(e.second);
+        }
+    };
+    auto restore = [&](int64_t slot) {
+        const char *p = arena + slot * sbytes;
+        for (const auto &e : st) {
+            if (e.second) cudaMemcpyAsync(e.first, p, e.second, cudaMemcpyDeviceToDevice, h->stream);
+            p += align256(e.second);
+        }
+    };
+    // the recorded step j of a segment: its inputs and the lists its forces read
+    auto slot = [&](int j, tis::Dev &dj) {
+        tis::AdjDev aj = a;
+        aj.rx = rx + (size_t)j * 9 * P;
+        aj.rf = rf + (size_t)j * 3 * P;
+        aj.rg = rg + (size_t)j * R * tis::kNoise;
+        aj.rhb = rhb + (size_t)j * std::max<size_t>(nhb, 1);
+        aj.rlr = rlr + (size_t)j * R;
+        aj.px = aj.rx;
+        aj.py = aj.rx + P;
+        aj.pz = aj.rx + 2 * P;
+        dj = d;
+        dj.n_sr = rnsr + (size_t)j * P;
+        dj.n_lr = rnlr + (size_t)j * P;
+        dj.nbr_sr = rbsr + (size_t)j * d.cap_sr * P;
+        dj.nbr_lr = rblr + (size_t)j * d.cap_lr * P;
+        return aj;
+    };
+
+    // forward, a checkpoint every K steps and one of the final state
+    for (int64_t s = 0; s < steps; ++s) {
+        if (s % K == 0) save(s / K);
+        enqueue_step(h);
+    }
+    save(nseg);
+    TIS_CUDA(cudaGetLastError());
+    if ((rc = check_flags(h))) return rc;
+
+    // dL/d(final state)
+    unsigned mask = 0;
+    for (int c = 0; c < 9; ++c)
+        if (seed && seed[c]) {
+            mask |= 1u << c;
+            TIS_CUDA(cudaMemcpyAsync(h->stage + (size_t)c * h->npk, seed[c] + off, sizeof(double) * h->npk,
+                                     cudaMemcpyHostToDevice, h->stream));
+        }
+    tis::launch_adj_unpack(d, h->stream, a.lam, h->stage, h->npk, mask);
+
+    // backward: each segment recomputed from its checkpoint, then its steps in reverse
+    for (int64_t g = nseg - 1; g >= 0; --g) {
+        restore(g);
+        const int len = (int)std::min<int64_t>(K, steps - g * K);
+        for (int j = 0; j < len; ++j) {
+            tis::Dev dj;
+            const tis::AdjDev aj = slot(j, dj);
+            h->dev.hb_rec = aj.rhb;
+            enqueue_forces(h, true);
+            h->dev.hb_rec = nullptr;
+            TIS_CUDA(cudaMemcpyAsync(aj.rg, d.gnoise, sizeof(double) * R * tis::kNoise, cudaMemcpyDeviceToDevice, h->stream));
+            TIS_CUDA(cudaMemcpyAsync(dj.n_sr, d.n_sr, 4 * P, cudaMemcpyDeviceToDevice, h->stream));
+            TIS_CUDA(cudaMemcpyAsync(dj.n_lr, d.n_lr, 4 * P, cudaMemcpyDeviceToDevice, h->stream));
+            TIS_CUDA(cudaMemcpyAsync(dj.nbr_sr, d.nbr_sr, 4 * (size_t)d.cap_sr * P, cudaMemcpyDeviceToDevice, h->stream));
+            TIS_CUDA(cudaMemcpyAsync(dj.nbr_lr, d.nbr_lr, 4 * (size_t)d.cap_lr * P, cudaMemcpyDeviceToDevice, h->stream));
+            tis::launch_adj_record(d, aj, h->stream);
+            tis::launch_integrate(d, h->stream);
+            tis::launch_rebuild(d, h->stream);
+        }
+        for (int j = len - 1; j >= 0; --j) {
+            tis::Dev dj;
+            const tis::AdjDev aj = slot(j, dj);
+            tis::launch_adj_step(dj, aj, h->stream);
+        }
+        TIS_CUDA(cudaGetLastError());
+    }
+    if ((rc = check_flags(h))) return rc;
+    restore(nseg);
+    TIS_CUDA(cudaMemcpyAsync(dtheta, a.dth, sizeof(double) * R * tis::kNParams, cudaMemcpyDeviceToHost, h->stream));
+    if (dstate0) {
+        tis::launch_adj_pack(d, h->stream, a.lam, h->stage, h->npk);
+        for (int c = 0; c < 9; ++c)
+            if (dstate0[c])
+                TIS_CUDA(cudaMemcpyAsync(dstate0[c] + off, h->stage + (size_t)c * h->npk, sizeof(double) * h->npk,
+                                         cudaMemcpyDeviceToHost, h->stream));
+    }
+    TIS_CUDA(cudaGetLastError());
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
     return check_flags(h);
 }
 
@@ -1460,6 +1690,24 @@ int tis_get_forces(tis_handle *h, int r, double *forces)
     if (rc) return rc;
     TIS_CUDA(cudaStreamSynchronize(h->stream));
     return grp_get_forces(g, loc, forces);
+}
+
+int tis_param_grad(tis_handle *h, double *out)
+{
+    if (!h || !out) return fail(TIS_ERR_ARG, "tis_param_grad: bad argument");
+    return each_group(h, [&](Group *g) { return grp_param_grad(g, out + (size_t)g->base * tis::kNParams); });
+}
+
+int tis_traj_grad(tis_handle *h, int64_t steps, int32_t checkpoint_every, const double *const *seed, double *dtheta,
+                  double *const *dstate0)
+{
+    if (!h || steps < 1 || checkpoint_every < 1 || !dtheta) return fail(TIS_ERR_ARG, "tis_traj_grad: bad argument");
+    int64_t off = 0;
+    return each_group(h, [&](Group *g) {
+        const int rc = grp_traj_grad(g, steps, checkpoint_every, seed, off, dtheta + (size_t)g->base * tis::kNParams, dstate0);
+        off += g->npk;
+        return rc;
+    });
 }
 
 int tis_full_forces(tis_handle *h)

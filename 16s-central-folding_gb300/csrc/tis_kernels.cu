@@ -1002,6 +1002,8 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
             }
         }
     }
+    if (do_hb && d.hb_rec)  // the bonds formed after the Monte Carlo (status 0; 1 broken, -1 out of range)
+        for (int i = tid; i < nhb; i += bd) d.hb_rec[hb0 + i] = w.st[i] == 0 ? 1 : 0;
     // ---- full_forces: the step's Gaussians follow the Monte Carlo draws ----
     const unsigned long long c1 = s_ctr;
     if (make_noise) gen_noise<D>(d, r, c1);

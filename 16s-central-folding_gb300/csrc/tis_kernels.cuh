@@ -58,6 +58,24 @@ struct Dev {
     double *eterm;              // R x kNE (per-term energies, compute_forces only)
     double *shift;              // R x 3, recentring shift of the current step (adjust_box)
     const int *cell_rep;        // replica of every cell
+    int *hb_rec;                // when not null: 1 per H-bond candidate formed after the step's Monte Carlo, else 0
+};
+
+// Adjoint work of one handle (tis_adjoint.cu).  Arrays of 3P or 9P values are
+// component-major (c * P + p) like the state arrays.
+constexpr int kNParams = 15;    // force-field parameters (TIS_N_PARAMS)
+struct AdjDev {
+    const double *st2_dss;      // d st_E / d ss_D of every secondary stack
+    const int *st2_cls;         // its 5' base (0 A, 1 C, 2 G, 3 U; -1 none)
+    const double *hb_dhs;       // d hb_E / d hs_D of every H-bond candidate
+    int nhb;                    // H-bond candidates of all replicas
+    double *lam;                // 9P: adjoint of (x, x_old, v)
+    double *lamf, *mu, *jv;     // 3P: adjoint of the step's force; of the held LR force; J lambda
+    double *cen;                // R x 3: adjoint of the recentring shift
+    double *dth;                // R x kNParams: parameter gradient
+    double *rx, *rf, *rg;       // recorded step: 9P state before it, 3P force, R x kNoise Gaussians
+    int *rhb, *rlr;             // recorded step: H-bonds formed (per candidate), LR refreshed (per replica)
+    const double *px, *py, *pz; // positions the pair and restraint terms are evaluated at
 };
 
 // Byte offsets of the H-bond kernel's shared-memory arrays (one replica's working
@@ -116,5 +134,17 @@ void launch_search(const Dev &d, cudaStream_t s);
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s);
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out);
 int kernel_launches_per_step();
+
+// adjoint (tis_adjoint.cu).  mode 0: dU/dtheta into a.dth at positions a.px..;
+// mode 1: a.jv += J tan and the parameter terms of lambda = tan.
+void launch_adj_pair(const Dev &d, const AdjDev &a, cudaStream_t s, bool lr, const double *tan, int mode);
+void launch_adj_topo(const Dev &d, const AdjDev &a, cudaStream_t s, const double *tan, int mode);
+// the reverse pass of one recorded step: a.lam (after the step) -> a.lam (before it)
+void launch_adj_step(const Dev &d, const AdjDev &a, cudaStream_t s);
+// records the step's inputs into a.rx, a.rf, a.rlr (after the forces, before the integrator)
+void launch_adj_record(const Dev &d, const AdjDev &a, cudaStream_t s);
+// packed host-order state arrays (tis_set_states layout) <-> 9P device arrays
+void launch_adj_unpack(const Dev &d, cudaStream_t s, double *dst, const double *stage, int n, unsigned mask);
+void launch_adj_pack(const Dev &d, cudaStream_t s, const double *src, double *stage, int n);
 
 }  // namespace tis

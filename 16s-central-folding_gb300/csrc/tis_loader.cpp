@@ -84,10 +84,13 @@ struct Setup {
     std::vector<std::vector<int>> hb_atom_cands{{}};  // HB_ATOM (1-based candidate ids)
     std::vector<int> hk10{0}, hk11{0}, hk12{0}, hk20{0}, hk21{0}, hk22{0}, hdode{0};
     std::vector<double> hr{0}, ht1{0}, ht2{0}, hp{0}, hp1{0}, hp2{0}, hE{0};
+    std::vector<double> hdE{0};  // d hb_E / d hs_D of every candidate
     std::vector<std::vector<int>> atom_hb{{}};  // ATOM_HB
     // stacks
     std::vector<int> st_i{0}, st_j{0}, site0{0}, site1{0}, st_excess;
     std::vector<double> sr{0}, st1{0}, st2{0}, sp{0}, sp1{0}, sp2{0}, sE{0};
+    std::vector<double> sdss{0};  // d st_E / d ss_D of every stack (0 for tertiary stacks)
+    std::vector<int> scls{0};     // 5' base of a secondary stack: 0 A, 1 C, 2 G, 3 U (-1 tertiary)
     int s3N = 0, stN = 0;
 
     double dist(int i1, int i2) const
@@ -346,6 +349,7 @@ struct Setup {
                         break;
                 if (k <= hbN) {
                     hE[k] -= p->hs_D * 0.73753;
+                    hdE[k] -= 0.73753;
                 } else if ((!strcmp(A0, "CAN51") && !strcmp(A2, "O2'")) || (!strcmp(A0, "CAN52") && !strcmp(A1, "O2'"))) {
                     k = hbN;
                     if (k < 1) {
@@ -363,6 +367,7 @@ struct Setup {
                     hp1.push_back(dihedral(k21, k11, k10, k12));
                     hp2.push_back(dihedral(k11, k21, k20, k22));
                     hE.push_back(-p->hs_D * 0.73753);
+                    hdE.push_back(-0.73753);
                     for (const CanGeom &g : kCan)
                         if (!strcmp(A0, g.code)) {
                             hr[hbN] = g.r; ht1[hbN] = g.t1; ht2[hbN] = g.t2;
@@ -431,6 +436,8 @@ struct Setup {
             sp1.push_back(dihedral(k21, k11, k10, k12));
             sp2.push_back(dihedral(k11, k21, k20, k22));
             sE.push_back(-p->st_D);
+            sdss.push_back(0.0);
+            scls.push_back(-1);
             if (A1[0] == '-') i--;
             if (A2[0] == '-') j--;
             if (i < 1 || j < 1) {
@@ -449,14 +456,17 @@ struct Setup {
             ++stN;
             st_i.push_back(i);
             st_j.push_back(0);
-            double r0 = 0, e = 0;
+            double r0 = 0, e = 0, de = 0;
             for (const SecStack &t : kSecStack)
                 if (amino[i] == t.a && amino[i + 2] == t.b) {
                     r0 = t.r0;
                     e = t.e0 + p->ss_D / t.div + t.slope * (T - t.t0);
+                    de = 1.0 / t.div;
                 }
             sr.push_back(r0);
             sE.push_back(e);
+            sdss.push_back(de);
+            scls.push_back(amino[i] == 'A' ? 0 : amino[i] == 'C' ? 1 : amino[i] == 'G' ? 2 : amino[i] == 'U' ? 3 : -1);
             st1.push_back(0); st2.push_back(0); sp.push_back(0); sp1.push_back(0); sp2.push_back(0);
             site0.push_back(i);
             site1.push_back(i + 1);
@@ -789,8 +799,8 @@ int tis_system_load(const tis_load_params *p, tis_system **out)
     // stacks
     {
         const int n3 = S.s3N, n2 = S.stN - S.s3N;
-        std::vector<int32_t> idx3, site, si3, sj3, idx2, si2, ex;
-        std::vector<double> nat3, E3, r02, E2;
+        std::vector<int32_t> idx3, site, si3, sj3, idx2, si2, ex, cls2;
+        std::vector<double> nat3, E3, r02, E2, dss2;
         for (int k = 1; k <= n3; ++k) {
             const int i = S.st_i[k], j = S.st_j[k];
             si3.push_back(i); sj3.push_back(j);
@@ -809,6 +819,8 @@ int tis_system_load(const tis_load_params *p, tis_system **out)
             for (int c = 0; c < 7; ++c) idx2.push_back(ids[c] - 1);
             r02.push_back(S.sr[k]);
             E2.push_back(S.sE[k]);
+            dss2.push_back(S.sdss[k]);
+            cls2.push_back(S.scls[k]);
         }
         for (int e = 1; e <= NBP; ++e) ex.push_back(S.st_excess[e]);
         std::vector<int32_t> off(2 * n3, -1);
@@ -831,18 +843,21 @@ int tis_system_load(const tis_load_params *p, tis_system **out)
         s->set_i32("st2_idx", idx2);
         s->set_f64("st2_r0", r02);
         s->set_f64("st2_E", E2);
+        s->set_f64("st2_dss", dss2);
+        s->set_i32("st2_cls", cls2);
     }
     // hydrogen bonds
     {
         const int nh = (int)S.hE.size() - 1;
         std::vector<int32_t> idx, dode, aoff{0}, aidx, val, coff{0}, cidx;
-        std::vector<double> nat, E;
+        std::vector<double> nat, E, dE;
         for (int k = 1; k <= nh; ++k) {
             const int ids[6] = {S.hk10[k], S.hk11[k], S.hk12[k], S.hk20[k], S.hk21[k], S.hk22[k]};
             for (int c = 0; c < 6; ++c) idx.push_back(ids[c] - 1);
             const double nv[6] = {S.hr[k], S.ht1[k], S.ht2[k], S.hp[k], S.hp1[k], S.hp2[k]};
             for (int c = 0; c < 6; ++c) nat.push_back(nv[c]);
             E.push_back(S.hE[k]);
+            dE.push_back(S.hdE[k]);
             dode.push_back(S.hdode[k]);
             for (int a : S.atom_hb[k]) aidx.push_back(a - 1);
             aoff.push_back((int32_t)aidx.size());
@@ -856,6 +871,7 @@ int tis_system_load(const tis_load_params *p, tis_system **out)
         s->set_i32("hb_idx", idx);
         s->set_f64("hb_native", nat);
         s->set_f64("hb_E", E);
+        s->set_f64("hb_dhs", dE);
         s->set_i32("hb_dode", dode);
         s->set_i32("hb_atom_off", aoff);
         s->set_i32("hb_atom_idx", aidx);

@@ -15,6 +15,10 @@ STATE_NAMES = ["x", "y", "z", "ox", "oy", "oz", "vx", "vy", "vz"]
 ENERGY_NAMES = ["E_lj", "E_coul_sr", "E_coul_lr", "E_bond", "E_angle", "E_excl",
                 "E2_STACK", "E3_STACK", "E2_HB", "E3_HB", "Rg"]
 TERM_SR, TERM_LR, TERM_BONDED, TERM_STACK, TERM_HB = 1, 2, 4, 8, 16
+# force-field parameters of tis_param_grad / tis_traj_grad (TIS_N_PARAMS, in order)
+PARAM_NAMES = ["ss_D_A", "ss_D_C", "ss_D_G", "ss_D_U", "st_D", "hs_D", "eps_P", "eps_S", "eps_B", "eps_Mg", "eps_Cl",
+               "eps_K", "R_Mg", "R_K", "lB"]
+N_PARAMS = len(PARAM_NAMES)
 PREC_MIXED, PREC_FP64 = 0, 1
 NOISE_REFERENCE, NOISE_OFF = 0, 1
 
@@ -101,6 +105,8 @@ def _declare(L):
         "tis_profile_stages": [vp, i64, dp],
         "tis_get_forces": [vp, i32, dp],
         "tis_pair_lists_noalloc": [vp, vp, vp, vp, C.c_int32, dp, C.c_double, C.c_double, vp, i64, vp, i64, vp, vp],
+        "tis_param_grad": [vp, dp],
+        "tis_traj_grad": [vp, i64, i32, C.POINTER(dp), dp, C.POINTER(dp)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -115,7 +121,8 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_move_rigid_units", "tis_check_shifts", "tis_step", "tis_sync", "tis_get_energies",
             "tis_get_stack_energies", "tis_get_counters", "tis_get_info", "tis_replica_size", "tis_get_launch_count",
             "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc", "tis_set_states",
-            "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts"]
+            "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
+            "tis_param_grad", "tis_traj_grad"]
 
 
 def read_last_frame(path, n):
@@ -289,6 +296,35 @@ class Engine:
         ptrs = [(_dp(out[k]) if k in names else None) for k in STATE_NAMES]
         _check(lib().tis_get_states(self.h, *ptrs))
         return {k: out[k] for k in names}
+
+    def param_grad(self):
+        """(replicas, N_PARAMS) array of dU/dtheta at every replica's current state (PARAM_NAMES order)."""
+        out = np.zeros((len(self.n), N_PARAMS))
+        _check(lib().tis_param_grad(self.h, _dp(out)))
+        return out
+
+    def traj_grad(self, steps, checkpoint_every, seed, want_state=False):
+        """Gradient of a loss of the state after `steps` fixed-noise steps (from a list build).
+        seed: {name: dL/d(final state), packed like set_states}; names left out are zero.
+        Returns (replicas, N_PARAMS) dL/dtheta, and with want_state also the packed
+        dL/d(initial state) dict."""
+        total = sum(self.n)
+        keep = []
+        seeds = (C.POINTER(C.c_double) * 9)()
+        for c, k in enumerate(STATE_NAMES):
+            if k in seed:
+                a = np.ascontiguousarray(seed[k], dtype=np.float64)
+                if a.size != total:
+                    raise ValueError(f"seed {k}: expected {total} values, got {a.size}")
+                keep.append(a)
+                seeds[c] = _dp(a)
+        out = np.zeros((len(self.n), N_PARAMS))
+        d0 = {k: np.zeros(total) for k in STATE_NAMES} if want_state else None
+        dps = None
+        if want_state:
+            dps = (C.POINTER(C.c_double) * 9)(*[_dp(d0[k]) for k in STATE_NAMES])
+        _check(lib().tis_traj_grad(self.h, int(steps), int(checkpoint_every), seeds, _dp(out), dps))
+        return (out, d0) if want_state else out
 
     def all_energies(self, out=None):
         """(replicas, 5) array of tis_get_energies' five values for every replica."""

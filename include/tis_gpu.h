@@ -252,6 +252,49 @@ int tis_get_launch_count(tis_handle *h, int64_t *n);
 int tis_rand_stream(uint64_t seed, uint64_t first, int64_t n, int32_t *out);
 
 /* ------------------------------------------------------------------------ */
+/* Parameter derivatives (no counterpart in the reference)                    */
+/* ------------------------------------------------------------------------ */
+/* The force-field parameters theta, in this order, as the reference defines them:
+ *   0-3  ss_D of the secondary stacks whose 5' base is A, C, G, U (the -D flag,
+ *        split by 5' base; st_E = e0 + ss_D / c + s (T - T0), E:4397-4427)
+ *   4    st_D, tertiary stacking strength (-d; st_E = -st_D, E:4344)
+ *   5    hs_D, H-bond strength (-E; hb_E = -0.73753 hs_D per bond of a candidate,
+ *        E:3881, E:3963)
+ *   6-11 ELJ of P, S, the four bases (one pooled value), Mg, Cl, K (MAXIKEY;
+ *        E_LJ = sqrt(ELJ_i ELJ_j), E:2930)
+ *   12-13 RLJ of Mg and K (the contact distance R_i + R_j of pairs with an ion,
+ *        E:2918-2922, and the friction 0.555 RLJ of the ion, E:2897-2903)
+ *   14   lB, the Coulomb strength 332.06 (0.0327 T - 0.0067) (E:6109)
+ * Derivatives follow the forces: the LJ energy is the shifted WCA form
+ * E_LJ (s^12 - 2 s^6 + 1) without the reporting clamp below D2_LJ_MINIMUM, bonded
+ * pairs carry the net LJ weight of the force path, and discrete events (H-bond
+ * Monte Carlo choices, stack switching, list membership, velocity cap, ion wrap)
+ * are held as the forward pass took them. */
+#define TIS_N_PARAMS 15
+
+/* dU/dtheta of every replica at its current state: out[TIS_N_PARAMS * replica + j],
+ * U the total potential (pairs, bonded, stacks, H-bonds).  The H-bond term uses
+ * the bonds that the valence-limited Monte Carlo (E:2239-2315) leaves formed at
+ * this state, run as a force evaluation runs it (it consumes rand() draws).  Lists
+ * are rebuilt first when the state was set since the last build. */
+int tis_param_grad(tis_handle *h, double *out);
+
+/* Gradient of a loss of the final state through `steps` steps of the fused
+ * Langevin step (fixed noise: the rand() stream is part of the state), starting
+ * with a list build (populate_lists, as the reference's run starts).  The forward
+ * pass keeps a checkpoint of the whole engine state every `checkpoint_every`
+ * steps; the backward pass recomputes each interval from its checkpoint and runs
+ * the adjoint of every step (integrator, recentring, the forces' Jacobian as a
+ * directional derivative, the multiple-time-step LR force held between its
+ * refreshes) in FP64.  seed[9]: dL/d(x, y, z, xo, yo, zo, vx, vy, vz) of the final
+ * state, packed as tis_set_states packs states (any may be NULL: zero).  Output:
+ * dtheta[TIS_N_PARAMS * replica + j] = dL/dtheta_j and, if dstate0 is not NULL,
+ * dL/d(initial state) packed the same way (NULL entries skipped).  On return the
+ * engine holds the final state of the forward pass. */
+int tis_traj_grad(tis_handle *h, int64_t steps, int32_t checkpoint_every, const double *const *seed,
+                  double *dtheta, double *const *dstate0);
+
+/* ------------------------------------------------------------------------ */
 /* Allocation-free list build                                                 */
 /* ------------------------------------------------------------------------ */
 /* No counterpart in the reference: an addition for callers that cannot allocate
