@@ -362,6 +362,33 @@ def gpu_arm(args):
         plain.sync()
         torch.cuda.synchronize()
         plain_sps = NP / (t0e.elapsed_time(t1e) / 1000.0)
+        plain.close()
+
+        # the differentiation workload: 16 replicas of the chain, dU/dtheta of 15
+        # parameters at their current frames, and the gradient through a 200-step
+        # fixed-noise trajectory with a checkpoint every 10 steps (forward, recomputation
+        # and reverse pass in one call); host wall clock around synchronous calls
+        adjoint = None
+        if rank == 0:
+            adj = Engine(systems[:16], precision=PREC_MIXED, device=local)
+            adj.populate_lists()
+            adj.step(50)
+            adj.sync()
+            adj.param_grad()
+            t0 = time.perf_counter()
+            for _ in range(5):
+                adj.param_grad()
+            t_pg = (time.perf_counter() - t0) / 5
+            rng = np.random.default_rng(0)
+            seed = {k: rng.standard_normal(sum(adj.n)) for k in ("x", "y", "z")}
+            adj.traj_grad(20, 10, seed)
+            t0 = time.perf_counter()
+            adj.traj_grad(200, 10, seed)
+            t_tg = time.perf_counter() - t0
+            adjoint = {"replicas": 16, "param_grad_frames_per_s": 16 / t_pg,
+                       "traj_steps": 200, "checkpoint_every": 10, "traj_grad_s": t_tg,
+                       "traj_grad_replica_steps_per_s": 16 * 200 / t_tg, "precision": "mixed forward, FP64 adjoint"}
+            adj.close()
 
     if rank != 0:
         return
@@ -379,7 +406,7 @@ def gpu_arm(args):
             "plain_fp64_single_replica_steps_per_s": plain_sps,
             "batched_vs_plain": value / world / plain_sps,
             "stage_ms_per_step": stages,
-            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "adjoint": adjoint,
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 

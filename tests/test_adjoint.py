@@ -98,8 +98,11 @@ def _loss(state, seed):
 @pytest.mark.parametrize("steps,every", [(40, 10), (23, 7)])
 def test_traj_grad_matches_finite_differences(small, thermal, steps, every):
     """dL/dtheta and dL/dx0 through `steps` fixed-noise FP64 steps (list rebuilds
-    and LR refreshes included) against central differences of L = w . (x_T, v_T),
-    h = 1e-5 relative."""
+    and LR refreshes included) against central differences of L = w . (x_T, v_T).
+    Steps: 1e-3 relative for the parameters that enter as factors (the difference
+    is then exact up to rounding), 1e-4 for the ion radii (whose truncation error,
+    h^2, is 1e-4 relative at h = 1e-3); floor: FP64 rounding of L (1e-14 |L|)
+    divided by the step."""
     th0 = params_of(small)
     n = thermal["x"].size
     rng = np.random.default_rng(11)
@@ -112,19 +115,24 @@ def test_traj_grad_matches_finite_differences(small, thermal, steps, every):
     ref = run_final_state(small, th0, thermal, steps, precision=PREC_FP64)
     for k in STATE_NAMES:  # tis_traj_grad leaves the forward pass's final state
         np.testing.assert_allclose(fin[k], ref[k], rtol=0, atol=1e-9)
-    L0 = _loss(ref, seed)
-    L1 = _loss(run_final_state(small, th0, thermal, steps, precision=PREC_FP64), seed)
-    noise = max(abs(L1 - L0), 1e-15 * sum(np.abs(ref[k]).sum() for k in seed))
-    rows = []
+    L = [_loss(ref, seed)] + [_loss(run_final_state(small, th0, thermal, steps, precision=PREC_FP64), seed)
+                              for _ in range(3)]
+    noise = max(max(L) - min(L), 1e-14 * abs(L[0]))
+    rows = [f"L {L[0]:.6e}, spread over 4 runs {max(L) - min(L):.2e}"]
+    worst = 0.0
     for j in range(N_PARAMS):
-        hj = 1e-5 * abs(th0[j])
+        hj = (1e-4 if PARAM_NAMES[j].startswith("R_") else 1e-3) * abs(th0[j])
         tp, tm = th0.copy(), th0.copy()
         tp[j] += hj
         tm[j] -= hj
         fd = (_loss(run_final_state(small, tp, thermal, steps, precision=PREC_FP64), seed) -
               _loss(run_final_state(small, tm, thermal, steps, precision=PREC_FP64), seed)) / (2 * hj)
-        tol = 1e-4 * abs(fd) + 10 * noise / hj
-        rows.append(f"{PARAM_NAMES[j]} adj {dth[0, j]:+.9e} fd {fd:+.9e}")
+        floor = noise / hj
+        tol = 1e-4 * abs(fd) + floor
+        rows.append(f"{PARAM_NAMES[j]:7s} adj {dth[0, j]:+.9e} fd {fd:+.9e} diff {abs(dth[0, j] - fd):.1e} "
+                    f"floor {floor:.1e}")
+        if floor < 1e-5 * abs(fd):
+            worst = max(worst, abs(dth[0, j] - fd) / abs(fd))
         assert abs(dth[0, j] - fd) <= tol, rows[-1]
     # a random direction of the initial positions
     delta = {k: rng.standard_normal(n) for k in ("x", "y", "z")}
@@ -135,8 +143,66 @@ def test_traj_grad_matches_finite_differences(small, thermal, steps, every):
           _loss(run_final_state(small, th0, sm, steps, precision=PREC_FP64), seed)) / (2 * h)
     ad = sum(float(np.dot(d0[k], delta[k])) for k in delta)
     rows.append(f"x0 direction adj {ad:+.9e} fd {fd:+.9e}")
+    rows.append(f"largest relative difference where the floor is below 1e-5 of it: {worst:.2e}")
     print("\n".join(rows))
-    assert abs(ad - fd) <= 1e-4 * abs(fd) + 10 * noise / h, rows[-1]
+    assert abs(ad - fd) <= 1e-4 * abs(fd) + noise / h, rows[-2]
+
+
+@pytest.mark.gpu
+def test_traj_grad_batch_equals_single(synth_dir):
+    """Three replicas (different seeds and ion counts) in two replica groups give
+    each replica the gradient it has alone; the packed dL/dx0 lands at each
+    replica's offset."""
+    systems = [load(synth_dir["small"], "small", seed=s, n_mg=m) for s, m in ((3, 10), (4, 20), (5, 0))]
+    ns = []
+    states = []
+    for s in systems:
+        e = Engine([s], precision=PREC_FP64)
+        e.populate_lists()
+        e.step(100)
+        e.sync()
+        states.append(e.get_states())
+        ns.append(states[-1]["x"].size)
+        e.close()
+    rng = np.random.default_rng(2)
+    seeds = [_loss_seed(n, rng) for n in ns]
+    single = []
+    for s, st, sd in zip(systems, states, seeds):
+        e = Engine([s], precision=PREC_FP64)
+        e.set_states(st)
+        single.append(e.traj_grad(15, 4, sd, want_state=True))
+        e.close()
+    e = Engine(systems, precision=PREC_FP64, groups=2)
+    e.set_states({k: np.concatenate([st[k] for st in states]) for k in STATE_NAMES})
+    seed = {k: np.concatenate([sd[k] for sd in seeds]) for k in seeds[0]}
+    dth, d0 = e.traj_grad(15, 4, seed, want_state=True)
+    e.close()
+    off = 0
+    for r, (g1, s1) in enumerate(single):
+        np.testing.assert_allclose(dth[r], g1[0], rtol=1e-8, atol=1e-10 * np.abs(g1[0]).max())
+        for k in STATE_NAMES:
+            np.testing.assert_allclose(d0[k][off:off + ns[r]], s1[k], rtol=1e-8,
+                                       atol=1e-10 * (np.abs(s1[k]).max() + 1e-300))
+        off += ns[r]
+
+
+@pytest.mark.gpu
+def test_traj_grad_mixed_forward_close_to_fp64(small, thermal):
+    """The mixed-precision forward (FP32 pair math, fixed-point sums) under the FP64
+    adjoint: the gradient differs from the FP64 path's by the trajectory's own
+    precision difference."""
+    th0 = params_of(small)
+    seed = _loss_seed(thermal["x"].size, np.random.default_rng(3))
+    out = {}
+    for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+        e = Engine([with_params(small, th0)], precision=prec)
+        e.set_states(thermal)
+        out[name] = e.traj_grad(40, 10, seed)[0]
+        e.close()
+    rel = np.abs(out["mixed"] - out["fp64"]) / np.maximum(np.abs(out["fp64"]), 1e-12)
+    print("mixed vs fp64 relative difference per parameter:", np.array2string(rel, precision=1))
+    big = np.abs(out["fp64"]) > 1e-3 * np.abs(out["fp64"]).max()
+    assert rel[big].max() < 1e-3
 
 
 @pytest.mark.gpu
@@ -153,7 +219,7 @@ def test_autograd_function_backward(small, thermal):
     loss = (fn.apply(theta, x0) * w).sum()
     loss.backward()
     j = 14  # lB
-    hj = 1e-5 * float(theta.detach()[j])
+    hj = 1e-3 * float(theta.detach()[j])
     with torch.no_grad():
         tp, tm = theta.detach().clone(), theta.detach().clone()
         tp[j] += hj
