@@ -615,6 +615,8 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
     d.C = h->C;
     d.fp64 = prm.precision == TIS_PREC_FP64;
     d.full_lists = prm.full_lists ? 1 : 0;
+    d.lanes_sr = prm.lanes_sr;
+    d.lanes_lr = prm.lanes_lr;
     d.noise = prm.noise;
     d.cap_sr = cap_sr;
     d.cap_lr = cap_lr;
@@ -1491,6 +1493,12 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     if (prm.sr <= 0) prm.sr = 12.0;
     if (prm.skin <= 0) prm.skin = 3.0;
     if (prm.groups < 0) return fail(TIS_ERR_ARG, "tis_create: negative group count");
+    if (prm.lanes_sr == 0) prm.lanes_sr = tis::kLanesSR;
+    if (prm.lanes_lr == 0) prm.lanes_lr = tis::kLanesLR;
+    if (prm.lanes_sr != 1 && prm.lanes_sr != 2 && prm.lanes_sr != 4)
+        return fail(TIS_ERR_ARG, "tis_create: lanes_sr %d is not 1, 2 or 4", prm.lanes_sr);
+    if (prm.lanes_lr != 2 && prm.lanes_lr != 4 && prm.lanes_lr != 8)
+        return fail(TIS_ERR_ARG, "tis_create: lanes_lr %d is not 2, 4 or 8", prm.lanes_lr);
     int G = prm.groups > 0 ? prm.groups : (3 * n_replicas + 15) / 16;  // about 5 1/3 replicas per group
     G = std::min(G, n_replicas);
     prm.groups = G;

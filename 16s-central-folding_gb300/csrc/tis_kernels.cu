@@ -1667,6 +1667,16 @@ void launch_ion_counts(const Dev &d, cudaStream_t s, int r, int nrna, int kind, 
 void launch_pair_sr(const Dev &d, cudaStream_t s, bool en, bool ex)
 {
     constexpr int L = kLanesSR, T = kBlock * kLanesSR;
+    if (!en && ex && d.lanes_sr == 2) {  // the step's SR launch in the other shapes (tis_run_params.lanes_sr)
+        if (d.fp64) k_pair<true, false, false, true, 2, 2 * kBlock><<<d.nblk, 2 * kBlock, 0, s>>>(d, 1);
+        else k_pair<false, false, false, true, 2, 2 * kBlock><<<d.nblk, 2 * kBlock, 0, s>>>(d, 1);
+        return;
+    }
+    if (!en && ex && d.lanes_sr == 4) {
+        if (d.fp64) k_pair<true, false, false, true, 4, 4 * kBlock><<<d.nblk, 4 * kBlock, 0, s>>>(d, 1);
+        else k_pair<false, false, false, true, 4, 4 * kBlock><<<d.nblk, 4 * kBlock, 0, s>>>(d, 1);
+        return;
+    }
     if (d.fp64) {
         if (en) k_pair<true, false, true, false, L, T><<<d.nblk, T, 0, s>>>(d, 1);
         else if (ex) k_pair<true, false, false, true, L, T><<<d.nblk, T, 0, s>>>(d, 1);
@@ -1682,6 +1692,16 @@ void launch_pair_lr(const Dev &d, cudaStream_t s, bool en, bool force_all)
 {
     constexpr int L = kLanesLR, T = kThreadsLR;
     const int fa = force_all ? 1 : 0;
+    if (!en && d.lanes_lr == 2) {  // the step's LR launch in the other shapes (tis_run_params.lanes_lr)
+        if (d.fp64) k_pair<true, true, false, false, 2, 2 * kBlock><<<d.nblk, 2 * kBlock, 0, s>>>(d, fa);
+        else k_pair<false, true, false, false, 2, 2 * kBlock><<<d.nblk, 2 * kBlock, 0, s>>>(d, fa);
+        return;
+    }
+    if (!en && d.lanes_lr == 8) {
+        if (d.fp64) k_pair<true, true, false, false, 8, 8 * kBlock><<<d.nblk, 8 * kBlock, 0, s>>>(d, fa);
+        else k_pair<false, true, false, false, 8, 8 * kBlock><<<d.nblk, 8 * kBlock, 0, s>>>(d, fa);
+        return;
+    }
     if (d.fp64) {
         if (en) k_pair<true, true, true, false, L, T><<<d.nblk, T, 0, s>>>(d, fa);
         else k_pair<true, true, false, false, L, T><<<d.nblk, T, 0, s>>>(d, fa);

@@ -59,6 +59,7 @@ struct Dev {
     double *shift;              // R x 3, recentring shift of the current step (adjust_box)
     const int *cell_rep;        // replica of every cell
     int *hb_rec;                // when not null: 1 per H-bond candidate formed after the step's Monte Carlo, else 0
+    int lanes_sr, lanes_lr;     // threads per particle of the step's SR (1, 2, 4) and LR (2, 4, 8) pair launches
 };
 
 // Adjoint work of one handle (tis_adjoint.cu).  Arrays of 3P or 9P values are

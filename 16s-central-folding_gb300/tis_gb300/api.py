@@ -41,7 +41,8 @@ class RunParams(C.Structure):
     _fields_ = [("precision", C.c_int32), ("noise", C.c_int32), ("sr", C.c_double), ("skin", C.c_double),
                 ("lr_interval", C.c_int32), ("cap_sr", C.c_int32), ("cap_lr", C.c_int32), ("device", C.c_int32),
                 ("use_graph", C.c_int32), ("graph_steps", C.c_int32), ("full_lists", C.c_int32),
-                ("groups", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("groups", C.c_int32), ("lanes_sr", C.c_int32), ("lanes_lr", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 _lib = None
@@ -106,6 +107,7 @@ def _declare(L):
         "tis_get_forces": [vp, i32, dp],
         "tis_pair_lists_noalloc": [vp, vp, vp, vp, C.c_int32, dp, C.c_double, C.c_double, vp, i64, vp, i64, vp, vp],
         "tis_param_grad": [vp, dp],
+        "tis_autotune": [C.POINTER(vp), i32, C.POINTER(RunParams), i64, cp, C.POINTER(RunParams), dp],
         "tis_traj_grad": [vp, i64, i32, C.POINTER(dp), dp, C.POINTER(dp)],
     }
     for name, args in sig.items():
@@ -122,7 +124,7 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_stack_energies", "tis_get_counters", "tis_get_info", "tis_replica_size", "tis_get_launch_count",
             "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc", "tis_set_states",
             "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
-            "tis_param_grad", "tis_traj_grad"]
+            "tis_param_grad", "tis_traj_grad", "tis_autotune"]
 
 
 def read_last_frame(path, n):
@@ -230,6 +232,18 @@ class System:
                 self.h = None
         except Exception:
             pass
+
+
+def autotune(systems, steps=300, cache=None, **params):
+    """Measured launch configuration for these replicas: (dict of the chosen
+    groups, graph_steps, lanes_sr, lanes_lr, replica-steps/s)."""
+    arr = (C.c_void_p * len(systems))(*[s.h.value for s in systems])
+    base = run_params(**params)
+    best = RunParams()
+    rate = C.c_double()
+    _check(lib().tis_autotune(arr, len(systems), C.byref(base), int(steps),
+                              os.fsencode(cache) if cache else None, C.byref(best), C.byref(rate)))
+    return {k: getattr(best, k) for k in ("groups", "graph_steps", "lanes_sr", "lanes_lr")}, rate.value
 
 
 def run_params(**kw):

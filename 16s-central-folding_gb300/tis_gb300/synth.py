@@ -74,7 +74,8 @@ def _direction(rng, prev_bond, theta, jitter):
     a = _unit(-prev_bond)
     tmp = rng.normal(size=3)
     p = _unit(tmp - tmp.dot(a) * a)
-    q = np.cross(a, p)
+    # a x p, as numpy.cross forms it (products, then one subtraction per component)
+    q = np.array([a[1] * p[2] - a[2] * p[1], a[2] * p[0] - a[0] * p[2], a[0] * p[1] - a[1] * p[0]])
     th = theta + rng.normal() * jitter
     phi = rng.uniform(0, 2 * np.pi)
     return np.cos(th) * a + np.sin(th) * (np.cos(phi) * p + np.sin(phi) * q)
@@ -86,13 +87,14 @@ def grow_chain(seq, rng, r_conf, min_sep=3.6, tries=400):
     n = len(seq)
     pos = []
     ids = []
+    buf = np.empty((3 * n, 3))  # pos as one array (rows [0, len(pos)))
 
     def ok(p, exclude):
         if np.linalg.norm(p) > r_conf:
             return False
         if not pos:
             return True
-        arr = np.asarray(pos)
+        arr = buf[:len(pos)]
         d2 = ((arr - p) ** 2).sum(1)
         if exclude:
             d2[list(exclude)] = 1e9
@@ -111,7 +113,7 @@ def grow_chain(seq, rng, r_conf, min_sep=3.6, tries=400):
         # crowded: give up the confinement but keep excluded volume if possible
         for _ in range(tries):
             p = origin + r0 * _unit(rng.normal(size=3))
-            arr = np.asarray(pos)
+            arr = buf[:len(pos)]
             d2 = ((arr - p) ** 2).sum(1)
             if exclude:
                 d2[list(exclude)] = 1e9
@@ -119,15 +121,19 @@ def grow_chain(seq, rng, r_conf, min_sep=3.6, tries=400):
                 return p
         return origin + r0 * _unit(rng.normal(size=3))
 
+    def add(p):
+        buf[len(pos)] = p
+        pos.append(p)
+
     s_prev = p_prev = None
     for t in range(n):
         b = seq[t]
         if t == 0:
             s = np.zeros(3)
-            pos.append(s)
+            add(s)
             sid = 0
             bpos = place(s, _R_SB[b], None, 0.0, {sid})
-            pos.append(bpos)
+            add(bpos)
             ids.append((-1, sid, sid + 1))
             s_prev, p_prev = s, None
             continue
@@ -138,12 +144,12 @@ def grow_chain(seq, rng, r_conf, min_sep=3.6, tries=400):
         # also stay apart, or the bond angle collapses onto its neighbour
         p = place(s_prev, _R_SP, prev_bond, theta, {sid_prev})
         pid = len(pos)
-        pos.append(p)
+        add(p)
         s = place(p, _R_PS, p - s_prev, _BETA1, {pid})
         sid = len(pos)
-        pos.append(s)
+        add(s)
         bpos = place(s, _R_SB[b], s - p, _ALPHA2[b], {sid})
-        pos.append(bpos)
+        add(bpos)
         ids.append((pid, sid, sid + 1))
         s_prev, p_prev = s, p
     return np.asarray(pos), ids

@@ -390,6 +390,38 @@ def gpu_arm(args):
                        "traj_grad_replica_steps_per_s": 16 * 200 / t_tg, "precision": "mixed forward, FP64 adjoint"}
             adj.close()
 
+        # the large system: a 1500-nt chain in a 600 A box with 1300 Mg, 22100 Cl,
+        # 21000 K (48,899 particles per replica), 16 replicas with independent seeds
+        # (one set-up, the seed varied), mixed precision, graphs of GRAPH_STEPS steps
+        large = None
+        if rank == 0 and args.large:
+            from tis_gb300 import System, synth
+            w = synth.WORKLOADS["large"]
+            lf = synth.generate(tmp, "large", w["n_nt"], seed=w["seed"], n_hb_pairs=w["n_hb_pairs"])
+            m, cl, kk = w["ions"]
+            base = System.load(lf["pdb"], lf["bonds"], lf["stacks"], lf["maxikey"], T=T_298, box=w["box"], rc=RC,
+                               n_mg=m, n_cl=cl, n_k=kk, seed=1, center=500, rng=1).to_dict()
+            reps = [System.from_arrays(dict(base, seed=np.array([s], dtype=np.int64))) for s in range(1, 17)]
+            le = Engine(reps, precision=PREC_MIXED, device=local, use_graph=1, graph_steps=GRAPH_STEPS)
+            le.populate_lists()
+            le.step(GRAPH_STEPS)
+            le.sync()
+            ls = torch.cuda.ExternalStream(le.stream())
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            LN = 3 * GRAPH_STEPS
+            with torch.cuda.stream(ls):
+                a0.record(ls)
+            le.step(LN)
+            with torch.cuda.stream(ls):
+                a1.record(ls)
+            le.sync()
+            torch.cuda.synchronize()
+            lms = a0.elapsed_time(a1)
+            large = {"workload": "16 replicas x 1500-nt chain (4499 beads), 600 A box, 1300 Mg / 22100 Cl / 21000 K",
+                     "particles_per_replica": le.n[0], "steps": LN, "ms_per_step": lms / LN,
+                     "replica_steps_per_s": 16 * LN / (lms / 1000.0), "precision": "mixed"}
+            le.close()
+
     if rank != 0:
         return
     cpu = cpu_sample(files_for_cpu(), replica_specs(), 2000, min(N_REPLICAS, os.cpu_count() or 1)) \
@@ -407,6 +439,7 @@ def gpu_arm(args):
             "batched_vs_plain": value / world / plain_sps,
             "stage_ms_per_step": stages,
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "adjoint": adjoint,
+            "large_system": large,
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
@@ -425,6 +458,8 @@ def main():
     ap.add_argument("--groups", type=int, default=0,
                     help="replica groups run concurrently (0: the library's default)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-large", dest="large", action="store_false",
+                    help="skip the large-system (48,899 particles x 16 replicas) throughput line")
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="stop after the timed loop (no e2e, stage timing, plain path): for profiler runs")
     args = ap.parse_args()

@@ -121,7 +121,10 @@ typedef struct tis_run_params {
                               the next rebuild */
     int32_t groups;        /* replica groups whose step graphs run concurrently on the GPU
                               (0: (3 n + 15) / 16 for n replicas, 12 for 64); results do not depend on it */
-    int32_t reserved[4];
+    int32_t lanes_sr;      /* threads per particle of the step's SR pair launch: 1, 2, 4 (0: 1) */
+    int32_t lanes_lr;      /* threads per particle of the step's LR pair launch: 2, 4, 8 (0: 4); in mixed
+                              precision results do not depend on either (fixed-point sums) */
+    int32_t reserved[2];
 } tis_run_params;
 
 int tis_run_params_default(tis_run_params *p);
@@ -250,6 +253,17 @@ int tis_get_launch_count(tis_handle *h, int64_t *n);
  * [1, 2^31-1].  The hydrogen-bond Monte Carlo (E:2251-2300) and full_forces
  * (E:2594-2606) consume it in the reference's order. */
 int tis_rand_stream(uint64_t seed, uint64_t first, int64_t n, int32_t *out);
+
+/* Measured choice of the launch configuration (no counterpart in the reference):
+ * replica groups, steps per captured graph and the threads per particle of the
+ * SR and LR pair launches, tuned one after another (coordinate descent) by timing
+ * `steps` graph-replayed steps (0: 300) of the given replicas with CUDA events on
+ * the handle's stream.  *best receives base with the chosen values and *rate (if
+ * not NULL) the measured replica-steps/s.  When `cache` names a file, a line for
+ * the same workload (replicas, particles, box, cutoff, precision, device) is
+ * reused without trials, and a new result is appended. */
+int tis_autotune(const tis_system *const *systems, int n_replicas, const tis_run_params *base, int64_t steps,
+                 const char *cache, tis_run_params *best, double *rate);
 
 /* ------------------------------------------------------------------------ */
 /* Parameter derivatives (no counterpart in the reference)                    */

@@ -876,6 +876,61 @@ void tis_o_terms(tis_o *o, double *f_sr, double *f_lr, double *f_bonded, double 
     if (e) memcpy(e, E, sizeof E);
 }
 
+static int cmp_i64(const void *a, const void *b)
+{
+    const int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
+    return x < y ? -1 : x > y;
+}
+
+/* F_sr + F_bonded of tis_o_terms (SR_interactions_lists E:1783-1847 and
+ * polymer_constraints E:2354-2520), summed with the LJ of each bonded pair
+ * weighted by one minus the number of bonded terms that name it instead of added
+ * in the pair sum and subtracted once per term (reduce_forces, E:880-897): the
+ * same force in exact arithmetic, without the cancellation of the two equal
+ * values, which loses the other pair forces of the bead when a folded 1-3 pair
+ * makes them reach 1e17 and more. */
+void tis_o_net_sr_bonded(tis_o *o, double *f)
+{
+    int n = o->d.n;
+    int64_t *key = (int64_t *)malloc(sizeof(int64_t) * (size_t)(o->d.n_bt > 0 ? o->d.n_bt : 1));
+    for (int t = 0; t < o->d.n_bt; ++t) {
+        int a = o->bt_a[t], b = o->bt_kind[t] == 0 ? o->bt_b[t] : o->bt_c[t];
+        int lo = a < b ? a : b, hi = a < b ? b : a;
+        key[t] = (int64_t)lo * n + hi;
+    }
+    qsort(key, (size_t)o->d.n_bt, sizeof(int64_t), cmp_i64);
+    zero3(o->fx, o->fy, o->fz, n);
+    double v[3];
+    for (int64_t p = 0; p < o->sr.n; p += 2) {
+        int i = o->sr.v[p], j = o->sr.v[p + 1];
+        int lo = i < j ? i : j, hi = i < j ? j : i;
+        int64_t k = (int64_t)lo * n + hi;
+        int mult = 0;
+        const int64_t *hit = (const int64_t *)bsearch(&k, key, (size_t)o->d.n_bt, sizeof(int64_t), cmp_i64);
+        if (hit) {
+            const int64_t *a = hit, *b = hit;
+            while (a > key && a[-1] == k) --a;
+            while (b + 1 < key + o->d.n_bt && b[1] == k) ++b;
+            mult = (int)(b - a) + 1;
+        }
+        int J = jn12(o->type[i], o->type[j]);
+        double r2 = image_r2(o, i, j, v);
+        double t = mult == 1 ? 0.0 : (1.0 - mult) * lj_force(o, r2, J);
+        if (charged(o, i) && charged(o, j)) t += coulomb_force(o, r2, J);
+        v[0] *= t; v[1] *= t; v[2] *= t;
+        o->fx[i] += v[0]; o->fx[j] -= v[0];
+        o->fy[i] += v[1]; o->fy[j] -= v[1];
+        o->fz[i] += v[2]; o->fz[j] -= v[2];
+    }
+    free(key);
+    for (int t = 0; t < o->d.n_bt; ++t) {
+        int a = o->bt_a[t], b = o->bt_b[t], c = o->bt_c[t];
+        if (o->bt_kind[t] == 0) bond_force(o, a, b, o->bt_k0[t], o->bt_x0[t]);
+        else angle_force(o, a, b, c, o->bt_k0[t], o->bt_x0[t], 0);
+    }
+    copy_f(o, o->fx, o->fy, o->fz, f);
+}
+
 void tis_o_last_energies(const tis_o *o, double *out5)
 {
     out5[0] = o->E2_HB; out5[1] = o->E3_HB; out5[2] = o->E2_STACK; out5[3] = o->E3_STACK;

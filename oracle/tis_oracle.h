@@ -66,6 +66,9 @@ void tis_o_get_hb(const tis_o *o, int32_t *status, int32_t *excess);
 /* per-term forces (3n each, may be NULL) and energies (TIS_O_NE) on the current state */
 void tis_o_terms(tis_o *o, double *f_sr, double *f_lr, double *f_bonded, double *f_stack,
                  double *f_hb, double *energies, int32_t *st_status);
+/* F_sr + F_bonded with each bonded pair's LJ weighted in the pair sum instead of
+ * added and subtracted (3n; see tis_oracle.c) */
+void tis_o_net_sr_bonded(tis_o *o, double *f);
 void tis_o_step(tis_o *o, int64_t nsteps);
 /* E2_HB, E3_HB, E2_STACK, E3_STACK, Rg of the last step */
 void tis_o_last_energies(const tis_o *o, double *out5);

@@ -203,6 +203,12 @@ class Oracle:
         out["st_status"] = sts[: self.n_st]
         return out
 
+    def net_sr_bonded(self):
+        """F_sr + F_bonded without adding and subtracting the bonded pairs' LJ."""
+        f = np.zeros(3 * self.n)
+        self.lib.tis_o_net_sr_bonded(self.h, _p(f, C.c_double))
+        return f
+
     def step(self, n):
         self.lib.tis_o_step(self.h, C.c_int64(n))
 
