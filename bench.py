@@ -227,7 +227,7 @@ def gpu_arm(args):
     import numpy as np
     import torch
 
-    from tis_gb300 import PREC_FP64, PREC_MIXED, Engine
+    from tis_gb300 import PREC_FP64, PREC_MIXED, Engine, autotune
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -243,17 +243,27 @@ def gpu_arm(args):
         for sp in specs:
             sp["seed"] += 100000 * rank
         systems = load_systems(files, specs)
-        eng = Engine(systems, precision=PREC_MIXED, device=local, use_graph=1, graph_steps=GRAPH_STEPS,
-                     groups=args.groups)
+        # the launch configuration: measured by tis_autotune (replica groups, steps per
+        # graph, threads per particle of the pair launches; 1000 steps per trial), or
+        # fixed by --groups
+        tune = {"groups": args.groups, "graph_steps": args.graph_steps, "lanes_sr": args.lanes_sr,
+                "lanes_lr": args.lanes_lr}
+        tune_s = None
+        if args.groups == 0:
+            t0 = time.perf_counter()
+            tune, _ = autotune(systems, steps=1000, precision=PREC_MIXED, device=local)
+            tune_s = time.perf_counter() - t0
+        eng = Engine(systems, precision=PREC_MIXED, device=local, use_graph=1, **tune)
+        graph_steps = eng.params.graph_steps
         eng.populate_lists()
         stream = torch.cuda.ExternalStream(eng.stream())
         flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
         K = max(1, args.steps)
         W = max(3, args.warmup)
         eng.step(W)                # W warm-up steps (direct launches) ...
-        eng.step(GRAPH_STEPS)      # ... and one graph replay, so capture happens before timing
+        eng.step(graph_steps)      # ... and one graph replay, so capture happens before timing
         eng.sync()
-        chunks = [GRAPH_STEPS] * (K // GRAPH_STEPS) + ([K % GRAPH_STEPS] if K % GRAPH_STEPS else [])
+        chunks = [graph_steps] * (K // graph_steps) + ([K % graph_steps] if K % graph_steps else [])
         iters = len(chunks)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(iters)]
         if world > 1:
@@ -292,7 +302,7 @@ def gpu_arm(args):
         # every replica) is read back into pinned host memory
         e2e = None
         if rank == 0:
-            E2E_STEPS = 100
+            E2E_STEPS = max(100, graph_steps)  # whole graphs between frames
             n_it = max(1, min(10, K // E2E_STEPS))
             state = eng.get_states()
             pinned = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in state.items()}
@@ -432,9 +442,12 @@ def gpu_arm(args):
             "config": {"workload": "64 replicas x 346-nt TIS chain (1037 beads) + Mg 0-20 mM sweep, 76 mM KCl, "
                                    "350 A box, T 298 K, rc 30 A",
                        "replicas_per_gpu": N_REPLICAS, "particles_per_gpu": n_part, "precision": "mixed",
-                       "graph_steps": GRAPH_STEPS, "replica_groups": eng.params.groups or (3 * N_REPLICAS + 15) // 16,
+                       "graph_steps": graph_steps, "replica_groups": eng.params.groups or (3 * N_REPLICAS + 15) // 16,
+                       "lanes_sr": eng.params.lanes_sr or 1, "lanes_lr": eng.params.lanes_lr or 4,
+                       "launch_config": "tis_autotune (1000 steps per trial)" if tune_s is not None else "--groups",
+                       "autotune_s": tune_s,
                        "l2": "flushed (256 MB write) between timed iterations of "
-                                                         f"{GRAPH_STEPS} steps", "parallelism": f"replicas x{world}"},
+                                                         f"{graph_steps} steps", "parallelism": f"replicas x{world}"},
             "plain_fp64_single_replica_steps_per_s": plain_sps,
             "batched_vs_plain": value / world / plain_sps,
             "stage_ms_per_step": stages,
@@ -456,7 +469,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--groups", type=int, default=0,
-                    help="replica groups run concurrently (0: the library's default)")
+                    help="fixed launch configuration: replica groups run concurrently (0: tis_autotune chooses "
+                         "groups, steps per graph and pair-launch shapes)")
+    ap.add_argument("--graph-steps", type=int, default=GRAPH_STEPS, help="steps per graph with --groups")
+    ap.add_argument("--lanes-sr", type=int, default=1, help="SR pair threads per particle with --groups")
+    ap.add_argument("--lanes-lr", type=int, default=4, help="LR pair threads per particle with --groups")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the large-system (48,899 particles x 16 replicas) throughput line")
