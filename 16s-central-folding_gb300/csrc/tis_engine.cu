@@ -1668,6 +1668,152 @@ int tis_ion_counts(tis_handle *h, int r, int kind, double radius, int32_t *count
     return grp_ion_counts(g, loc, kind, radius, counts, cap, n_p, total);
 }
 
+}  // extern "C"
+
+struct tis_density {
+    tis_handle *h = nullptr;
+    Group *g = nullptr;
+    int loc = 0, kind = 0, n = 0, n_fit = 0;
+    double lo[3] = {0, 0, 0}, delta = 1;
+    int dims[3] = {0, 0, 0};
+    int *d_idx = nullptr;
+    double *d_ref = nullptr, *d_fit = nullptr;
+    unsigned long long *d_grid = nullptr;
+    int64_t frames = 0;
+    size_t cells() const { return (size_t)dims[0] * dims[1] * dims[2]; }
+    ~tis_density()
+    {
+        for (void *p : {(void *)d_idx, (void *)d_ref, (void *)d_fit, (void *)d_grid})
+            if (p) cudaFree(p);
+    }
+};
+
+extern "C" {
+
+int tis_density_create(tis_handle *h, int r, int kind, const double lo[3], double delta, const int32_t dims[3],
+                       int32_t n_fit, const int32_t *fit_beads, const double *fit_ref, tis_density **out)
+{
+    if (!out || !lo || !dims) return fail(TIS_ERR_ARG, "tis_density_create: bad argument");
+    *out = nullptr;
+    Group *g;
+    int loc, rc = locate(h, r, &g, &loc);
+    if (rc) return rc;
+    if (!(delta > 0) || dims[0] < 1 || dims[1] < 1 || dims[2] < 1 ||
+        (double)dims[0] * dims[1] * dims[2] > 2147483647.0)
+        return fail(TIS_ERR_ARG, "tis_density_create: bad grid (delta %g, dims %d %d %d)", delta, dims[0], dims[1], dims[2]);
+    if (kind < 0 || kind > 255) return fail(TIS_ERR_ARG, "tis_density_create: kind %d", kind);
+    const RepHost &hr = g->rep[loc];
+    if (n_fit < 0 || (n_fit > 0 && (!fit_beads || !fit_ref)) || n_fit == 1 || n_fit == 2)
+        return fail(TIS_ERR_ARG, "tis_density_create: a fit needs at least three beads and their reference positions");
+    for (int i = 0; i < n_fit; ++i)
+        if (fit_beads[i] < 0 || fit_beads[i] >= hr.n) return fail(TIS_ERR_ARG, "tis_density_create: fit bead %d", fit_beads[i]);
+    TIS_CUDA(cudaSetDevice(h->prm.device));
+    tis_density *d = new tis_density();
+    d->h = h;
+    d->g = g;
+    d->loc = loc;
+    d->kind = kind;
+    d->n = hr.n;
+    d->n_fit = n_fit;
+    d->delta = delta;
+    for (int a = 0; a < 3; ++a) {
+        d->lo[a] = lo[a];
+        d->dims[a] = dims[a];
+    }
+    auto bail = [&](cudaError_t e) {
+        delete d;
+        return fail(TIS_ERR_NOMEM, "tis_density_create: %s", cudaGetErrorString(e));
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc((void **)&d->d_grid, sizeof(unsigned long long) * d->cells())) != cudaSuccess ||
+        (e = cudaMalloc((void **)&d->d_fit, sizeof(double) * 16)) != cudaSuccess ||
+        (e = cudaMemset(d->d_grid, 0, sizeof(unsigned long long) * d->cells())) != cudaSuccess ||
+        (e = cudaMemset(d->d_fit, 0, sizeof(double) * 16)) != cudaSuccess)
+        return bail(e);
+    if (n_fit > 0) {
+        if ((e = cudaMalloc((void **)&d->d_idx, sizeof(int) * n_fit)) != cudaSuccess ||
+            (e = cudaMalloc((void **)&d->d_ref, sizeof(double) * 3 * n_fit)) != cudaSuccess ||
+            (e = cudaMemcpy(d->d_idx, fit_beads, sizeof(int) * n_fit, cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (e = cudaMemcpy(d->d_ref, fit_ref, sizeof(double) * 3 * n_fit, cudaMemcpyHostToDevice)) != cudaSuccess)
+            return bail(e);
+    }
+    *out = d;
+    return TIS_OK;
+}
+
+int tis_density_add(tis_density *d)
+{
+    if (!d) return fail(TIS_ERR_ARG, "tis_density_add: null grid");
+    TIS_CUDA(cudaSetDevice(d->h->prm.device));
+    const tis::Dev &dev = d->g->dev;
+    if (d->n_fit > 0) tis::launch_fit(dev, d->h->stream, d->loc, d->n_fit, d->d_idx, d->d_ref, d->d_fit);
+    tis::launch_density(dev, d->h->stream, d->loc, d->n, d->kind, d->n_fit > 0 ? d->d_fit : nullptr, d->lo, d->delta,
+                        d->dims, d->d_grid);
+    TIS_CUDA(cudaGetLastError());
+    ++d->frames;
+    return TIS_OK;
+}
+
+int tis_density_get(tis_density *d, double *counts, int64_t cap, int64_t *frames, double *rmsd)
+{
+    if (!d) return fail(TIS_ERR_ARG, "tis_density_get: null grid");
+    TIS_CUDA(cudaSetDevice(d->h->prm.device));
+    std::vector<unsigned long long> c(d->cells());
+    double fit[16];
+    TIS_CUDA(cudaMemcpyAsync(c.data(), d->d_grid, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost, d->h->stream));
+    TIS_CUDA(cudaMemcpyAsync(fit, d->d_fit, sizeof fit, cudaMemcpyDeviceToHost, d->h->stream));
+    TIS_CUDA(cudaStreamSynchronize(d->h->stream));
+    if (counts)
+        for (size_t i = 0; i < c.size() && (int64_t)i < cap; ++i) counts[i] = (double)c[i];
+    if (frames) *frames = d->frames;
+    if (rmsd) *rmsd = d->n_fit > 0 ? fit[15] : 0.0;
+    return TIS_OK;
+}
+
+int tis_density_write_dx(tis_density *d, const char *path)
+{
+    if (!d || !path) return fail(TIS_ERR_ARG, "tis_density_write_dx: bad argument");
+    std::vector<double> c(d->cells());
+    int64_t frames = 0;
+    int rc = tis_density_get(d, c.data(), (int64_t)c.size(), &frames, nullptr);
+    if (rc) return rc;
+    FILE *f = fopen(path, "w");
+    if (!f) return fail(TIS_ERR_IO, "cannot open %s", path);
+    const int *n = d->dims;
+    fprintf(f, "# OpenDX grid: ion counts of kind %d accumulated over %lld frames\n", d->kind, (long long)frames);
+    fprintf(f, "# bins of %g A; the origin is the centre of bin (0, 0, 0)\n", d->delta);
+    fprintf(f, "# values follow the grid positions with the last index (z) varying fastest,\n");
+    fprintf(f, "# then y, then x\n");
+    fprintf(f, "# written by tis_density_write_dx\n");
+    fprintf(f, "# (no comment lines below this one)\n");
+    fprintf(f, "object 1 class gridpositions counts %d %d %d\n", n[0], n[1], n[2]);
+    fprintf(f, "origin %.6f %.6f %.6f\n", d->lo[0] + 0.5 * d->delta, d->lo[1] + 0.5 * d->delta, d->lo[2] + 0.5 * d->delta);
+    fprintf(f, "delta %.6f 0.000000 0.000000\n", d->delta);
+    fprintf(f, "delta 0.000000 %.6f 0.000000\n", d->delta);
+    fprintf(f, "delta 0.000000 0.000000 %.6f\n", d->delta);
+    fprintf(f, "object 2 class gridconnections counts %d %d %d\n", n[0], n[1], n[2]);
+    fprintf(f, "object 3 class array type \"double\" rank 0 items %zu data follows\n", c.size());
+    for (size_t i = 0; i < c.size(); ++i) fprintf(f, (i % 3 == 2 || i + 1 == c.size()) ? "%.7g\n" : "%.7g ", c[i]);
+    fprintf(f, "attribute \"dep\" string \"positions\"\n");
+    fprintf(f, "object \"density\" class field\n");
+    fprintf(f, "component \"positions\" value 1\n");
+    fprintf(f, "component \"connections\" value 2\n");
+    fprintf(f, "component \"data\" value 3\n");
+    const bool ok = !ferror(f);
+    fclose(f);
+    return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
+}
+
+int tis_density_destroy(tis_density *d)
+{
+    if (d) {
+        cudaSetDevice(d->h->prm.device);
+        cudaStreamSynchronize(d->h->stream);
+        delete d;
+    }
+    return TIS_OK;
+}
+
 int tis_get_hb_status(tis_handle *h, int r, int32_t *status, int32_t *excess)
 {
     Group *g;

@@ -136,6 +136,14 @@ void launch_force_all_rebuild(const Dev &d, cudaStream_t s);
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out);
 int kernel_launches_per_step();
 
+// ion density grids (tis_density.cu): the least-squares fit of replica r's beads idx
+// (replica-local) onto ref (3 per bead) into out[16] (R, frame centroid, reference
+// centroid, rmsd); every particle of `kind` of replica r (n particles), moved by the
+// fit when fit != null, binned into grid (dims[0] x dims[1] x dims[2], z fastest)
+void launch_fit(const Dev &d, cudaStream_t s, int r, int n_fit, const int *idx, const double *ref, double *out);
+void launch_density(const Dev &d, cudaStream_t s, int r, int n, int kind, const double *fit, const double lo[3],
+                    double delta, const int dims[3], unsigned long long *grid);
+
 // adjoint (tis_adjoint.cu).  mode 0: dU/dtheta into a.dth at positions a.px..;
 // mode 1: a.jv += J tan and the parameter terms of lambda = tan.
 void launch_adj_pair(const Dev &d, const AdjDev &a, cudaStream_t s, bool lr, const double *tan, int mode);

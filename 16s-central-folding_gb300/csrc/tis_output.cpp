@@ -74,4 +74,131 @@ int tis_read_last_frame(const char *coordinates, int n, double *x, double *y, do
     return TIS_OK;
 }
 
+namespace {
+
+int64_t sys_i64(const tis_system *s, const char *name, int64_t def)
+{
+    const tis::Array *a = s->get(name);
+    if (!a || a->count() < 1) return def;
+    if (a->dtype == TIS_I64) return a->as<int64_t>()[0];
+    if (a->dtype == TIS_I32) return a->as<int32_t>()[0];
+    return (int64_t)a->as<double>()[0];
+}
+
+bool put_i32(FILE *f, int32_t v) { return fwrite(&v, 4, 1, f) == 1; }
+
+}  // namespace
+
+int tis_write_psf(const tis_system *s, const char *path)
+{
+    if (!s || !path) return fail(TIS_ERR_ARG, "tis_write_psf: bad argument");
+    const int n = (int)sys_i64(s, "n_particles", -1), ntp = (int)sys_i64(s, "n_rna", -1);
+    const tis::Array *type = s->get("type"), *kind = s->get("kind");
+    if (n < 1 || ntp < 1 || ntp > n || !type || !kind || type->dtype != TIS_I32 || kind->dtype != TIS_I32 ||
+        type->count() != n || kind->count() != n)
+        return fail(TIS_ERR_ARG, "tis_write_psf: the system lacks n_particles, n_rna, type or kind");
+    const int32_t *ty = type->as<int32_t>(), *kd = kind->as<int32_t>();
+    // the nucleotide letter of bead i (1-based): its base bead's type (3 A, 4 G, 5 C, 6 U)
+    auto letter = [&](int i) {
+        const int b = 3 * (i / 3) + 1;  // 0-based index of the base bead of nucleotide i / 3 + 1
+        const int t = b < ntp ? ty[b] : 0;
+        return t == 3 ? 'A' : t == 4 ? 'G' : t == 5 ? 'C' : t == 6 ? 'U' : 'N';
+    };
+    FILE *f = fopen(path, "w");
+    if (!f) return fail(TIS_ERR_IO, "cannot open %s", path);
+    // the layout of the reference's topology exporter (analysis/make_ninfo/16SCD_ninfo.cpp:6563-6650)
+    fprintf(f, "%8i !NATOM\n", n);
+    for (int i = 1; i <= ntp; ++i) {
+        const char c = letter(i);
+        fprintf(f, "%8iR%c %4i      R%c", i, c, i / 3 + 1, c);
+        if (i % 3 == 1) fprintf(f, "    S   S     %11.6f%14.4f", 0.0, 10.0);
+        else if (i % 3 == 2) fprintf(f, "    %cb  B     %11.6f%14.4f", c, 0.0, 10.0);
+        else fprintf(f, "    P   P     %11.6f%14.4f", -1.0, 10.0);
+        fprintf(f, "           0\n");
+    }
+    for (int i = ntp + 1; i <= n; ++i) {
+        const int k = kd[i - 1];  // part_key: 3 Mg, 4 Cl, 5 K
+        const char *nm = k == 3 ? "Mg " : k == 4 ? "Cl " : "K  ";
+        const char *r2 = k == 3 ? "Mg" : k == 4 ? "Cl" : "K ";
+        const double q = k == 3 ? 2.0 : k == 4 ? -1.0 : 1.0;
+        fprintf(f, "%8i%s%4i      %s    %s  %s    %11.6f%14.4f           0\n", i, nm, ntp / 3 + i - ntp + 1, r2, r2,
+                r2, q, 10.0);
+    }
+    fprintf(f, "%8i !NBOND\n", ntp - 1);
+    int col = 0;
+    for (int i = 2; i <= ntp; ++i) {  // P-S, S-B of a nucleotide; S-P to the next one
+        fprintf(f, "%8i%8i", i % 3 == 0 ? i - 2 : i - 1, i);
+        if (++col == 4) {
+            fprintf(f, "\n");
+            col = 0;
+        }
+    }
+    const bool ok = !ferror(f);
+    fclose(f);
+    return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
+}
+
+int tis_write_dcd(tis_handle *h, int replica, const char *path, int32_t nsavc, double delta)
+{
+    if (!h || !path || nsavc < 1) return fail(TIS_ERR_ARG, "tis_write_dcd: bad argument");
+    int n = 0, rc;
+    if ((rc = tis_replica_size(h, replica, &n))) return rc;
+    std::vector<double> x(n), y(n), z(n);
+    if ((rc = tis_get_state(h, replica, x.data(), y.data(), z.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
+                            nullptr)))
+        return rc;
+    FILE *f = fopen(path, "r+b");
+    int32_t nset = 0;
+    if (f) {
+        char head[8];
+        if (fread(head, 1, 8, f) != 8 || memcmp(head + 4, "CORD", 4) != 0 || fread(&nset, 4, 1, f) != 1) {
+            fclose(f);
+            return fail(TIS_ERR_FORMAT, "%s: not a DCD file written here", path);
+        }
+        int32_t natom = 0;  // record 3, after the 84-byte control record and the title record
+        int32_t tlen = 0;
+        if (fseek(f, 4 + 84 + 4, SEEK_SET) || fread(&tlen, 4, 1, f) != 1 || fseek(f, tlen + 4 + 4, SEEK_CUR) ||
+            fread(&natom, 4, 1, f) != 1 || natom != n) {
+            fclose(f);
+            return fail(TIS_ERR_FORMAT, "%s: %d atoms, the replica has %d", path, natom, n);
+        }
+        fseek(f, 0, SEEK_END);
+    } else {
+        f = fopen(path, "w+b");
+        if (!f) return fail(TIS_ERR_IO, "cannot open %s", path);
+        // CHARMM/NAMD DCD: control record (NSET, ISTART, NSAVC, NSTEP, ..., DELTA, ..., version 24)
+        int32_t ic[20] = {0};
+        ic[1] = nsavc;
+        ic[2] = nsavc;
+        const float dt = (float)delta;
+        memcpy(&ic[9], &dt, 4);
+        ic[19] = 24;
+        bool ok = put_i32(f, 84) && fwrite("CORD", 1, 4, f) == 4 && fwrite(ic, 4, 20, f) == 20 && put_i32(f, 84);
+        char title[2][80];
+        memset(title, ' ', sizeof title);
+        const char *t0 = "REMARKS TIS-RNA Langevin engine (GB300)";
+        memcpy(title[0], t0, strlen(t0));
+        char t1[81];
+        snprintf(t1, sizeof t1, "REMARKS replica %d, a frame every %d steps", replica, nsavc);
+        memcpy(title[1], t1, strlen(t1));
+        ok = ok && put_i32(f, 4 + 160) && put_i32(f, 2) && fwrite(title, 1, 160, f) == 160 && put_i32(f, 4 + 160);
+        ok = ok && put_i32(f, 4) && put_i32(f, n) && put_i32(f, 4);
+        if (!ok) {
+            fclose(f);
+            return fail(TIS_ERR_IO, "short write to %s", path);
+        }
+    }
+    std::vector<float> buf(n);
+    bool ok = true;
+    for (const std::vector<double> *a : {&x, &y, &z}) {
+        for (int i = 0; i < n; ++i) buf[i] = (float)(*a)[i];
+        ok = ok && put_i32(f, 4 * n) && fwrite(buf.data(), 4, n, f) == (size_t)n && put_i32(f, 4 * n);
+    }
+    ++nset;
+    const int32_t nstep = nset * nsavc;
+    ok = ok && fseek(f, 8, SEEK_SET) == 0 && put_i32(f, nset) && fseek(f, 8 + 12, SEEK_SET) == 0 && put_i32(f, nstep);
+    fclose(f);
+    return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
+}
+
 }  // extern "C"

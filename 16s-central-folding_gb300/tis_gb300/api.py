@@ -108,6 +108,13 @@ def _declare(L):
         "tis_pair_lists_noalloc": [vp, vp, vp, vp, C.c_int32, dp, C.c_double, C.c_double, vp, i64, vp, i64, vp, vp],
         "tis_param_grad": [vp, dp],
         "tis_autotune": [C.POINTER(vp), i32, C.POINTER(RunParams), i64, cp, C.POINTER(RunParams), dp],
+        "tis_density_create": [vp, i32, i32, dp, C.c_double, ip, i32, ip, dp, C.POINTER(vp)],
+        "tis_density_add": [vp],
+        "tis_density_get": [vp, dp, i64, C.POINTER(C.c_int64), dp],
+        "tis_density_write_dx": [vp, cp],
+        "tis_density_destroy": [vp],
+        "tis_write_psf": [vp, cp],
+        "tis_write_dcd": [vp, i32, cp, i32, C.c_double],
         "tis_traj_grad": [vp, i64, i32, C.POINTER(dp), dp, C.POINTER(dp)],
     }
     for name, args in sig.items():
@@ -124,7 +131,8 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_stack_energies", "tis_get_counters", "tis_get_info", "tis_replica_size", "tis_get_launch_count",
             "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc", "tis_set_states",
             "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
-            "tis_param_grad", "tis_traj_grad", "tis_autotune"]
+            "tis_param_grad", "tis_traj_grad", "tis_autotune", "tis_density_create", "tis_density_add",
+            "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd"]
 
 
 def read_last_frame(path, n):
@@ -225,6 +233,10 @@ class System:
     def to_dict(self):
         return {k: self[k] for k in self.names()}
 
+    def write_psf(self, path):
+        """The topology in the PSF layout of the reference's exporter (tis_write_psf)."""
+        _check(lib().tis_write_psf(self.h, os.fsencode(path)))
+
     def __del__(self):
         try:
             if self.h:
@@ -244,6 +256,52 @@ def autotune(systems, steps=300, cache=None, **params):
     _check(lib().tis_autotune(arr, len(systems), C.byref(base), int(steps),
                               os.fsencode(cache) if cache else None, C.byref(best), C.byref(rate)))
     return {k: getattr(best, k) for k in ("groups", "graph_steps", "lanes_sr", "lanes_lr")}, rate.value
+
+
+class Density:
+    """Ion counts of one kind of one replica binned over frames on the device."""
+
+    def __init__(self, engine, r, kind, lo, delta, dims, fit_beads=None, fit_ref=None):
+        self.engine = engine  # the handle must outlive the grid
+        self.dims = tuple(int(v) for v in dims)
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        dm = np.ascontiguousarray(self.dims, dtype=np.int32)
+        nf = 0
+        fb = fr = None
+        if fit_beads is not None:
+            fb = np.ascontiguousarray(fit_beads, dtype=np.int32)
+            fr = np.ascontiguousarray(fit_ref, dtype=np.float64).reshape(-1)
+            nf = fb.size
+        out = C.c_void_p()
+        _check(lib().tis_density_create(engine.h, r, kind, _dp(lo), float(delta), dm.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        nf, fb.ctypes.data_as(C.POINTER(C.c_int32)) if fb is not None else None,
+                                        _dp(fr) if fr is not None else None, C.byref(out)))
+        self.h = out
+
+    def add(self):
+        _check(lib().tis_density_add(self.h))
+
+    def get(self):
+        """(counts array of dims, frames, rmsd of the last fit)."""
+        c = np.zeros(self.dims)
+        fr = C.c_int64()
+        rm = C.c_double()
+        _check(lib().tis_density_get(self.h, _dp(c), c.size, C.byref(fr), C.byref(rm)))
+        return c, fr.value, rm.value
+
+    def write_dx(self, path):
+        _check(lib().tis_density_write_dx(self.h, os.fsencode(path)))
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().tis_density_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def run_params(**kw):
@@ -339,6 +397,14 @@ class Engine:
             dps = (C.POINTER(C.c_double) * 9)(*[_dp(d0[k]) for k in STATE_NAMES])
         _check(lib().tis_traj_grad(self.h, int(steps), int(checkpoint_every), seeds, _dp(out), dps))
         return (out, d0) if want_state else out
+
+    def write_dcd(self, r, path, nsavc, delta=0.05):
+        """Appends replica r's positions as one DCD frame (tis_write_dcd)."""
+        _check(lib().tis_write_dcd(self.h, r, os.fsencode(path), int(nsavc), float(delta)))
+
+    def density(self, r, kind, lo, delta, dims, fit_beads=None, fit_ref=None):
+        """A device-side ion density grid of replica r (tis_density_create)."""
+        return Density(self, r, kind, lo, delta, dims, fit_beads, fit_ref)
 
     def all_energies(self, out=None):
         """(replicas, 5) array of tis_get_energies' five values for every replica."""

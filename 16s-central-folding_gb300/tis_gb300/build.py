@@ -10,7 +10,7 @@ LIB = os.path.join(OUT, "libtis_gpu.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["tis_kernels.cu", "tis_engine.cu", "tis_system.cpp", "tis_loader.cpp", "tis_noalloc.cu", "tis_output.cpp",
-           "tis_adjoint.cu", "tis_autotune.cpp"]
+           "tis_adjoint.cu", "tis_autotune.cpp", "tis_density.cu"]
 RUN = os.path.join(OUT, "tis_run")  # the command-line program (csrc/tis_run.cpp) over the library
 
 

@@ -216,6 +216,41 @@ int tis_get_all_energies(tis_handle *h, double *out);
 int tis_ion_counts(tis_handle *h, int replica, int kind, double radius, int32_t *counts, int64_t cap,
                    int64_t *n_p, int32_t *total);
 
+/* Topology and trajectory files for analysis tools (the reference's
+ * analysis/make_ninfo/16SCD_ninfo.cpp:6563-6650 writes the PSF; its analyses read
+ * DCD trajectories).  tis_write_psf: the system's beads and ions with the
+ * exporter's names, residue numbers, charges and masses, and the chain's P-S, S-B,
+ * S-P bonds.  tis_write_dcd: appends the replica's current positions as one
+ * CHARMM/NAMD DCD frame (single precision), writing the header first when the
+ * file does not exist and updating its frame count; nsavc: steps per frame,
+ * delta: the time step in the header. */
+int tis_write_psf(const tis_system *s, const char *path);
+int tis_write_dcd(tis_handle *h, int replica, const char *path, int32_t nsavc, double delta);
+
+/* Ion density grid of one replica accumulated on the device over frames (the
+ * reference's analysis/Mg_distribution_3D/calc_Mg_density.py:118-150, which bins
+ * Mg positions read back from trajectory files with numpy.histogramdd, after
+ * bestfit_motifs.py:51-58 superposed each frame on a reference structure by the
+ * beads of a motif).  Bins of `delta` A from the lower corner lo, dims[0] x dims[1]
+ * x dims[2] of them (the upper faces belong to the last bins).  With n_fit > 0
+ * each frame is first superposed, by the least-squares rotation and translation
+ * of beads fit_beads[] (replica-local indices) onto fit_ref[3 * i ..], and the
+ * ions are moved with it.  tis_density_add bins the replica's current frame on
+ * the handle's stream (no host synchronisation); tis_density_get returns the
+ * counts (x slowest, z fastest), the frames added and the last fit's rmsd. */
+typedef struct tis_density tis_density;
+int tis_density_create(tis_handle *h, int replica, int kind, const double lo[3], double delta,
+                       const int32_t dims[3], int32_t n_fit, const int32_t *fit_beads, const double *fit_ref,
+                       tis_density **out);
+int tis_density_add(tis_density *g);
+int tis_density_get(tis_density *g, double *counts, int64_t cap, int64_t *frames, double *rmsd);
+/* The grid as an OpenDX file (the format calc_Mg_density.py exports and
+ * search_dx_maxvalue.py reads): six comment lines, the gridpositions object with
+ * the origin at the centre of the first bin, three delta lines, the
+ * gridconnections object, the data array of counts three per line, the field. */
+int tis_density_write_dx(tis_density *g, const char *path);
+int tis_density_destroy(tis_density *g);
+
 /* Appends one frame of a replica to the reference's three output files (any may
  * be NULL): the Contacts file ("%+.3f " per tertiary stack energy, then a
  * newline, E:6290-6294), the Coordinates file (x, y, z, each as the reference's

@@ -113,3 +113,79 @@ def test_ion_counts_match_a_direct_count(kind, radius):
     within = r2 <= radius * radius
     assert np.array_equal(counts, within.sum(1))
     assert total == int(within.any(0).sum())
+
+
+def test_psf_matches_the_exporter_layout(tmp_path):
+    """tis_write_psf: the layout of the reference's topology exporter
+    (analysis/make_ninfo/16SCD_ninfo.cpp:6563-6650): atom records with residue
+    names R<base>, atom names S / <base>b / P and ions, charges, the chain bonds."""
+    s = load(golden_inputs(), "small")
+    p = str(tmp_path / "t.psf")
+    s.write_psf(p)
+    lines = open(p).read().split("\n")
+    n, ntp = int(s["n_particles"][0]), int(s["n_rna"][0])
+    assert lines[0] == f"{n:8d} !NATOM"
+    atoms = lines[1:1 + n]
+    letter = {3: "A", 4: "G", 5: "C", 6: "U"}
+    typ, kind = s["type"], s["kind"]
+    for i in range(1, ntp + 1):
+        a = atoms[i - 1]
+        c = letter[typ[3 * (i // 3) + 1]]
+        assert int(a[:8]) == i and a[8:11] == f"R{c} " and int(a[11:15]) == i // 3 + 1
+        assert a[15:23] == f"      R{c}"
+        name = a[23:29].strip()
+        assert name == ("S" if i % 3 == 1 else f"{c}b" if i % 3 == 2 else "P")
+        assert float(a[37:48]) == (-1.0 if i % 3 == 0 else 0.0) and float(a[48:62]) == 10.0
+        assert a.endswith("           0")
+    charges = {3: 2.0, 4: -1.0, 5: 1.0}
+    for i in range(ntp + 1, n + 1):
+        a = atoms[i - 1]
+        assert float(a[37:48]) == charges[kind[i - 1]]
+        assert int(a[11:15]) == ntp // 3 + i - ntp + 1
+    assert lines[1 + n] == f"{ntp - 1:8d} !NBOND"
+    ints = [int(t) for ln in lines[2 + n:] for t in [ln[k:k + 8] for k in range(0, len(ln), 8)] if t.strip()]
+    pairs = list(zip(ints[0::2], ints[1::2]))
+    assert len(pairs) == ntp - 1
+    assert pairs[0] == (1, 2) and pairs[1] == (1, 3) and pairs[2] == (3, 4) and pairs[3] == (4, 5)
+
+
+def _read_dcd(path):
+    """Frames of a CHARMM/NAMD DCD file: (n_set, natom, [frames of (3, natom) float32])."""
+    raw = open(path, "rb").read()
+    i32 = lambda o: int(np.frombuffer(raw, np.int32, 1, o)[0])
+    assert i32(0) == 84 and raw[4:8] == b"CORD" and i32(88) == 84
+    nset, nsavc = i32(8), i32(16)
+    o = 92
+    tlen = i32(o)
+    o += 4 + tlen + 4
+    assert i32(o) == 4
+    natom = i32(o + 4)
+    o += 12
+    frames = []
+    while o < len(raw):
+        xyz = []
+        for _ in range(3):
+            assert i32(o) == 4 * natom
+            xyz.append(np.frombuffer(raw, np.float32, natom, o + 4))
+            o += 4 * natom + 8
+        frames.append(np.stack(xyz))
+    return nset, nsavc, natom, frames
+
+
+@pytest.mark.gpu
+def test_dcd_frames_equal_the_engine_positions(tmp_path):
+    s = load(golden_inputs(), "small")
+    e = Engine([s])
+    e.populate_lists()
+    p = str(tmp_path / "t.dcd")
+    want = []
+    for _ in range(3):
+        e.step(10)
+        e.write_dcd(0, p, 10)
+        st = e.get_state(0)
+        want.append(np.stack([st["x"], st["y"], st["z"]]).astype(np.float32))
+    nset, nsavc, natom, frames = _read_dcd(p)
+    assert (nset, nsavc, natom) == (3, 10, e.n[0]) and len(frames) == 3
+    for a, b in zip(frames, want):
+        assert np.array_equal(a, b)
+    e.close()
