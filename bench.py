@@ -352,6 +352,11 @@ def gpu_arm(args):
                     "traffic": traffic * N_REPLICAS if traffic is not None else None,
                     "alg_bytes_per_launch": alg[dom], "peak_source": peak_kind,
                     "mean_neighbours": {"sr": sr, "lr": lr}, "stages": per_stage,
+                    "step": {"alg_bytes": sum(alg.values()),
+                             "achieved_gbs": sum(alg.values()) / (ms_per_step * 1e-3) / 1e9,
+                             "frac": sum(alg.values()) / (ms_per_step * 1e-3) / 1e9 / peak,
+                             "note": "every stage's algorithmic bytes of one step of the batch over the "
+                                     "graph-replayed step time"},
                     "note": "stage = its kernels over all replica groups run alone; launch = one step of "
                             "the batch; the integrator is FP64-pipe bound, the H-bond kernel latency bound "
                             "(serial Monte Carlo per replica)"}
