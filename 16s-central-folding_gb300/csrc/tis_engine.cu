@@ -1885,6 +1885,32 @@ int tis_step(tis_handle *h, int64_t n)
     return each_group(h, [n](Group *g) { return grp_step(g, n); });
 }
 
+int tis_capture_graph(tis_handle *h, int32_t steps)
+{
+    if (!h || steps < 1) return fail(TIS_ERR_ARG, "tis_capture_graph: bad argument");
+    h->prm.graph_steps = steps;
+    h->prm.use_graph = 1;
+    return each_group(h, [steps](Group *g) -> int {
+        int rc;
+        if (!g->lists_built && (rc = populate(g))) return rc;
+        if (g->graph) {
+            TIS_CUDA(cudaGraphExecDestroy(g->graph));
+            g->graph = nullptr;
+        }
+        g->prm.graph_steps = steps;
+        g->prm.use_graph = 1;
+        cudaGraph_t gr;
+        TIS_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+        for (int s = 0; s < steps; ++s) enqueue_step(g);
+        TIS_CUDA(cudaStreamEndCapture(g->stream, &gr));
+        const cudaError_t e = cudaGraphInstantiate(&g->graph, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        g->graph_steps = steps;
+        return TIS_OK;
+    });
+}
+
 int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
 {
     // stage times of the groups run one after another, summed over the groups

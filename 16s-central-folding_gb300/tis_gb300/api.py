@@ -114,6 +114,7 @@ def _declare(L):
         "tis_density_write_dx": [vp, cp],
         "tis_density_destroy": [vp],
         "tis_write_psf": [vp, cp],
+        "tis_capture_graph": [vp, i32],
         "tis_write_dcd": [vp, i32, cp, i32, C.c_double],
         "tis_traj_grad": [vp, i64, i32, C.POINTER(dp), dp, C.POINTER(dp)],
     }
@@ -132,7 +133,7 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc", "tis_set_states",
             "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
             "tis_param_grad", "tis_traj_grad", "tis_autotune", "tis_density_create", "tis_density_add",
-            "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd"]
+            "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd", "tis_capture_graph"]
 
 
 def read_last_frame(path, n):
@@ -456,6 +457,9 @@ class Engine:
 
     def step(self, n):
         _check(lib().tis_step(self.h, n))
+
+    def capture_graph(self, steps):
+        _check(lib().tis_capture_graph(self.h, int(steps)))
 
     def sync(self):
         _check(lib().tis_sync(self.h))

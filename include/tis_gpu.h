@@ -196,6 +196,11 @@ int tis_get_forces(tis_handle *h, int replica, double *forces);
 /* n steps of the whole sequence for every replica (CUDA-graph replay when
  * use_graph is set); asynchronous: returns after enqueueing. */
 int tis_step(tis_handle *h, int64_t n);
+/* Captures (again) the CUDA graph of `steps` fused steps of every replica group,
+ * building the lists first when needed; later tis_step calls replay it for every
+ * whole `steps` (no counterpart in the reference; tis_step captures on its first
+ * call otherwise). */
+int tis_capture_graph(tis_handle *h, int32_t steps);
 /* Waits for the handle's stream; reports device-side error flags. */
 int tis_sync(tis_handle *h);
 

@@ -328,10 +328,13 @@ def test_split_calls_and_graph_equal_fused_step(systems):
     check_shifts), the fused step and the captured graph give identical states."""
     s = systems["small"]
     runs = []
-    for mode in ["split", "direct", "graph"]:
+    for mode in ["split", "direct", "graph", "captured"]:
         e = Engine([s], use_graph=1 if mode == "graph" else 0, graph_steps=20)
         e.populate_lists()
-        if mode == "split":
+        if mode == "captured":  # tis_capture_graph: a 25-step graph replayed 4 times
+            e.capture_graph(25)
+            e.step(100)
+        elif mode == "split":
             for _ in range(100):
                 e.deterministic_forces()
                 e.full_forces()
@@ -344,6 +347,7 @@ def test_split_calls_and_graph_equal_fused_step(systems):
     for k in runs[0]:
         assert np.array_equal(runs[0][k], runs[1][k]), k
         assert np.array_equal(runs[1][k], runs[2][k]), k
+        assert np.array_equal(runs[1][k], runs[3][k]), k
 
 
 def test_nonfinite_state_is_reported(systems):
