@@ -85,22 +85,48 @@ struct APos {
 };
 
 // Force contributions of one term evaluated at unit strength: the derivative
-// part, times the term's strength, goes to jv; lambda . value is summed in w
-// (lambda = the tangent direction).
+// part is summed per atom of the term (its atoms set first, at most kSlots) and,
+// times the term's strength, added to jv once per atom by flush(); lambda . value
+// is summed in w (lambda = the tangent direction).
+constexpr int kSlots = 7;
 struct AAcc {
     double *jv;
     const double *lam;
     int P;
     double scale;
     double w;
+    int ids[kSlots];
+    double acc[kSlots][3];
+    __device__ void atoms(const int *a, int n)
+    {
+#pragma unroll
+        for (int s = 0; s < kSlots; ++s) {
+            ids[s] = s < n ? a[s] : -1;
+            acc[s][0] = acc[s][1] = acc[s][2] = 0.0;
+        }
+    }
     __device__ void add(int i, DV g)
     {
-        if (jv) {
-            atomicAdd(jv + i, scale * g.x.d);
-            atomicAdd(jv + P + i, scale * g.y.d);
-            atomicAdd(jv + 2 * P + i, scale * g.z.d);
-        }
+        if (jv)
+#pragma unroll
+            for (int s = 0; s < kSlots; ++s)
+                if (ids[s] == i) {  // a slot per atom: registers, no atomics until flush
+                    acc[s][0] += g.x.d;
+                    acc[s][1] += g.y.d;
+                    acc[s][2] += g.z.d;
+                }
         if (lam) w += lam[i] * g.x.v + lam[P + i] * g.y.v + lam[2 * P + i] * g.z.v;
+    }
+    __device__ void flush()
+    {
+        if (!jv) return;
+#pragma unroll
+        for (int s = 0; s < kSlots; ++s)
+            if (ids[s] >= 0 && (acc[s][0] != 0.0 || acc[s][1] != 0.0 || acc[s][2] != 0.0)) {
+                atomicAdd(jv + ids[s], scale * acc[s][0]);
+                atomicAdd(jv + P + ids[s], scale * acc[s][1]);
+                atomicAdd(jv + 2 * P + ids[s], scale * acc[s][2]);
+            }
     }
 };
 
@@ -232,6 +258,15 @@ __device__ inline int eps_param(int t)
 }
 __device__ inline int radius_param(int t) { return t == 7 ? 12 : t == 9 ? 13 : -1; }
 
+// g[i] += v for a run-time i, the array kept in registers (a select per slot
+// instead of an indexed store, which would place g in local memory)
+template <int N>
+__device__ inline void gadd(double (&g)[N], int i, double v)
+{
+#pragma unroll
+    for (int c = 0; c < N; ++c) g[c] += (c == i) ? v : 0.0;
+}
+
 // sum of NV doubles over a block of blockDim.x threads (multiple of 32) into thread 0
 template <int NV>
 __device__ void block_reduce(double (&v)[NV], double *smem /* NV * 32 */)
@@ -314,22 +349,22 @@ __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const doub
                 if (mode == 0) {
                     const double s6 = s4.v * s2.v, s12 = s6 * s6;
                     const double u = ljw * R->elj_d[J] * (s12 - 2.0 * s6 + 1.0);
-                    if (eps_p > 0.0) g[eps_param(tp) - 6] += 0.25 * u / eps_p;
-                    if (eps_j > 0.0) g[eps_param(tj) - 6] += 0.25 * u / eps_j;
+                    if (eps_p > 0.0) gadd(g, eps_param(tp) - 6, 0.25 * u / eps_p);
+                    if (eps_j > 0.0) gadd(g, eps_param(tj) - 6, 0.25 * u / eps_j);
                     if (radius) {
                         const double dud = 0.5 * ljw * 12.0 * R->elj_d[J] * (s12 - s6) / dr.v;
                         const int ip = radius_param(tp), ij = radius_param(tj);
-                        if (ip >= 0) g[ip - 6] += dud;
-                        if (ij >= 0) g[ij - 6] += dud;
+                        if (ip >= 0) gadd(g, ip - 6, dud);
+                        if (ij >= 0) gadd(g, ij - 6, dud);
                     }
                 } else {
-                    if (eps_p > 0.0) g[eps_param(tp) - 6] += wl * phi.v / (2.0 * eps_p);
-                    if (eps_j > 0.0) g[eps_param(tj) - 6] += wl * phi.v / (2.0 * eps_j);
+                    if (eps_p > 0.0) gadd(g, eps_param(tp) - 6, wl * phi.v / (2.0 * eps_p));
+                    if (eps_j > 0.0) gadd(g, eps_param(tj) - 6, wl * phi.v / (2.0 * eps_j));
                     if (radius) {
                         const double dphi = c0 * (13.0 * s14.v - 7.0 * s8.v) / rr.v;
                         const int ip = radius_param(tp), ij = radius_param(tj);
-                        if (ip >= 0) g[ip - 6] += wl * dphi;
-                        if (ij >= 0) g[ij - 6] += wl * dphi;
+                        if (ip >= 0) gadd(g, ip - 6, wl * dphi);
+                        if (ij >= 0) gadd(g, ij - 6, wl * dphi);
                     }
                 }
             }
@@ -362,7 +397,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const doub
 // ---------------------------------------------------------------------------
 // bonded terms, stacks and formed H-bonds, one thread per term
 // ---------------------------------------------------------------------------
-constexpr int kAdjTopoThreads = 256;
+constexpr int kAdjTopoThreads = 128;
 
 __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, const double *tan, int mode)
 {
@@ -376,14 +411,17 @@ __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, c
     if (kind == 0 && mode == 0) return;  // no parameter of this set enters the bonded terms
     if (kind == 3 && !a.rhb[item]) return;
     const APos P{a.px, a.py, a.pz, mode == 1 ? tan : nullptr, d.P};
-    AAcc A{mode == 1 ? a.jv : nullptr, mode == 1 ? tan : nullptr, d.P, 1.0, 0.0};
+    AAcc A{mode == 1 ? a.jv : nullptr, mode == 1 ? tan : nullptr, d.P, 1.0, 0.0, {}, {}};
     int r = 0, param = -1;
     double dE = 0.0, u1 = 0.0;
     if (kind == 0) {
         const int4 id = d.bt_idx[item];
         const double2 par = d.bt_par[item];
+        const int at[3] = {id.x, id.y, id.z};
+        A.atoms(at, id.w == 0 ? 2 : 3);
         if (id.w == 0) bond_force(P, A, id.x, id.y, cst(par.x), par.y);
         else angle_force(P, A, id.x, id.y, id.z, cst(par.x), par.y, false);
+        A.flush();
         return;
     } else if (kind == 1) {  // tertiary: U = st_E / (1 + q), st_E = -st_D
         const int *id = d.st3_idx + 6 * item;
@@ -397,7 +435,9 @@ __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, c
         dE = -1.0;
         if (mode == 1) {
             A.scale = d.st3_E[item];
+            A.atoms(id, 6);
             six_force(P, A, id, nat, br, -1.0 / (Dn * Dn));
+            A.flush();
         }
     } else if (kind == 2) {  // secondary: U = st_E / (1 + 1.4 dr^2 + 4 dpsi1^2 + 4 dpsi2^2)
         const int *id = d.st2_idx + 7 * item;
@@ -419,10 +459,12 @@ __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, c
         dE = a.st2_dss[item];
         if (mode == 1) {
             A.scale = d.st2_E[item];
+            A.atoms(id, 7);
             const Dual w = -1.0 / (Dn * Dn);
             bond_force(P, A, id[2], id[5], 1.4 * w, r0);
             dihedral_force(P, A, id[0], id[1], id[3], id[4], 4.0 * w, p10);
             dihedral_force(P, A, id[6], id[4], id[3], id[1], 4.0 * w, p20);
+            A.flush();
         }
     } else {  // formed H-bond: U = hb_E exp(-q)
         const int *id = d.hb_idx + 6 * item;
@@ -437,7 +479,9 @@ __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, c
         dE = a.hb_dhs[item];
         if (mode == 1) {
             A.scale = d.hb_E[item];
+            A.atoms(id, 6);
             six_force(P, A, id, nat, br, -e);
+            A.flush();
         }
     }
     if (param < 0 || dE == 0.0) return;

@@ -385,7 +385,7 @@ def gpu_arm(args):
         # and reverse pass in one call); host wall clock around synchronous calls
         adjoint = None
         if rank == 0:
-            adj = Engine(systems[:16], precision=PREC_MIXED, device=local)
+            adj = Engine(systems[:16], precision=PREC_MIXED, device=local, groups=1)  # the adjoint runs group by group
             adj.populate_lists()
             adj.step(50)
             adj.sync()
