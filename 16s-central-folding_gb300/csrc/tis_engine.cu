@@ -1412,6 +1412,7 @@ struct tis_handle {
     std::vector<Group *> groups;
     std::vector<cudaEvent_t> join;
     std::vector<int> grp_of, loc_of;
+    std::vector<tis_density *> densities;  // grids on this handle: released with it
 
     ~tis_handle()
     {
@@ -1538,10 +1539,15 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     return TIS_OK;
 }
 
+static void density_release(tis_density *d);
+
 int tis_destroy(tis_handle *h)
 {
     if (h) {
         cudaSetDevice(h->prm.device);
+        cudaStreamSynchronize(h->stream);
+        for (tis_density *d : h->densities) density_release(d);  // the grids stay valid handles, now empty
+        h->densities.clear();
         for (Group *g : h->groups) grp_destroy(g);
         h->groups.clear();
         cudaStreamSynchronize(h->stream);
@@ -1681,12 +1687,22 @@ struct tis_density {
     unsigned long long *d_grid = nullptr;
     int64_t frames = 0;
     size_t cells() const { return (size_t)dims[0] * dims[1] * dims[2]; }
-    ~tis_density()
+    void release()
     {
         for (void *p : {(void *)d_idx, (void *)d_ref, (void *)d_fit, (void *)d_grid})
             if (p) cudaFree(p);
+        d_idx = nullptr;
+        d_ref = d_fit = nullptr;
+        d_grid = nullptr;
+        h = nullptr;
+        g = nullptr;
     }
+    ~tis_density() { release(); }
 };
+
+// the handle is being destroyed: its grids lose their device memory and report
+// TIS_ERR_STATE from then on
+static void density_release(tis_density *d) { d->release(); }
 
 extern "C" {
 
@@ -1737,6 +1753,7 @@ int tis_density_create(tis_handle *h, int r, int kind, const double lo[3], doubl
             (e = cudaMemcpy(d->d_ref, fit_ref, sizeof(double) * 3 * n_fit, cudaMemcpyHostToDevice)) != cudaSuccess)
             return bail(e);
     }
+    h->densities.push_back(d);
     *out = d;
     return TIS_OK;
 }
@@ -1744,6 +1761,7 @@ int tis_density_create(tis_handle *h, int r, int kind, const double lo[3], doubl
 int tis_density_add(tis_density *d)
 {
     if (!d) return fail(TIS_ERR_ARG, "tis_density_add: null grid");
+    if (!d->h) return fail(TIS_ERR_STATE, "tis_density_add: the grid's handle was destroyed");
     TIS_CUDA(cudaSetDevice(d->h->prm.device));
     const tis::Dev &dev = d->g->dev;
     if (d->n_fit > 0) tis::launch_fit(dev, d->h->stream, d->loc, d->n_fit, d->d_idx, d->d_ref, d->d_fit);
@@ -1757,6 +1775,7 @@ int tis_density_add(tis_density *d)
 int tis_density_get(tis_density *d, double *counts, int64_t cap, int64_t *frames, double *rmsd)
 {
     if (!d) return fail(TIS_ERR_ARG, "tis_density_get: null grid");
+    if (!d->h) return fail(TIS_ERR_STATE, "tis_density_get: the grid's handle was destroyed");
     TIS_CUDA(cudaSetDevice(d->h->prm.device));
     std::vector<unsigned long long> c(d->cells());
     double fit[16];
@@ -1807,8 +1826,12 @@ int tis_density_write_dx(tis_density *d, const char *path)
 int tis_density_destroy(tis_density *d)
 {
     if (d) {
-        cudaSetDevice(d->h->prm.device);
-        cudaStreamSynchronize(d->h->stream);
+        if (d->h) {
+            cudaSetDevice(d->h->prm.device);
+            cudaStreamSynchronize(d->h->stream);
+            auto &v = d->h->densities;
+            v.erase(std::remove(v.begin(), v.end(), d), v.end());
+        }
         delete d;
     }
     return TIS_OK;

@@ -254,6 +254,8 @@ int tis_density_get(tis_density *g, double *counts, int64_t cap, int64_t *frames
  * the origin at the centre of the first bin, three delta lines, the
  * gridconnections object, the data array of counts three per line, the field. */
 int tis_density_write_dx(tis_density *g, const char *path);
+/* Destroying the handle releases its grids' device memory: later calls on such a
+ * grid return TIS_ERR_STATE; tis_density_destroy still frees the object. */
 int tis_density_destroy(tis_density *g);
 
 /* Appends one frame of a replica to the reference's three output files (any may

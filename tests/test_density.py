@@ -114,3 +114,17 @@ def test_density_rejects_bad_grids():
     with pytest.raises(TisError):
         e.density(0, K_ION, (0, 0, 0), 1.0, (10, 10, 10), fit_beads=[0, 1], fit_ref=np.zeros((2, 3)))
     e.close()
+
+
+def test_density_outliving_its_handle_reports_state_error():
+    from tis_gb300 import TisError
+    s = load(golden_inputs(), "small")
+    e = Engine([s], precision=PREC_MIXED)
+    e.populate_lists()
+    g = e.density(0, K_ION, (0, 0, 0), 10.0, (20, 20, 20))
+    g.add()
+    e.close()  # releases the grid's device memory
+    with pytest.raises(TisError) as err:
+        g.get()
+    assert err.value.code == 8
+    g.close()
