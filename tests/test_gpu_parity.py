@@ -221,6 +221,30 @@ def test_noise_free_trajectory_tracks_oracle(systems, prec_name, prec, tol_pos):
     assert e.counters(0)[2] == o.draws()
 
 
+@pytest.mark.parametrize("prec_name,prec,tol_pos", [("fp64", PREC_FP64, 0.1), ("mixed", PREC_MIXED, 1.0)])
+def test_noise_free_trajectory_10k_steps(systems, prec_name, prec, tol_pos):
+    """10^4 noise-free steps of the small system against the FP64 oracle: the
+    divergence curve (max position deviation every 1000 steps) is printed.  Any
+    difference grows with the dynamics' own sensitivity (about tenfold per 1000
+    steps): the FP64 path, which differs from the oracle only in the order of its
+    force sums (1e-13 A after 100 steps), reaches ~5e-3 A at 10^4 steps (held to
+    0.1 A); mixed precision, which rounds each pair force to FP32, levels off at a
+    few 1e-2 A (held to 1 A, a fraction of a bond length)."""
+    s = systems["small"]
+    o = _oracle(s, noise=False)
+    o.populate_lists()
+    e = Engine([s], precision=prec, noise=NOISE_OFF)
+    e.populate_lists()
+    dev = []
+    for k in range(10):
+        o.step(1000)
+        e.step(1000)
+        e.sync()
+        dev.append(np.abs(_positions(e.get_state(0)) - _positions(o.get_state())).max())
+    print(f"{prec_name} max |dx| every 1000 steps:", " ".join(f"{d:.2e}" for d in dev))
+    assert max(dev) < tol_pos
+
+
 @pytest.mark.parametrize("prec_name,prec,tol_pos", [("fp64", PREC_FP64, 1e-7), ("mixed", PREC_MIXED, 1e-3)])
 def test_stochastic_trajectory_tracks_oracle(systems, prec_name, prec, tol_pos):
     """Langevin noise and Monte Carlo from the shared Philox stream: 200 steps."""
