@@ -138,6 +138,59 @@ int tis_write_psf(const tis_system *s, const char *path)
     return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
 }
 
+int tis_write_cgpdb(const tis_system *s, const double *x, const double *y, const double *z, const char *path)
+{
+    if (!s || !path) return fail(TIS_ERR_ARG, "tis_write_cgpdb: bad argument");
+    const int n = (int)sys_i64(s, "n_particles", -1), ntp = (int)sys_i64(s, "n_rna", -1);
+    const int nbp = (int)sys_i64(s, "n_entries", -1);
+    const tis::Array *type = s->get("type"), *kind = s->get("kind");
+    if (n < 1 || ntp < 1 || ntp > n || nbp < 1 || !type || !kind || type->dtype != TIS_I32 ||
+        kind->dtype != TIS_I32 || type->count() != n || kind->count() != n)
+        return fail(TIS_ERR_ARG, "tis_write_cgpdb: the system lacks n_particles, n_rna, n_entries, type or kind");
+    const double *c[3] = {x, y, z};
+    const char *nm[3] = {"x", "y", "z"};
+    for (int a = 0; a < 3; ++a)
+        if (!c[a]) {  // the system's own (set-up) coordinates
+            const tis::Array *arr = s->get(nm[a]);
+            if (!arr || arr->dtype != TIS_F64 || arr->count() != n) return fail(TIS_ERR_ARG, "tis_write_cgpdb: no %s", nm[a]);
+            c[a] = arr->as<double>();
+        }
+    const int32_t *ty = type->as<int32_t>(), *kd = kind->as<int32_t>();
+    auto letter = [&](int i) {
+        const int b = 3 * (i / 3) + 1;
+        const int t = b < ntp ? ty[b] : 0;
+        return t == 3 ? 'A' : t == 4 ? 'G' : t == 5 ? 'C' : t == 6 ? 'U' : 'N';
+    };
+    FILE *f = fopen(path, "w");
+    if (!f) return fail(TIS_ERR_IO, "cannot open %s", path);
+    // the layout of the reference's exporter (analysis/make_ninfo/16SCD_ninfo.cpp:6479-6561): its
+    // counts are the PDB entries (N_amino = NBP_atom), entries plus ions (NB_atom), RNA beads
+    // (NTP_atom), RNA bead pairs (NpTP_atom) and particles (NT_atom)
+    fprintf(f, "RECORD   N_amino   %5i\n", nbp);
+    fprintf(f, "RECORD   NBP_atom  %5i\n", nbp);
+    fprintf(f, "RECORD   NB_atom   %5i\n", nbp + (n - ntp));
+    fprintf(f, "RECORD   NTP_atom  %5i\n", ntp);
+    fprintf(f, "RECORD   NpTP_atom %5i\n", ntp * (ntp + 1) / 2);
+    fprintf(f, "RECORD   NT_atom   %5i\n", n);
+    for (int i = 1; i <= ntp; ++i) {
+        const char l = letter(i);
+        if (i % 3 == 1) fprintf(f, "ATOM  %5i  S   R%c  A%4i", i, l, i / 3 + 1);
+        else if (i % 3 == 2) fprintf(f, "ATOM  %5i  %cb  R%c  A%4i", i, l, l, i / 3 + 1);
+        else fprintf(f, "ATOM  %5i  P   R%c  A%4i", i, l, i / 3 + 1);
+        fprintf(f, "    %8.3f%8.3f%8.3f\n", c[0][i - 1], c[1][i - 1], c[2][i - 1]);
+    }
+    fprintf(f, "TER\n");
+    for (int i = ntp + 1; i <= n; ++i) {
+        const int k = kd[i - 1];
+        const char *nmr = k == 3 ? "MG    MG" : k == 4 ? " Cl   Cl" : " K    K ";
+        fprintf(f, "ATOM  %5i %s B%4i    %8.3f%8.3f%8.3f\n", i, nmr, i, c[0][i - 1], c[1][i - 1], c[2][i - 1]);
+    }
+    fprintf(f, "TER\n");
+    const bool ok = !ferror(f);
+    fclose(f);
+    return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
+}
+
 int tis_write_dcd(tis_handle *h, int replica, const char *path, int32_t nsavc, double delta)
 {
     if (!h || !path || nsavc < 1) return fail(TIS_ERR_ARG, "tis_write_dcd: bad argument");

@@ -114,6 +114,7 @@ def _declare(L):
         "tis_density_write_dx": [vp, cp],
         "tis_density_destroy": [vp],
         "tis_write_psf": [vp, cp],
+        "tis_write_cgpdb": [vp, dp, dp, dp, cp],
         "tis_capture_graph": [vp, i32],
         "tis_write_dcd": [vp, i32, cp, i32, C.c_double],
         "tis_traj_grad": [vp, i64, i32, C.POINTER(dp), dp, C.POINTER(dp)],
@@ -133,7 +134,8 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_rand_stream", "tis_profile_stages", "tis_get_forces", "tis_pair_lists_noalloc", "tis_set_states",
             "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
             "tis_param_grad", "tis_traj_grad", "tis_autotune", "tis_density_create", "tis_density_add",
-            "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd", "tis_capture_graph"]
+            "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd", "tis_capture_graph",
+            "tis_write_cgpdb"]
 
 
 def read_last_frame(path, n):
@@ -233,6 +235,15 @@ class System:
 
     def to_dict(self):
         return {k: self[k] for k in self.names()}
+
+    def write_cgpdb(self, path, state=None):
+        """The coarse-grained PDB of the reference's exporter (tis_write_cgpdb); state:
+        {x, y, z} arrays (None: the system's own coordinates)."""
+        if state is None:
+            _check(lib().tis_write_cgpdb(self.h, None, None, None, os.fsencode(path)))
+        else:
+            xyz = [np.ascontiguousarray(state[k], dtype=np.float64) for k in ("x", "y", "z")]
+            _check(lib().tis_write_cgpdb(self.h, *[_dp(a) for a in xyz], os.fsencode(path)))
 
     def write_psf(self, path):
         """The topology in the PSF layout of the reference's exporter (tis_write_psf)."""

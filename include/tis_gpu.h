@@ -230,6 +230,10 @@ int tis_ion_counts(tis_handle *h, int replica, int kind, double radius, int32_t 
  * file does not exist and updating its frame count; nsavc: steps per frame,
  * delta: the time step in the header. */
 int tis_write_psf(const tis_system *s, const char *path);
+/* The coarse-grained PDB of the same exporter (16SCD_ninfo.cpp:6479-6561): six
+ * RECORD count lines, the beads (S, <base>b, P of residue R<base>), TER, the ions,
+ * TER; coordinates x, y, z of n_particles each (NULL: the system's own). */
+int tis_write_cgpdb(const tis_system *s, const double *x, const double *y, const double *z, const char *path);
 int tis_write_dcd(tis_handle *h, int replica, const char *path, int32_t nsavc, double delta);
 
 /* Ion density grid of one replica accumulated on the device over frames (the

@@ -189,3 +189,31 @@ def test_dcd_frames_equal_the_engine_positions(tmp_path):
     for a, b in zip(frames, want):
         assert np.array_equal(a, b)
     e.close()
+
+
+def test_cgpdb_matches_the_exporter_layout(tmp_path):
+    """tis_write_cgpdb: the exporter's RECORD counts, bead and ion records in PDB
+    columns (16SCD_ninfo.cpp:6479-6561), coordinates to 1e-3 A."""
+    s = load(golden_inputs(), "small")
+    p = str(tmp_path / "t.pdb")
+    s.write_cgpdb(p)
+    lines = open(p).read().splitlines()
+    n, ntp, nbp = int(s["n_particles"][0]), int(s["n_rna"][0]), int(s["n_entries"][0])
+    want = [("N_amino", nbp), ("NBP_atom", nbp), ("NB_atom", nbp + n - ntp), ("NTP_atom", ntp),
+            ("NpTP_atom", ntp * (ntp + 1) // 2), ("NT_atom", n)]
+    for ln, (k, v) in zip(lines[:6], want):
+        assert ln.split() == ["RECORD", k, str(v)]
+    atoms = lines[6:6 + ntp]
+    assert lines[6 + ntp] == "TER" and lines[-1] == "TER" and len(lines) == 6 + n + 2
+    x, y, z = s["x"], s["y"], s["z"]
+    letter = {3: "A", 4: "G", 5: "C", 6: "U"}
+    for i, a in enumerate(atoms, start=1):
+        c = letter[s["type"][3 * (i // 3) + 1]]
+        assert a[:6] == "ATOM  " and int(a[6:11]) == i
+        assert a[12:16] == (" S  " if i % 3 == 1 else f" {c}b " if i % 3 == 2 else " P  ")
+        assert a[17:20] == f"R{c} " [:3] and a[21] == "A" and int(a[22:26]) == i // 3 + 1
+        assert [float(a[30:38]), float(a[38:46]), float(a[46:54])] == pytest.approx([x[i - 1], y[i - 1], z[i - 1]], abs=6e-4)
+    names = {3: "MG    MG", 4: " Cl   Cl", 5: " K    K "}
+    for i in range(ntp + 1, n + 1):
+        a = lines[6 + i]
+        assert int(a[6:11]) == i and a[12:20] == names[s["kind"][i - 1]] and a[21] == "B" and int(a[22:26]) == i
