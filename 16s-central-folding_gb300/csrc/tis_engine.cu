@@ -895,7 +895,8 @@ static int grp_ion_counts(Group *h, int r, int kind, double radius, int32_t *cou
 {
     int rc = valid_replica(h, r);
     if (rc) return rc;
-    if (kind < 3 || kind > 5) return fail(TIS_ERR_ARG, "tis_ion_counts: ion kind %d is not 3 (Mg), 4 (Cl) or 5 (K)", kind);
+    if (kind != 0 && (kind < 3 || kind > 5))
+        return fail(TIS_ERR_ARG, "tis_ion_counts: kind %d is not 0 (P), 3 (Mg), 4 (Cl) or 5 (K)", kind);
     if (!(radius > 0) || radius > h->prm.sr)
         return fail(TIS_ERR_ARG, "tis_ion_counts: radius %g outside (0, %g] (the SR radius)", radius, h->prm.sr);
     if (!h->lists_built && (rc = populate(h))) return rc;

@@ -6,9 +6,10 @@ from tis_gb300 import System, Engine
     eng.step(1000); eng.sync()
 """
 from .api import (ENERGY_NAMES, N_PARAMS, NOISE_OFF, NOISE_REFERENCE, PARAM_NAMES, PREC_FP64, PREC_MIXED, STATE_NAMES,
-                  TERM_BONDED, TERM_HB, TERM_LR, TERM_SR, TERM_STACK, Engine, System, TisError, autotune, lib,
+                  TERM_BONDED, TERM_HB, TERM_LR, TERM_SR, TERM_STACK, Engine, System, TisError, autotune, contact_concentration,
+                  lib,
                   read_last_frame)
 
 __all__ = ["System", "Engine", "TisError", "lib", "STATE_NAMES", "ENERGY_NAMES", "TERM_SR", "TERM_LR",
            "TERM_BONDED", "TERM_STACK", "TERM_HB", "PREC_MIXED", "PREC_FP64", "NOISE_REFERENCE", "NOISE_OFF",
-           "read_last_frame", "PARAM_NAMES", "N_PARAMS", "autotune"]
+           "read_last_frame", "PARAM_NAMES", "N_PARAMS", "autotune", "contact_concentration"]

@@ -316,6 +316,13 @@ class Density:
             pass
 
 
+def contact_concentration(count_sum, frames, cut=7.300000001):
+    """Contact concentration (mol/L) of particles counted within `cut` A of a
+    phosphate, summed over `frames` frames (analysis/salt_nt/integrate_num_ions.py:
+    51-55: count / (frames * 4/3 pi cut^3 * 6.02214e-4))."""
+    return np.asarray(count_sum, dtype=np.float64) / (float(frames) * 4.0 / 3.0 * np.pi * cut ** 3 * 6.02214 / 1e4)
+
+
 def run_params(**kw):
     p = RunParams()
     lib().tis_run_params_default(C.byref(p))

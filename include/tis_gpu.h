@@ -214,10 +214,12 @@ int tis_get_all_energies(tis_handle *h, double *out);
  * mg_bound.F90:94-116 and analysis/salt_nt/dcd_traj_SaltCount_Kinetics_PBC.py:
  * 42-70, which read them back from trajectory files): for every phosphate of the
  * replica, in bead order, the number of ions of `kind` (3 Mg, 4 Cl, 5 K, the
- * reference's part_key) whose minimum-image FP64 distance is at most `radius`
- * (at most the SR radius, e.g. 4.4, 5 or 7.2684 A); *n_p receives the number of
- * phosphates (at most cap counts are written) and *total the number of distinct
- * ions within range of some phosphate. */
+ * reference's part_key; 0 counts the other phosphates) whose minimum-image FP64
+ * distance is at most `radius` (at most the SR radius, e.g. 4.4, 5 or 7.2684 A);
+ * *n_p receives the number of phosphates (at most cap counts are written) and
+ * *total the number of distinct particles within range of some phosphate.  Summed
+ * over frames at radius 7.3 A these give analysis/salt_nt/integrate_num_ions.py's
+ * contact concentrations (count / (frames 4/3 pi r^3 6.02214e-4), mol/L). */
 int tis_ion_counts(tis_handle *h, int replica, int kind, double radius, int32_t *counts, int64_t cap,
                    int64_t *n_p, int32_t *total);
 

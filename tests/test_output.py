@@ -88,7 +88,7 @@ def test_cli_runs_writes_and_restarts(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind,radius", [(3, 4.4), (3, 7.2684), (5, 5.0), (5, 7.2684), (4, 7.2684)])
+@pytest.mark.parametrize("kind,radius", [(3, 4.4), (3, 7.2684), (5, 5.0), (5, 7.2684), (4, 7.2684), (0, 7.3)])
 def test_ion_counts_match_a_direct_count(kind, radius):
     """Ions of one kind within a radius of each phosphate (the reference's bound-ion
     analyses), counted on the device from the SR lists, equal a direct count over
@@ -110,6 +110,8 @@ def test_ion_counts_match_a_direct_count(kind, radius):
     d = np.where(d > 0.5 * L, d - L, d)
     d = np.where(d < -0.5 * L, d + L, d)
     r2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+    if kind == 0:  # phosphates around phosphates: not itself
+        r2[np.arange(len(P)), np.arange(len(P))] = np.inf
     within = r2 <= radius * radius
     assert np.array_equal(counts, within.sum(1))
     assert total == int(within.any(0).sum())
@@ -217,3 +219,13 @@ def test_cgpdb_matches_the_exporter_layout(tmp_path):
     for i in range(ntp + 1, n + 1):
         a = lines[6 + i]
         assert int(a[6:11]) == i and a[12:20] == names[s["kind"][i - 1]] and a[21] == "B" and int(a[22:26]) == i
+
+
+def test_contact_concentration_formula():
+    """integrate_num_ions.py:51-55: count / (nstep 4/3 pi cut^3 6.02214 / 10^4) mol/L."""
+    import math
+    from tis_gb300 import contact_concentration
+    cut = 7.300000001
+    got = contact_concentration([12, 0, 3], 40)
+    want = [c / (40 * 4 / 3.0 * math.pi * (cut ** 3) * 6.02214 / (10 ** 4)) for c in (12, 0, 3)]
+    assert np.allclose(got, want, rtol=1e-15)
