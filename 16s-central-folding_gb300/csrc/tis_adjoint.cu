@@ -30,34 +30,51 @@ constexpr int kNP = kNParams;
 // ---------------------------------------------------------------------------
 // dual numbers: value and derivative along the tangent direction
 // ---------------------------------------------------------------------------
-struct Dual {
-    double v, d;
+template <class T>
+struct DualT {
+    T v, d;
 };
-__device__ inline Dual cst(double v) { return {v, 0.0}; }
-__device__ inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
-__device__ inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
-__device__ inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
-__device__ inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
-__device__ inline Dual operator/(Dual a, Dual b)
+template <class T>
+__device__ inline DualT<T> operator+(DualT<T> a, DualT<T> b) { return {a.v + b.v, a.d + b.d}; }
+template <class T>
+__device__ inline DualT<T> operator-(DualT<T> a, DualT<T> b) { return {a.v - b.v, a.d - b.d}; }
+template <class T>
+__device__ inline DualT<T> operator-(DualT<T> a) { return {-a.v, -a.d}; }
+template <class T>
+__device__ inline DualT<T> operator*(DualT<T> a, DualT<T> b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+template <class T>
+__device__ inline DualT<T> operator/(DualT<T> a, DualT<T> b)
 {
-    const double q = a.v / b.v;
+    const T q = a.v / b.v;
     return {q, (a.d - q * b.d) / b.v};
 }
-__device__ inline Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
-__device__ inline Dual operator+(double a, Dual b) { return {a + b.v, b.d}; }
-__device__ inline Dual operator-(Dual a, double b) { return {a.v - b, a.d}; }
-__device__ inline Dual operator-(double a, Dual b) { return {a - b.v, -b.d}; }
-__device__ inline Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
-__device__ inline Dual operator/(double a, Dual b)
+template <class T>
+__device__ inline DualT<T> operator+(DualT<T> a, T b) { return {a.v + b, a.d}; }
+template <class T>
+__device__ inline DualT<T> operator+(T a, DualT<T> b) { return {a + b.v, b.d}; }
+template <class T>
+__device__ inline DualT<T> operator-(DualT<T> a, T b) { return {a.v - b, a.d}; }
+template <class T>
+__device__ inline DualT<T> operator-(T a, DualT<T> b) { return {a - b.v, -b.d}; }
+template <class T>
+__device__ inline DualT<T> operator*(T a, DualT<T> b) { return {a * b.v, a * b.d}; }
+template <class T>
+__device__ inline DualT<T> operator/(T a, DualT<T> b)
 {
-    const double q = a / b.v;
+    const T q = a / b.v;
     return {q, -q * b.d / b.v};
 }
-__device__ inline Dual dsqrt(Dual a)
+template <class T>
+__device__ inline DualT<T> dsqrt(DualT<T> a)
 {
-    const double s = sqrt(a.v);
-    return {s, s > 0.0 ? 0.5 * a.d / s : 0.0};
+    const T s = sqrt(a.v);
+    return {s, s > T(0) ? T(0.5) * a.d / s : T(0)};
 }
+
+// FP64 duals for the restraint terms and the parameter derivatives; the pair
+// Jacobian of a mixed-precision engine runs in FP32 duals (FP64 sums)
+using Dual = DualT<double>;
+__device__ inline Dual cst(double v) { return {v, 0.0}; }
 __device__ inline Dual dexp(Dual a)
 {
     const double e = exp(a.v);
@@ -296,9 +313,10 @@ __device__ void block_reduce(double (&v)[NV], double *smem /* NV * 32 */)
 // partners' lists).  mode 0: dU/dtheta (each pair half from each side); mode 1:
 // jv[p] += (J tan)_p and the parameter terms of lambda = tan.  The LR kernel in
 // mode 1 runs only for replicas whose LR force was refreshed in the step.
-template <bool LR>
+template <bool LR, class T>
 __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const double *tan, int mode)
 {
+    using DT = DualT<T>;
     __shared__ double s_red[9 * 32];
     const int p = blockIdx.x * kBlock + threadIdx.x;
     const int r = d.blk_rep[blockIdx.x];
@@ -327,41 +345,42 @@ __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const doub
                 if (v[c] > R->hbox[c]) v[c] -= R->box[c];
                 if (v[c] < -R->hbox[c]) v[c] += R->box[c];
             }
+            // cutoff decisions in FP64, as the forward pass decides them
             const double r2e = __dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2]));
             const bool lj = !LR && ljw != 0.0 && r2e <= R->dlj2_d[J];
             const bool cou = (LR || (chp && kj != 1 && kj != 2)) && r2e <= R->rc2;
             if (!lj && !cou) continue;
-            const DV dv = {{v[0], tan ? lx - tan[j] : 0.0}, {v[1], tan ? ly - tan[P + j] : 0.0},
-                           {v[2], tan ? lz - tan[2 * P + j] : 0.0}};
-            const Dual r2 = dot(dv, dv);
-            const Dual rr = dsqrt(r2);
-            Dual F = cst(0.0);
+            const V3<DT> dv = {{(T)v[0], tan ? (T)(lx - tan[j]) : T(0)}, {(T)v[1], tan ? (T)(ly - tan[P + j]) : T(0)},
+                               {(T)v[2], tan ? (T)(lz - tan[2 * P + j]) : T(0)}};
+            const DT r2 = dot(dv, dv);
+            const DT rr = dsqrt(r2);
+            DT F = {T(0), T(0)};
             const double wl = lx * v[0] + ly * v[1] + lz * v[2];  // lambda_p . (x_p - x_j)
             if (lj) {
-                const Dual dr = rr + (kSig0 - R->dlj_d[J]);
-                const Dual s = kSig0 / dr;
-                const Dual s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+                const DT dr = rr + (T)(kSig0 - R->dlj_d[J]);
+                const DT s = (T)kSig0 / dr;
+                const DT s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
                 const double c0 = ljw * R->flj_d[J];
-                const Dual phi = c0 * (s14 - s8) * dr / rr;
+                const DT phi = (T)c0 * (s14 - s8) * dr / rr;
                 F = F + phi;
                 const double eps_j = R->elj_d[jn12(tj, tj)];
                 const bool radius = !(tp <= 6 && tj <= 6);
                 if (mode == 0) {
-                    const double s6 = s4.v * s2.v, s12 = s6 * s6;
+                    const double s6 = (double)s4.v * (double)s2.v, s12 = s6 * s6;
                     const double u = ljw * R->elj_d[J] * (s12 - 2.0 * s6 + 1.0);
                     if (eps_p > 0.0) gadd(g, eps_param(tp) - 6, 0.25 * u / eps_p);
                     if (eps_j > 0.0) gadd(g, eps_param(tj) - 6, 0.25 * u / eps_j);
                     if (radius) {
-                        const double dud = 0.5 * ljw * 12.0 * R->elj_d[J] * (s12 - s6) / dr.v;
+                        const double dud = 0.5 * ljw * 12.0 * R->elj_d[J] * (s12 - s6) / (double)dr.v;
                         const int ip = radius_param(tp), ij = radius_param(tj);
                         if (ip >= 0) gadd(g, ip - 6, dud);
                         if (ij >= 0) gadd(g, ij - 6, dud);
                     }
                 } else {
-                    if (eps_p > 0.0) gadd(g, eps_param(tp) - 6, wl * phi.v / (2.0 * eps_p));
-                    if (eps_j > 0.0) gadd(g, eps_param(tj) - 6, wl * phi.v / (2.0 * eps_j));
+                    if (eps_p > 0.0) gadd(g, eps_param(tp) - 6, wl * (double)phi.v / (2.0 * eps_p));
+                    if (eps_j > 0.0) gadd(g, eps_param(tj) - 6, wl * (double)phi.v / (2.0 * eps_j));
                     if (radius) {
-                        const double dphi = c0 * (13.0 * s14.v - 7.0 * s8.v) / rr.v;
+                        const double dphi = c0 * (13.0 * (double)s14.v - 7.0 * (double)s8.v) / (double)rr.v;
                         const int ip = radius_param(tp), ij = radius_param(tj);
                         if (ip >= 0) gadd(g, ip - 6, wl * dphi);
                         if (ij >= 0) gadd(g, ij - 6, wl * dphi);
@@ -369,17 +388,17 @@ __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const doub
                 }
             }
             if (cou) {
-                const Dual psi = R->qclb_d[J] / (rr * r2);
+                const DT psi = (T)R->qclb_d[J] / (rr * r2);
                 F = F + psi;
                 if (R->lB != 0.0) {
-                    if (mode == 0) g[8] += 0.5 * R->qclb_d[J] / rr.v / R->lB;
-                    else g[8] += wl * psi.v / R->lB;
+                    if (mode == 0) g[8] += 0.5 * R->qclb_d[J] / (double)rr.v / R->lB;
+                    else g[8] += wl * (double)psi.v / R->lB;
                 }
             }
-            if (mode == 1) {  // d/dtan of F (x_p - x_j)
-                jx += F.d * v[0] + F.v * dv.x.d;
-                jy += F.d * v[1] + F.v * dv.y.d;
-                jz += F.d * v[2] + F.v * dv.z.d;
+            if (mode == 1) {  // d/dtan of F (x_p - x_j), summed in FP64
+                jx += (double)F.d * v[0] + (double)F.v * (double)dv.x.d;
+                jy += (double)F.d * v[1] + (double)F.v * (double)dv.y.d;
+                jz += (double)F.d * v[2] + (double)F.v * (double)dv.z.d;
             }
         }
         if (mode == 1) {
@@ -628,8 +647,15 @@ __global__ void __launch_bounds__(kBlock) k_adj_pack(Dev d, const double *src, d
 
 void launch_adj_pair(const Dev &d, const AdjDev &a, cudaStream_t s, bool lr, const double *tan, int mode)
 {
-    if (lr) k_adj_pair<true><<<d.nblk, kBlock, 0, s>>>(d, a, tan, mode);
-    else k_adj_pair<false><<<d.nblk, kBlock, 0, s>>>(d, a, tan, mode);
+    // the Jacobian products of a mixed-precision engine in FP32 duals (its forward
+    // pair math is FP32); dU/dtheta and FP64 engines in FP64 duals
+    if (mode == 1 && !d.fp64) {
+        if (lr) k_adj_pair<true, float><<<d.nblk, kBlock, 0, s>>>(d, a, tan, mode);
+        else k_adj_pair<false, float><<<d.nblk, kBlock, 0, s>>>(d, a, tan, mode);
+    } else {
+        if (lr) k_adj_pair<true, double><<<d.nblk, kBlock, 0, s>>>(d, a, tan, mode);
+        else k_adj_pair<false, double><<<d.nblk, kBlock, 0, s>>>(d, a, tan, mode);
+    }
 }
 
 void launch_adj_topo(const Dev &d, const AdjDev &a, cudaStream_t s, const double *tan, int mode)
