@@ -54,6 +54,32 @@ def replica_specs(n=N_REPLICAS):
     return [dict(n_mg=m, n_cl=c, n_k=k, seed=1000 + r) for r, (m, c, k) in enumerate(ions)]
 
 
+def rank_replica_specs(rank, n=N_REPLICAS):
+    """The batch of one rank: replicas only, so every rank runs the whole workload
+    with its own seeds (offset by 100000 x rank) and nothing is exchanged."""
+    specs = replica_specs(n)
+    for sp in specs:
+        sp["seed"] += 100000 * rank
+    return specs
+
+
+def max_over_ranks(ms, world, device=None):
+    """The slowest rank's timed region in ms (the job ends with it); the one
+    collective of a multi-rank run, outside the timed region."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(ms, world, n_rep, steps):
+    """Whole-job replica-steps/s: every rank's replicas over the slowest rank's time."""
+    return world * n_rep * steps / (ms / 1000.0)
+
+
 def make_inputs(tmp):
     from tis_gb300 import synth
     return synth.generate(tmp, "central", N_NT, seed=GEN_SEED, n_hb_pairs=120)
@@ -238,10 +264,7 @@ def gpu_arm(args):
         dist.init_process_group("nccl")
     with tempfile.TemporaryDirectory() as tmp:
         files = make_inputs(tmp)
-        specs = replica_specs()
-        # replicas only: every rank runs its own full batch of independent replicas
-        for sp in specs:
-            sp["seed"] += 100000 * rank
+        specs = rank_replica_specs(rank)  # replicas only: every rank its own batch
         systems = load_systems(files, specs)
         # the launch configuration: measured by tis_autotune (replica groups, steps per
         # graph, threads per particle of the pair launches; 1000 steps per trial), or
@@ -282,13 +305,11 @@ def gpu_arm(args):
             torch.cuda.synchronize()
         ms = sum(a.elapsed_time(b) for a, b in ev)
         launches = eng.launches() - launches0
+        ms = max_over_ranks(ms, world, device=f"cuda:{local}")
         if world > 1:
-            t = torch.tensor([ms], device=f"cuda:{local}")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
             torch.distributed.barrier()
         ms_per_step = ms / K
-        value = world * N_REPLICAS * K / (ms / 1000.0)
+        value = job_value(ms, world, N_REPLICAS, K)
 
         if not args.extras:
             if rank == 0:
