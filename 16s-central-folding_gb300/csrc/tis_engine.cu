@@ -1870,6 +1870,79 @@ int tis_get_forces(tis_handle *h, int r, double *forces)
     return grp_get_forces(g, loc, forces);
 }
 
+// Bit-exact checkpoint: every array a step reads and leaves for the next one
+// (step_state: x, x_old, v, fixed-point positions, the held LR force, replica
+// counters with the rand() position, neighbour lists, H-bond status), per group.
+int tis_checkpoint_save(tis_handle *h, const char *path)
+{
+    if (!h || !path) return fail(TIS_ERR_ARG, "tis_checkpoint_save: bad argument");
+    TIS_CUDA(cudaSetDevice(h->prm.device));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(TIS_ERR_IO, "cannot open %s", path);
+    bool ok = fwrite("TISCKPT1", 1, 8, f) == 8;
+    const int32_t head[2] = {(int32_t)h->groups.size(), h->R};
+    ok = ok && fwrite(head, 4, 2, f) == 2;
+    std::vector<char> buf;
+    for (Group *g : h->groups) {
+        if (!ok) break;
+        TIS_CUDA(cudaStreamSynchronize(g->stream));
+        const int32_t gh[5] = {g->R, g->P, g->dev.cap_sr, g->dev.cap_lr, g->lists_built ? 1 : 0};
+        ok = ok && fwrite(gh, 4, 5, f) == 5;
+        for (const auto &e : step_state(g)) {
+            const uint64_t n = e.second;
+            buf.resize(n);
+            if (n) TIS_CUDA(cudaMemcpy(buf.data(), e.first, n, cudaMemcpyDeviceToHost));
+            ok = ok && fwrite(&n, 8, 1, f) == 1 && fwrite(buf.data(), 1, n, f) == n;
+        }
+    }
+    ok = fclose(f) == 0 && ok;
+    return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
+}
+
+int tis_checkpoint_load(tis_handle *h, const char *path)
+{
+    if (!h || !path) return fail(TIS_ERR_ARG, "tis_checkpoint_load: bad argument");
+    TIS_CUDA(cudaSetDevice(h->prm.device));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(TIS_ERR_IO, "cannot open %s", path);
+    auto bad = [&](const char *why) {
+        fclose(f);
+        return fail(TIS_ERR_FORMAT, "%s: %s", path, why);
+    };
+    char magic[8];
+    int32_t head[2];
+    if (fread(magic, 1, 8, f) != 8 || memcmp(magic, "TISCKPT1", 8) != 0 || fread(head, 4, 2, f) != 2)
+        return bad("not a checkpoint written by tis_checkpoint_save");
+    if (head[0] != (int32_t)h->groups.size() || head[1] != h->R)
+        return bad("replica groups or replicas differ from the handle's");
+    std::vector<char> buf;
+    for (Group *g : h->groups) {
+        int32_t gh[5];
+        if (fread(gh, 4, 5, f) != 5) return bad("truncated");
+        if (gh[0] != g->R || gh[1] != g->P) return bad("a replica group's size differs from the handle's");
+        TIS_CUDA(cudaStreamSynchronize(g->stream));
+        if (gh[2] != g->dev.cap_sr || gh[3] != g->dev.cap_lr) {
+            const int rc = grow_lists(g, gh[2], gh[3]);  // the saved list capacity
+            if (rc) {
+                fclose(f);
+                return rc;
+            }
+        }
+        for (const auto &e : step_state(g)) {
+            uint64_t n = 0;
+            if (fread(&n, 8, 1, f) != 1 || n != e.second) return bad("an array's size differs from the handle's");
+            buf.resize(n);
+            if (fread(buf.data(), 1, n, f) != n) return bad("truncated");
+            if (n) TIS_CUDA(cudaMemcpy(e.first, buf.data(), n, cudaMemcpyHostToDevice));
+        }
+        g->lists_built = gh[4] != 0;
+    }
+    fclose(f);
+    return TIS_OK;
+}
+
 int tis_param_grad(tis_handle *h, double *out)
 {
     if (!h || !out) return fail(TIS_ERR_ARG, "tis_param_grad: bad argument");

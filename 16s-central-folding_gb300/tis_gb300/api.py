@@ -116,6 +116,8 @@ def _declare(L):
         "tis_write_psf": [vp, cp],
         "tis_write_cgpdb": [vp, dp, dp, dp, cp],
         "tis_capture_graph": [vp, i32],
+        "tis_checkpoint_save": [vp, cp],
+        "tis_checkpoint_load": [vp, cp],
         "tis_write_dcd": [vp, i32, cp, i32, C.c_double],
         "tis_traj_grad": [vp, i64, i32, C.POINTER(dp), dp, C.POINTER(dp)],
     }
@@ -135,7 +137,7 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
             "tis_param_grad", "tis_traj_grad", "tis_autotune", "tis_density_create", "tis_density_add",
             "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd", "tis_capture_graph",
-            "tis_write_cgpdb"]
+            "tis_write_cgpdb", "tis_checkpoint_save", "tis_checkpoint_load"]
 
 
 def read_last_frame(path, n):
@@ -475,6 +477,12 @@ class Engine:
 
     def step(self, n):
         _check(lib().tis_step(self.h, n))
+
+    def checkpoint_save(self, path):
+        _check(lib().tis_checkpoint_save(self.h, os.fsencode(path)))
+
+    def checkpoint_load(self, path):
+        _check(lib().tis_checkpoint_load(self.h, os.fsencode(path)))
 
     def capture_graph(self, steps):
         _check(lib().tis_capture_graph(self.h, int(steps)))

@@ -281,6 +281,15 @@ int tis_get_stack_energies(tis_handle *h, int replica, double *out, int64_t cap,
 /* Step counter (klok), rebuild count and rand() draws consumed by one replica. */
 int tis_get_counters(tis_handle *h, int replica, int64_t *klok, int64_t *rebuilds, int64_t *draws);
 
+/* Bit-exact checkpoint of the whole engine state (no counterpart in the reference,
+ * whose restart, tis_read_last_frame, resumes from positions only): x, x_old, v,
+ * the held LR force, every replica's counters and rand() position, the neighbour
+ * lists and H-bond status of every replica group.  A handle created with the same
+ * systems and run parameters continues from a loaded checkpoint exactly as the
+ * saving handle would have continued (bit for bit in mixed precision). */
+int tis_checkpoint_save(tis_handle *h, const char *path);
+int tis_checkpoint_load(tis_handle *h, const char *path);
+
 /* Number of replicas, particles of one replica, and the CUDA stream (cudaStream_t). */
 int tis_get_info(tis_handle *h, int *n_replicas, int *device, void **stream);
 int tis_replica_size(tis_handle *h, int replica, int *n_particles);

@@ -229,3 +229,28 @@ def test_contact_concentration_formula():
     got = contact_concentration([12, 0, 3], 40)
     want = [c / (40 * 4 / 3.0 * math.pi * (cut ** 3) * 6.02214 / (10 ** 4)) for c in (12, 0, 3)]
     assert np.allclose(got, want, rtol=1e-15)
+
+
+@pytest.mark.gpu
+def test_checkpoint_resumes_bit_for_bit(tmp_path):
+    """tis_checkpoint_save / _load: a fresh handle continues exactly as the saving
+    one (lists, held LR force, counters and rand() positions included)."""
+    systems = [load(golden_inputs(), "small", seed=s) for s in (3, 4, 5)]
+    path = str(tmp_path / "run.ckpt")
+    a = Engine(systems, groups=2)
+    a.populate_lists()
+    a.step(137)  # mid-interval of the LR refresh, lists some steps old
+    a.checkpoint_save(path)
+    a.step(150)
+    ref = a.get_states()
+    ref_c = [a.counters(r) for r in range(3)]
+    b = Engine(systems, groups=2)
+    b.checkpoint_load(path)
+    b.step(150)
+    got = b.get_states()
+    for k in ref:
+        assert np.array_equal(got[k], ref[k]), k
+    assert [b.counters(r) for r in range(3)] == ref_c
+    c = Engine(systems, groups=1)
+    with pytest.raises(TisError):
+        c.checkpoint_load(path)
