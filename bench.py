@@ -272,9 +272,15 @@ def gpu_arm(args):
         tune = {"groups": args.groups, "graph_steps": args.graph_steps, "lanes_sr": args.lanes_sr,
                 "lanes_lr": args.lanes_lr}
         tune_s = None
+        tune_note = "--groups"
         if args.groups == 0:
             t0 = time.perf_counter()
-            tune, _ = autotune(systems, steps=1000, precision=PREC_MIXED, device=local)
+            try:
+                tune, _ = autotune(systems, steps=1000, precision=PREC_MIXED, device=local)
+                tune_note = "tis_autotune (1000 steps per trial)"
+            except Exception as exc:  # the library's defaults if tuning fails
+                tune = {"groups": 0, "graph_steps": GRAPH_STEPS, "lanes_sr": 1, "lanes_lr": 4}
+                tune_note = f"library defaults (tis_autotune failed: {exc})"
             tune_s = time.perf_counter() - t0
         eng = Engine(systems, precision=PREC_MIXED, device=local, use_graph=1, **tune)
         graph_steps = eng.params.graph_steps
@@ -470,7 +476,7 @@ def gpu_arm(args):
                        "replicas_per_gpu": N_REPLICAS, "particles_per_gpu": n_part, "precision": "mixed",
                        "graph_steps": graph_steps, "replica_groups": eng.params.groups or (3 * N_REPLICAS + 15) // 16,
                        "lanes_sr": eng.params.lanes_sr or 1, "lanes_lr": eng.params.lanes_lr or 4,
-                       "launch_config": "tis_autotune (1000 steps per trial)" if tune_s is not None else "--groups",
+                       "launch_config": tune_note,
                        "autotune_s": tune_s,
                        "l2": "flushed (256 MB write) between timed iterations of "
                                                          f"{graph_steps} steps", "parallelism": f"replicas x{world}"},
