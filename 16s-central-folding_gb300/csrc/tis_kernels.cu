@@ -21,6 +21,12 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// Programmatic dependent launch: the kernels of a step's sequential chain are
+// launched so that their blocks may be scheduled while the previous kernel on
+// the stream drains; each waits here, before its first global access, until that
+// kernel has finished and its writes are visible (a no-op for a normal launch).
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // position and force accessors
 // ---------------------------------------------------------------------------
@@ -1048,6 +1054,7 @@ __device__ inline bool bounded(double x)
 template <bool D>
 __global__ void k_shift(Dev d)
 {
+    wait_prior_grid();
     const int r = blockIdx.x;
     const RepParams *R = d.rp + r;
     if (threadIdx.x == 0) {
@@ -1064,6 +1071,7 @@ __global__ void k_shift(Dev d)
 template <bool D>
 __global__ void __launch_bounds__(kBlock / kIntPer) k_integrate(Dev d)
 {
+    wait_prior_grid();
     const int r = d.blk_rep[blockIdx.x];
     const RepParams *R = d.rp + r;
     __shared__ unsigned long long s_max;
@@ -1240,6 +1248,7 @@ constexpr int kCellThreads = 1024;
 template <bool D>
 __global__ void __launch_bounds__(kCellThreads) k_cells(Dev d)
 {
+    wait_prior_grid();
     extern __shared__ int s_cells[];
     __shared__ int s_warp[32];
     __shared__ int s_carry;
@@ -1409,6 +1418,7 @@ __device__ inline int axis_neighbours(int i, int m, int out[3])
 template <bool D>
 __global__ void __launch_bounds__(128) k_pair_search(Dev d)
 {
+    wait_prior_grid();
     __shared__ int s_pre[4][32], s_beg[4][32];  // per warp: candidate offsets and first slots of its cells
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -1762,16 +1772,34 @@ void launch_noise(const Dev &d, cudaStream_t s)
     else k_noise<false><<<d.R, kTopoThreads, 0, s>>>(d);
 }
 
+// a launch that may begin before the previous kernel on the stream has finished
+// (the kernel waits in wait_prior_grid)
+template <class K>
+void launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t s, const Dev &d)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, d);
+}
+
 void launch_shift(const Dev &d, cudaStream_t s)
 {
-    if (d.fp64) k_shift<true><<<d.R, 32, 0, s>>>(d);
-    else k_shift<false><<<d.R, 32, 0, s>>>(d);
+    if (d.fp64) launch_pdl(k_shift<true>, d.R, 32, 0, s, d);
+    else launch_pdl(k_shift<false>, d.R, 32, 0, s, d);
 }
 
 void launch_move(const Dev &d, cudaStream_t s)
 {
-    if (d.fp64) k_integrate<true><<<d.nblk, kBlock / kIntPer, 0, s>>>(d);
-    else k_integrate<false><<<d.nblk, kBlock / kIntPer, 0, s>>>(d);
+    if (d.fp64) launch_pdl(k_integrate<true>, d.nblk, kBlock / kIntPer, 0, s, d);
+    else launch_pdl(k_integrate<false>, d.nblk, kBlock / kIntPer, 0, s, d);
 }
 
 void launch_integrate(const Dev &d, cudaStream_t s)
@@ -1782,14 +1810,14 @@ void launch_integrate(const Dev &d, cudaStream_t s)
 
 void launch_cells(const Dev &d, cudaStream_t s)
 {
-    if (d.fp64) k_cells<true><<<d.R, kCellThreads, d.cell_smem, s>>>(d);
-    else k_cells<false><<<d.R, kCellThreads, d.cell_smem, s>>>(d);
+    if (d.fp64) launch_pdl(k_cells<true>, d.R, kCellThreads, d.cell_smem, s, d);
+    else launch_pdl(k_cells<false>, d.R, kCellThreads, d.cell_smem, s, d);
 }
 
 void launch_search(const Dev &d, cudaStream_t s)
 {
-    if (d.fp64) k_pair_search<true><<<d.search_warps / 4, 128, 0, s>>>(d);
-    else k_pair_search<false><<<d.search_warps / 4, 128, 0, s>>>(d);
+    if (d.fp64) launch_pdl(k_pair_search<true>, d.search_warps / 4, 128, 0, s, d);
+    else launch_pdl(k_pair_search<false>, d.search_warps / 4, 128, 0, s, d);
 }
 
 void launch_rebuild(const Dev &d, cudaStream_t s)
