@@ -71,34 +71,39 @@ __device__ inline DualT<T> dsqrt(DualT<T> a)
     return {s, s > T(0) ? T(0.5) * a.d / s : T(0)};
 }
 
-// FP64 duals for the restraint terms and the parameter derivatives; the pair
-// Jacobian of a mixed-precision engine runs in FP32 duals (FP64 sums)
+// The restraint terms and the pair Jacobian of a mixed-precision engine run in
+// FP32 duals (differences taken in FP64 first, sums in FP64); FP64 engines and
+// the parameter derivatives in FP64 duals
 using Dual = DualT<double>;
-__device__ inline Dual cst(double v) { return {v, 0.0}; }
-__device__ inline Dual dexp(Dual a)
+template <class T>
+__device__ inline DualT<T> dexp(DualT<T> a)
 {
-    const double e = exp(a.v);
+    const T e = exp(a.v);
     return {e, e * a.d};
 }
-__device__ inline Dual datan2(Dual y, Dual x)
+template <class T>
+__device__ inline DualT<T> datan2(DualT<T> y, DualT<T> x)
 {
-    const double n = x.v * x.v + y.v * y.v;
-    return {atan2(y.v, x.v), n > 0.0 ? (x.v * y.d - y.v * x.d) / n : 0.0};
+    const T n = x.v * x.v + y.v * y.v;
+    return {atan2(y.v, x.v), n > T(0) ? (x.v * y.d - y.v * x.d) / n : T(0)};
 }
 
-using DV = V3<Dual>;
+template <class T>
+using DVT = V3<DualT<T>>;
 
-// positions (FP64 arrays) with the tangent (3P, component-major) as derivative
+// positions (FP64 arrays) with the tangent (3P, component-major) as derivative;
+// differences are formed in FP64 and then rounded to T
+template <class T>
 struct APos {
     const double *x, *y, *z, *t;
     int P;
-    __device__ DV at(int i) const
-    {
-        if (!t) return {cst(x[i]), cst(y[i]), cst(z[i])};
-        return {{x[i], t[i]}, {y[i], t[P + i]}, {z[i], t[2 * P + i]}};
-    }
     // position(b) - position(a), raw difference (the bonded terms' convention)
-    __device__ DV vec(int a, int b) const { return at(b) - at(a); }
+    __device__ DVT<T> vec(int a, int b) const
+    {
+        const T dx = (T)(x[b] - x[a]), dy = (T)(y[b] - y[a]), dz = (T)(z[b] - z[a]);
+        if (!t) return {{dx, T(0)}, {dy, T(0)}, {dz, T(0)}};
+        return {{dx, (T)(t[b] - t[a])}, {dy, (T)(t[P + b] - t[P + a])}, {dz, (T)(t[2 * P + b] - t[2 * P + a])}};
+    }
 };
 
 // Force contributions of one term evaluated at unit strength: the derivative
@@ -106,6 +111,7 @@ struct APos {
 // times the term's strength, added to jv once per atom by flush(); lambda . value
 // is summed in w (lambda = the tangent direction).
 constexpr int kSlots = 7;
+template <class T>
 struct AAcc {
     double *jv;
     const double *lam;
@@ -122,17 +128,17 @@ struct AAcc {
             acc[s][0] = acc[s][1] = acc[s][2] = 0.0;
         }
     }
-    __device__ void add(int i, DV g)
+    __device__ void add(int i, DVT<T> g)
     {
         if (jv)
 #pragma unroll
             for (int s = 0; s < kSlots; ++s)
                 if (ids[s] == i) {  // a slot per atom: registers, no atomics until flush
-                    acc[s][0] += g.x.d;
-                    acc[s][1] += g.y.d;
-                    acc[s][2] += g.z.d;
+                    acc[s][0] += (double)g.x.d;
+                    acc[s][1] += (double)g.y.d;
+                    acc[s][2] += (double)g.z.d;
                 }
-        if (lam) w += lam[i] * g.x.v + lam[P + i] * g.y.v + lam[2 * P + i] * g.z.v;
+        if (lam) w += lam[i] * (double)g.x.v + lam[P + i] * (double)g.y.v + lam[2 * P + i] * (double)g.z.v;
     }
     __device__ void flush()
     {
@@ -147,68 +153,75 @@ struct AAcc {
     }
 };
 
-__device__ inline DV neg(DV a) { return {-a.x, -a.y, -a.z}; }
+template <class T>
+__device__ inline DVT<T> neg(DVT<T> a) { return {-a.x, -a.y, -a.z}; }
 
 // ---------------------------------------------------------------------------
 // the restraint terms (E:924-1454) over dual numbers
 // ---------------------------------------------------------------------------
-__device__ Dual angle_of(const APos &P, int i1, int i2, int i3)
+template <class T>
+__device__ DualT<T> angle_of(const APos<T> &P, int i1, int i2, int i3)
 {
-    const DV a = P.vec(i2, i1), b = P.vec(i2, i3);
-    const DV w = cross(a, b);
+    const DVT<T> a = P.vec(i2, i1), b = P.vec(i2, i3);
+    const DVT<T> w = cross(a, b);
     return datan2(dsqrt(dot(w, w)), dot(a, b));
 }
 
-__device__ Dual dihedral_of(const APos &P, int i1, int i2, int i3, int i4)
+template <class T>
+__device__ DualT<T> dihedral_of(const APos<T> &P, int i1, int i2, int i3, int i4)
 {
-    const DV v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
-    const DV m = cross(v1, v2), n = cross(v2, v3);
+    const DVT<T> v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
+    const DVT<T> m = cross(v1, v2), n = cross(v2, v3);
     return datan2(dot(v1, n) * dsqrt(dot(v2, v2)), dot(m, n));
 }
 
 // force of V = k0 (r0 - r)^2 on i1, i2
-__device__ void bond_force(const APos &P, AAcc &A, int i1, int i2, Dual k0, double r0)
+template <class T>
+__device__ void bond_force(const APos<T> &P, AAcc<T> &A, int i1, int i2, DualT<T> k0, double r0)
 {
-    const DV v = P.vec(i1, i2);
-    const Dual r = dsqrt(dot(v, v));
-    const Dual t = 2.0 * k0 * (r0 - r) / r;
-    const DV g = t * v;
+    const DVT<T> v = P.vec(i1, i2);
+    const DualT<T> r = dsqrt(dot(v, v));
+    const DualT<T> t = T(2) * k0 * ((T)r0 - r) / r;
+    const DVT<T> g = t * v;
     A.add(i1, neg(g));
     A.add(i2, g);
 }
 
 // force of V = k0 (th0 - theta)^2 at i2; clamp: none once cos theta < -0.99995 (E:1138-1251)
-__device__ void angle_force(const APos &P, AAcc &A, int i1, int i2, int i3, Dual k0, double th0, bool clamp)
+template <class T>
+__device__ void angle_force(const APos<T> &P, AAcc<T> &A, int i1, int i2, int i3, DualT<T> k0, double th0, bool clamp)
 {
-    const DV a = P.vec(i2, i1), b = P.vec(i2, i3);
-    const Dual aa = dot(a, a), bb = dot(b, b), ab = dot(a, b);
-    if (clamp && ab.v / sqrt(aa.v * bb.v) < -0.99995) return;
-    const DV w = cross(a, b);
-    const Dual ww = dsqrt(dot(w, w));
-    if (ww.v == 0.0) return;
-    const Dual th = datan2(ww, ab);
-    const Dual s = 2.0 * k0 * (th0 - th) / ww;
-    const DV g1 = (s / aa) * cross(a, w);
-    const DV g3 = (-s / bb) * cross(b, w);
+    const DVT<T> a = P.vec(i2, i1), b = P.vec(i2, i3);
+    const DualT<T> aa = dot(a, a), bb = dot(b, b), ab = dot(a, b);
+    if (clamp && ab.v / sqrt(aa.v * bb.v) < T(-0.99995)) return;
+    const DVT<T> w = cross(a, b);
+    const DualT<T> ww = dsqrt(dot(w, w));
+    if (ww.v == T(0)) return;
+    const DualT<T> th = datan2(ww, ab);
+    const DualT<T> s = T(2) * k0 * ((T)th0 - th) / ww;
+    const DVT<T> g1 = (s / aa) * cross(a, w);
+    const DVT<T> g3 = (-s / bb) * cross(b, w);
     A.add(i1, g1);
     A.add(i2, neg(g1 + g3));
     A.add(i3, g3);
 }
 
 // force of V = k0 (psi0 - psi)^2 of the dihedral i1-i2-i3-i4 (E:1306-1454)
-__device__ void dihedral_force(const APos &P, AAcc &A, int i1, int i2, int i3, int i4, Dual k0, double psi0)
+template <class T>
+__device__ void dihedral_force(const APos<T> &P, AAcc<T> &A, int i1, int i2, int i3, int i4, DualT<T> k0,
+                               double psi0)
 {
-    const DV v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
-    const DV m = cross(v1, v2), n = cross(v2, v3);
-    const Dual mm = dot(m, m), nn = dot(n, n), v22 = dot(v2, v2);
-    if (mm.v == 0.0 || nn.v == 0.0) return;
-    const Dual l2 = dsqrt(v22);
-    const Dual psi = datan2(dot(v1, n) * l2, dot(m, n));
-    const Dual c = 2.0 * k0 * (psi0 - psi);
-    const DV g1 = (-c * l2 / mm) * m;
-    const DV g4 = (c * l2 / nn) * n;
-    const Dual p = dot(v1, v2) / v22, q = dot(v3, v2) / v22;
-    const DV g2 = (-1.0 - p) * g1 + q * g4;
+    const DVT<T> v1 = P.vec(i1, i2), v2 = P.vec(i2, i3), v3 = P.vec(i3, i4);
+    const DVT<T> m = cross(v1, v2), n = cross(v2, v3);
+    const DualT<T> mm = dot(m, m), nn = dot(n, n), v22 = dot(v2, v2);
+    if (mm.v == T(0) || nn.v == T(0)) return;
+    const DualT<T> l2 = dsqrt(v22);
+    const DualT<T> psi = datan2(dot(v1, n) * l2, dot(m, n));
+    const DualT<T> c = T(2) * k0 * ((T)psi0 - psi);
+    const DVT<T> g1 = (-c * l2 / mm) * m;
+    const DVT<T> g4 = (c * l2 / nn) * n;
+    const DualT<T> p = dot(v1, v2) / v22, q = dot(v3, v2) / v22;
+    const DVT<T> g2 = (T(-1) - p) * g1 + q * g4;
     A.add(i1, g1);
     A.add(i2, g2);
     A.add(i3, neg(g1 + g2 + g4));
@@ -225,38 +238,42 @@ __device__ inline int branch_of(double psi, double nat)
 __device__ inline double shifted(double nat, int br) { return nat + 2.0 * 3.14159265358979323846 * br; }
 
 // the six-term native-geometry restraint sum q (E:1983-2056, E:2177-2231)
-__device__ Dual six_q(const APos &P, const int *k, const double *nat, Dual rdev, double init, int br[3])
+template <class T>
+__device__ DualT<T> six_q(const APos<T> &P, const int *k, const double *nat, DualT<T> rdev, double init, int br[3])
 {
-    const Dual t1 = angle_of(P, k[0], k[1], k[4]);
-    const Dual t2 = angle_of(P, k[3], k[4], k[1]);
-    const Dual p0 = dihedral_of(P, k[0], k[1], k[4], k[3]);
-    const Dual p1 = dihedral_of(P, k[4], k[1], k[0], k[2]);
-    const Dual p2 = dihedral_of(P, k[1], k[4], k[3], k[5]);
-    br[0] = branch_of(p0.v, nat[3]);
-    br[1] = branch_of(p1.v, nat[4]);
-    br[2] = branch_of(p2.v, nat[5]);
-    const Dual d0 = p0 - shifted(nat[3], br[0]), d1 = p1 - shifted(nat[4], br[1]), d2 = p2 - shifted(nat[5], br[2]);
-    Dual q = init + 5.0 * rdev * rdev;
-    q = q + 1.5 * (t1 - nat[1]) * (t1 - nat[1]);
-    q = q + 1.5 * (t2 - nat[2]) * (t2 - nat[2]);
-    q = q + 0.15 * d0 * d0 + 0.15 * d1 * d1 + 0.15 * d2 * d2;
+    const DualT<T> t1 = angle_of(P, k[0], k[1], k[4]);
+    const DualT<T> t2 = angle_of(P, k[3], k[4], k[1]);
+    const DualT<T> p0 = dihedral_of(P, k[0], k[1], k[4], k[3]);
+    const DualT<T> p1 = dihedral_of(P, k[4], k[1], k[0], k[2]);
+    const DualT<T> p2 = dihedral_of(P, k[1], k[4], k[3], k[5]);
+    br[0] = branch_of((double)p0.v, nat[3]);
+    br[1] = branch_of((double)p1.v, nat[4]);
+    br[2] = branch_of((double)p2.v, nat[5]);
+    const DualT<T> d0 = p0 - (T)shifted(nat[3], br[0]), d1 = p1 - (T)shifted(nat[4], br[1]),
+                   d2 = p2 - (T)shifted(nat[5], br[2]);
+    DualT<T> q = (T)init + T(5) * rdev * rdev;
+    q = q + T(1.5) * (t1 - (T)nat[1]) * (t1 - (T)nat[1]);
+    q = q + T(1.5) * (t2 - (T)nat[2]) * (t2 - (T)nat[2]);
+    q = q + T(0.15) * d0 * d0 + T(0.15) * d1 * d1 + T(0.15) * d2 * d2;
     return q;
 }
 
 // force of V = w q for the six-term restraint
-__device__ void six_force(const APos &P, AAcc &A, const int *k, const double *nat, const int br[3], Dual w)
+template <class T>
+__device__ void six_force(const APos<T> &P, AAcc<T> &A, const int *k, const double *nat, const int br[3], DualT<T> w)
 {
-    bond_force(P, A, k[1], k[4], 5.0 * w, nat[0]);
-    angle_force(P, A, k[0], k[1], k[4], 1.5 * w, nat[1], true);
-    angle_force(P, A, k[3], k[4], k[1], 1.5 * w, nat[2], true);
-    dihedral_force(P, A, k[0], k[1], k[4], k[3], 0.15 * w, shifted(nat[3], br[0]));
-    dihedral_force(P, A, k[4], k[1], k[0], k[2], 0.15 * w, shifted(nat[4], br[1]));
-    dihedral_force(P, A, k[1], k[4], k[3], k[5], 0.15 * w, shifted(nat[5], br[2]));
+    bond_force(P, A, k[1], k[4], T(5) * w, nat[0]);
+    angle_force(P, A, k[0], k[1], k[4], T(1.5) * w, nat[1], true);
+    angle_force(P, A, k[3], k[4], k[1], T(1.5) * w, nat[2], true);
+    dihedral_force(P, A, k[0], k[1], k[4], k[3], T(0.15) * w, shifted(nat[3], br[0]));
+    dihedral_force(P, A, k[4], k[1], k[0], k[2], T(0.15) * w, shifted(nat[4], br[1]));
+    dihedral_force(P, A, k[1], k[4], k[3], k[5], T(0.15) * w, shifted(nat[5], br[2]));
 }
 
-__device__ inline Dual distance(const APos &P, int a, int b)
+template <class T>
+__device__ inline DualT<T> distance(const APos<T> &P, int a, int b)
 {
-    const DV v = P.vec(a, b);
+    const DVT<T> v = P.vec(a, b);
     return dsqrt(dot(v, v));
 }
 
@@ -418,8 +435,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const doub
 // ---------------------------------------------------------------------------
 constexpr int kAdjTopoThreads = 128;
 
+template <class T>
 __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, const double *tan, int mode)
 {
+    using DT = DualT<T>;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int kind, item;
     if (t < d.nbt) { kind = 0; item = t; }
@@ -429,8 +448,8 @@ __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, c
     else return;
     if (kind == 0 && mode == 0) return;  // no parameter of this set enters the bonded terms
     if (kind == 3 && !a.rhb[item]) return;
-    const APos P{a.px, a.py, a.pz, mode == 1 ? tan : nullptr, d.P};
-    AAcc A{mode == 1 ? a.jv : nullptr, mode == 1 ? tan : nullptr, d.P, 1.0, 0.0, {}, {}};
+    const APos<T> P{a.px, a.py, a.pz, mode == 1 ? tan : nullptr, d.P};
+    AAcc<T> A{mode == 1 ? a.jv : nullptr, mode == 1 ? tan : nullptr, d.P, 1.0, 0.0, {}, {}};
     int r = 0, param = -1;
     double dE = 0.0, u1 = 0.0;
     if (kind == 0) {
@@ -438,8 +457,9 @@ __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, c
         const double2 par = d.bt_par[item];
         const int at[3] = {id.x, id.y, id.z};
         A.atoms(at, id.w == 0 ? 2 : 3);
-        if (id.w == 0) bond_force(P, A, id.x, id.y, cst(par.x), par.y);
-        else angle_force(P, A, id.x, id.y, id.z, cst(par.x), par.y, false);
+        const DT k0 = {(T)par.x, T(0)};
+        if (id.w == 0) bond_force(P, A, id.x, id.y, k0, par.y);
+        else angle_force(P, A, id.x, id.y, id.z, k0, par.y, false);
         A.flush();
         return;
     } else if (kind == 1) {  // tertiary: U = st_E / (1 + q), st_E = -st_D
@@ -447,15 +467,15 @@ __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, c
         const double *nat = d.st3_nat + 6 * item;
         r = d.rep_of[id[0]];
         int br[3];
-        const Dual rdev = distance(P, id[1], id[4]) - nat[0];
-        const Dual Dn = six_q(P, id, nat, rdev, 1.0, br);
-        u1 = 1.0 / Dn.v;
+        const DT rdev = distance(P, id[1], id[4]) - (T)nat[0];
+        const DT Dn = six_q(P, id, nat, rdev, 1.0, br);
+        u1 = 1.0 / (double)Dn.v;
         param = 4;
         dE = -1.0;
         if (mode == 1) {
             A.scale = d.st3_E[item];
             A.atoms(id, 6);
-            six_force(P, A, id, nat, br, -1.0 / (Dn * Dn));
+            six_force(P, A, id, nat, br, T(-1) / (Dn * Dn));
             A.flush();
         }
     } else if (kind == 2) {  // secondary: U = st_E / (1 + 1.4 dr^2 + 4 dpsi1^2 + 4 dpsi2^2)
@@ -464,25 +484,26 @@ __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, c
         for (int u = d.st2_offby_off[item]; u < d.st2_offby_off[item + 1]; ++u) {  // E:1960-1981
             const int k = d.st2_offby_idx[u];
             const int *tid = d.st3_idx + 6 * k;
-            if (distance(P, tid[1], tid[4]).v - d.st3_nat[6 * k] < 10.0) return;
+            if ((double)distance(P, tid[1], tid[4]).v - d.st3_nat[6 * k] < 10.0) return;
         }
-        const Dual rr = distance(P, id[2], id[5]);
-        const Dual p1 = dihedral_of(P, id[0], id[1], id[3], id[4]);
-        const Dual p2 = dihedral_of(P, id[6], id[4], id[3], id[1]);
-        const double p10 = shifted(-2.58684, branch_of(p1.v, -2.58684));
-        const double p20 = shifted(3.07135, branch_of(p2.v, 3.07135));
+        const DT rr = distance(P, id[2], id[5]);
+        const DT p1 = dihedral_of(P, id[0], id[1], id[3], id[4]);
+        const DT p2 = dihedral_of(P, id[6], id[4], id[3], id[1]);
+        const double p10 = shifted(-2.58684, branch_of((double)p1.v, -2.58684));
+        const double p20 = shifted(3.07135, branch_of((double)p2.v, 3.07135));
         const double r0 = d.st2_r0[item];
-        const Dual Dn = 1.0 + 1.4 * (rr - r0) * (rr - r0) + 4.0 * (p1 - p10) * (p1 - p10) + 4.0 * (p2 - p20) * (p2 - p20);
-        u1 = 1.0 / Dn.v;
+        const DT Dn = T(1) + T(1.4) * (rr - (T)r0) * (rr - (T)r0) + T(4) * (p1 - (T)p10) * (p1 - (T)p10) +
+                      T(4) * (p2 - (T)p20) * (p2 - (T)p20);
+        u1 = 1.0 / (double)Dn.v;
         param = a.st2_cls[item];
         dE = a.st2_dss[item];
         if (mode == 1) {
             A.scale = d.st2_E[item];
             A.atoms(id, 7);
-            const Dual w = -1.0 / (Dn * Dn);
-            bond_force(P, A, id[2], id[5], 1.4 * w, r0);
-            dihedral_force(P, A, id[0], id[1], id[3], id[4], 4.0 * w, p10);
-            dihedral_force(P, A, id[6], id[4], id[3], id[1], 4.0 * w, p20);
+            const DT w = T(-1) / (Dn * Dn);
+            bond_force(P, A, id[2], id[5], T(1.4) * w, r0);
+            dihedral_force(P, A, id[0], id[1], id[3], id[4], T(4) * w, p10);
+            dihedral_force(P, A, id[6], id[4], id[3], id[1], T(4) * w, p20);
             A.flush();
         }
     } else {  // formed H-bond: U = hb_E exp(-q)
@@ -490,10 +511,10 @@ __global__ void __launch_bounds__(kAdjTopoThreads) k_adj_topo(Dev d, AdjDev a, c
         const double *nat = d.hb_nat + 6 * item;
         r = d.rep_of[id[0]];
         int br[3];
-        const Dual rdev = distance(P, id[1], id[4]) - nat[0];
-        const Dual q = six_q(P, id, nat, rdev, 0.0, br);
-        const Dual e = dexp(-q);
-        u1 = e.v;
+        const DT rdev = distance(P, id[1], id[4]) - (T)nat[0];
+        const DT q = six_q(P, id, nat, rdev, 0.0, br);
+        const DT e = dexp(-q);
+        u1 = (double)e.v;
         param = 5;
         dE = a.hb_dhs[item];
         if (mode == 1) {
@@ -661,7 +682,10 @@ void launch_adj_pair(const Dev &d, const AdjDev &a, cudaStream_t s, bool lr, con
 void launch_adj_topo(const Dev &d, const AdjDev &a, cudaStream_t s, const double *tan, int mode)
 {
     const int n = d.nbt + d.nst3 + d.nst2 + a.nhb;
-    if (n > 0) k_adj_topo<<<(n + kAdjTopoThreads - 1) / kAdjTopoThreads, kAdjTopoThreads, 0, s>>>(d, a, tan, mode);
+    if (n <= 0) return;
+    const int nb = (n + kAdjTopoThreads - 1) / kAdjTopoThreads;
+    if (mode == 1 && !d.fp64) k_adj_topo<float><<<nb, kAdjTopoThreads, 0, s>>>(d, a, tan, mode);
+    else k_adj_topo<double><<<nb, kAdjTopoThreads, 0, s>>>(d, a, tan, mode);
 }
 
 void launch_adj_step(const Dev &d, const AdjDev &a, cudaStream_t s)
