@@ -3,6 +3,7 @@
 //   tis_run [-D<ss_D>] [-E<hs_D>] [-d<st_D>] [-T<T>] [-c<c_Mg>] [-f<c_K>] [-s<seed>]
 //           [--steps N] [--every N] [--replicas R] [--precision mixed|fp64] [--device K]
 //           [--pdb F] [--bonds F] [--stacks F] [--maxikey F] [--box L] [--rc A] [--center B]
+//           [--checkpoint FILE] [--dcd] [--tune]
 //
 // The single-letter flags are the reference's (E:6082-6099) with its defaults;
 // the input files default to the reference's names in the working directory.
@@ -12,7 +13,12 @@
 // and its restart: an existing Coordinates file resumes from its last frame, at
 // step frames * every, with x_old = x - v h (E:6181-6211).  --replicas R runs seeds s, s+1, ..., s+R-1 in
 // one process, each with its own files.  Steps run to --steps (default the
-// reference's 3 * 10^9).
+// reference's 3 * 10^9).  Beyond the reference: --checkpoint FILE saves the whole
+// engine state at every frame and, when FILE exists at start, continues from it
+// bit for bit instead of the positions-only restart; --dcd also appends every frame
+// to a DCD trajectory per replica (Trajectory_..._s<seed>.dcd); --tune measures the
+// launch configuration first (cached in tis_tune.txt).
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -84,6 +90,8 @@ int main(int argc, char **argv)
     tis_run_params_default(&rp);
     long long steps = 3000000000LL, every = 1000000, snap_every = 5000000;
     int replicas = 1;
+    std::string ckpt;
+    bool dcd = false, tune = false;
     for (int i = 1; i < argc; ++i) {
         const char *a = argv[i];
         auto next = [&](const char *flag) -> const char * {
@@ -106,6 +114,9 @@ int main(int argc, char **argv)
         else if (!strcmp(a, "--box")) lp.box = atof(next(a));
         else if (!strcmp(a, "--rc")) lp.rc = atof(next(a));
         else if (!strcmp(a, "--center")) lp.center = atoi(next(a));
+        else if (!strcmp(a, "--checkpoint")) ckpt = next(a);
+        else if (!strcmp(a, "--dcd")) dcd = true;
+        else if (!strcmp(a, "--tune")) tune = true;
         else if (a[0] == '-' && a[1] != '-') {
             switch (a[1]) {  // E:6082-6099
             case 'D': lp.ss_D = atof(a + 2); break;
@@ -136,10 +147,30 @@ int main(int argc, char **argv)
         if (report(tis_system_load(&q, &sys[r]), "set-up")) return 1;
         files[r] = names(lp, q.seed);
     }
+    if (tune) {
+        tis_run_params best;
+        if (report(tis_autotune(sys.data(), replicas, &rp, 1000, "tis_tune.txt", &best, nullptr), "tune")) return 1;
+        rp = best;
+    }
     tis_handle *h = nullptr;
     if (report(tis_create(sys.data(), replicas, &rp, &h), "tis_create")) return 1;
     long long klok_old = -1;  // every replica resumes at the same step (the first file's frames)
-    for (int r = 0; r < replicas; ++r) {
+    bool resumed = false;
+    if (!ckpt.empty()) {  // the bit-exact checkpoint and its step (FILE.klok) when present
+        FILE *probe = fopen(ckpt.c_str(), "rb");
+        if (probe) {
+            fclose(probe);
+            if (report(tis_checkpoint_load(h, ckpt.c_str()), "checkpoint")) return 1;
+            FILE *kf = fopen((ckpt + ".klok").c_str(), "r");
+            if (!kf || fscanf(kf, "%lld", &klok_old) != 1) {
+                fprintf(stderr, "tis_run: %s.klok missing or unreadable\n", ckpt.c_str());
+                return 1;
+            }
+            fclose(kf);
+            resumed = true;
+        }
+    }
+    for (int r = 0; r < replicas && !resumed; ++r) {
         int n = 0;
         tis_replica_size(h, r, &n);
         FILE *probe = fopen(files[r].coordinates.c_str(), "rb");
@@ -189,19 +220,35 @@ int main(int argc, char **argv)
             return 1;
     }
     if (klok_old < 0) klok_old = 0;
-    if (report(tis_populate_lists(h), "populate_lists")) return 1;
+    if (!resumed && report(tis_populate_lists(h), "populate_lists")) return 1;
+    double step_h = 0.05;
+    {
+        int dt = 0;
+        const void *pv = nullptr;
+        int64_t cnt = 0;
+        if (tis_system_get(sys[0], "h", &dt, &pv, &cnt) == TIS_OK && pv && dt == TIS_F64) step_h = ((const double *)pv)[0];
+    }
 
     // the run loop (E:6274-6387): a frame at every multiple of `every`, before that step
     const long long end = steps + 1;
     long long klok = klok_old + 1;
+    bool skip_frame = resumed;  // a checkpoint is saved after its frame was written
     while (klok < end) {
-        if (klok % every == 0) {
+        if (klok % every == 0 && !skip_frame) {
             if (report(tis_sync(h), "step")) return 1;
             for (int r = 0; r < replicas; ++r) {
                 if (report(tis_write_frame(h, r, files[r].contacts.c_str(), files[r].coordinates.c_str(),
                                            files[r].energies.c_str()),
                            "output"))
                     return 1;
+                if (dcd) {
+                    std::string trj = files[r].coordinates;
+                    trj.replace(0, strlen("Coordinates"), "Trajectory");
+                    trj.replace(trj.size() - 4, 4, ".dcd");
+                    if (report(tis_write_dcd(h, r, trj.c_str(), (int)std::min<long long>(every, 2147483647LL), step_h),
+                               "dcd"))
+                        return 1;
+                }
                 if (snap_every > 0 && (klok % snap_every == 0 || klok == end - 1)) {
                     const Names snap = names(lp, seed0 + r, true, klok / snap_every);
                     copy_file(files[r].contacts, snap.contacts);
@@ -216,6 +263,22 @@ int main(int argc, char **argv)
                 }
             }
         }
+        if (!ckpt.empty() && klok % every == 0 && !skip_frame) {  // checkpoint at every frame, replaced atomically
+            const std::string tmp = ckpt + ".tmp";
+            if (report(tis_checkpoint_save(h, tmp.c_str()), "checkpoint")) return 1;
+            FILE *kf = fopen((tmp + ".klok").c_str(), "w");
+            if (!kf) {
+                fprintf(stderr, "tis_run: cannot write %s.klok\n", tmp.c_str());
+                return 1;
+            }
+            fprintf(kf, "%lld\n", klok - 1);
+            fclose(kf);
+            if (rename(tmp.c_str(), ckpt.c_str()) != 0 || rename((tmp + ".klok").c_str(), (ckpt + ".klok").c_str()) != 0) {
+                fprintf(stderr, "tis_run: cannot replace %s\n", ckpt.c_str());
+                return 1;
+            }
+        }
+        skip_frame = false;
         long long next = (klok / every + 1) * every;
         if (next > end) next = end;
         if (report(tis_step(h, next - klok), "step")) return 1;

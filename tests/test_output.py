@@ -254,3 +254,35 @@ def test_checkpoint_resumes_bit_for_bit(tmp_path):
     c = Engine(systems, groups=1)
     with pytest.raises(TisError):
         c.checkpoint_load(path)
+
+
+@pytest.mark.gpu
+def test_cli_checkpoint_continues_bit_for_bit(tmp_path):
+    """tis_run --checkpoint: a run stopped at step 200 and started again to 400
+    writes the same files, frame for frame, as one run to 400; --dcd appends every
+    frame to a trajectory."""
+    _build.build()
+    g = golden_inputs()
+    args = [_build.RUN, "-T0.59219", "-c0.005", "-f0.05", "-s3", "--box", "200", "--rc", "30", "--center", "100",
+            "--every", "50", "--snapshot-every", "0", "--replicas", "2", "--checkpoint", "run.ckpt", "--dcd"]
+    for d in ("split", "whole"):
+        (tmp_path / d).mkdir()
+        for src, dst in [(g["pdb"], "16SCD.pdb"), (g["bonds"], "16SCD_16SCD_unprocessed_bonds.dat"),
+                         (g["stacks"], "16SCD_16SCD_unprocessed_stacks.dat"), (g["maxikey"], "MAXIKEY_Mg_Cl_K.dat")]:
+            shutil.copy(src, tmp_path / d / dst)
+    for steps in ("200", "400"):
+        subprocess.run(args + ["--steps", steps], cwd=tmp_path / "split", check=True, capture_output=True, text=True,
+                       timeout=300)
+    subprocess.run(args + ["--steps", "400"], cwd=tmp_path / "whole", check=True, capture_output=True, text=True,
+                   timeout=300)
+    base = "16SCD_EPS_Mg_Cl_K_D0.850_E3.975_d6.500_T0.592_cM0.0050_f0.050_s{}"
+    for seed in (3, 4):
+        for kind, ext in (("Coordinates", "dat"), ("Energies", "dat"), ("Contacts", "dat"), ("Trajectory", "dcd")):
+            name = f"{kind}_{base.format(seed)}.{ext}"
+            a = (tmp_path / "split" / name).read_bytes()
+            b = (tmp_path / "whole" / name).read_bytes()
+            assert a == b, name
+        energies = (tmp_path / "whole" / f"Energies_{base.format(seed)}.dat").read_text().splitlines()
+        assert len(energies) == 8
+        nset, _, _, frames = _read_dcd(str(tmp_path / "whole" / f"Trajectory_{base.format(seed)}.dcd"))
+        assert nset == 8 and len(frames) == 8
