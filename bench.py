@@ -429,7 +429,8 @@ def gpu_arm(args):
             t_tg = time.perf_counter() - t0
             adjoint = {"replicas": 16, "param_grad_frames_per_s": 16 / t_pg,
                        "traj_steps": 200, "checkpoint_every": 10, "traj_grad_s": t_tg,
-                       "traj_grad_replica_steps_per_s": 16 * 200 / t_tg, "precision": "mixed forward, FP64 adjoint"}
+                       "traj_grad_replica_steps_per_s": 16 * 200 / t_tg,
+                       "precision": "mixed forward; adjoint in FP32 dual numbers with FP64 sums"}
             adj.close()
 
         # the large system: a 1500-nt chain in a 600 A box with 1300 Mg, 22100 Cl,
