@@ -8,6 +8,8 @@
 #include <vector>
 
 #include "tis_host.h"
+#include <nvtx3/nvToolsExt.h>
+
 #include "tis_kernels.cuh"
 
 using tis::fail;
@@ -89,6 +91,14 @@ int64_t scalar_i64(const tis_system *s, const char *name, int64_t def)
 }
 
 int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// an NVTX range around one API call (header-only NVTX; no cost without a profiler)
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range &) = delete;
+    Range &operator=(const Range &) = delete;
+};
 
 }  // namespace
 
@@ -1627,6 +1637,7 @@ int tis_get_all_energies(tis_handle *h, double *out)
 
 int tis_populate_lists(tis_handle *h)
 {
+    Range range("tis_populate_lists");
     // every group's build is launched before any is checked, so the builds overlap
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     int rc = fork_groups(h);
@@ -1875,6 +1886,7 @@ int tis_get_forces(tis_handle *h, int r, double *forces)
 // counters with the rand() position, neighbour lists, H-bond status), per group.
 int tis_checkpoint_save(tis_handle *h, const char *path)
 {
+    Range range("tis_checkpoint_save");
     if (!h || !path) return fail(TIS_ERR_ARG, "tis_checkpoint_save: bad argument");
     TIS_CUDA(cudaSetDevice(h->prm.device));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
@@ -1902,6 +1914,7 @@ int tis_checkpoint_save(tis_handle *h, const char *path)
 
 int tis_checkpoint_load(tis_handle *h, const char *path)
 {
+    Range range("tis_checkpoint_load");
     if (!h || !path) return fail(TIS_ERR_ARG, "tis_checkpoint_load: bad argument");
     TIS_CUDA(cudaSetDevice(h->prm.device));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
@@ -1945,6 +1958,7 @@ int tis_checkpoint_load(tis_handle *h, const char *path)
 
 int tis_param_grad(tis_handle *h, double *out)
 {
+    Range range("tis_param_grad");
     if (!h || !out) return fail(TIS_ERR_ARG, "tis_param_grad: bad argument");
     return each_group(h, [&](Group *g) { return grp_param_grad(g, out + (size_t)g->base * tis::kNParams); });
 }
@@ -1952,6 +1966,7 @@ int tis_param_grad(tis_handle *h, double *out)
 int tis_traj_grad(tis_handle *h, int64_t steps, int32_t checkpoint_every, const double *const *seed, double *dtheta,
                   double *const *dstate0)
 {
+    Range range("tis_traj_grad");
     if (!h || steps < 1 || checkpoint_every < 1 || !dtheta) return fail(TIS_ERR_ARG, "tis_traj_grad: bad argument");
     int64_t off = 0;
     return each_group(h, [&](Group *g) {
@@ -1978,6 +1993,7 @@ int tis_check_shifts(tis_handle *h)
 
 int tis_step(tis_handle *h, int64_t n)
 {
+    Range range("tis_step");
     if (!h || n < 0) return fail(TIS_ERR_ARG, "tis_step: bad argument");
     return each_group(h, [n](Group *g) { return grp_step(g, n); });
 }
