@@ -286,3 +286,12 @@ def test_cli_checkpoint_continues_bit_for_bit(tmp_path):
         assert len(energies) == 8
         nset, _, _, frames = _read_dcd(str(tmp_path / "whole" / f"Trajectory_{base.format(seed)}.dcd"))
         assert nset == 8 and len(frames) == 8
+
+
+def test_cli_without_inputs_or_gpu_fails_cleanly(tmp_path):
+    """tis_run reports a missing input file (or, on a machine without a GPU, the
+    missing device) as an error message and exit status 1, without a crash."""
+    _build.build()
+    r = subprocess.run([_build.RUN, "--steps", "10"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1
+    assert "tis_run:" in r.stderr and "error" in r.stderr
