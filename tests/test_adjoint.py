@@ -76,6 +76,37 @@ def test_param_grad_matches_finite_differences(small, thermal):
     assert np.count_nonzero(g) >= 12  # every class of term is present in this system
 
 
+def oracle_potential(system, theta, state):
+    """The FP64 oracle's total potential energy at `state` with parameters theta."""
+    from oracle_bridge import Oracle
+    o = Oracle(with_params(system, theta).to_dict(), seed=int(system["seed"][0]))
+    o.set_state(state)
+    o.populate_lists()
+    t = o.terms()
+    return sum(t[k] for k in U_TERMS)
+
+
+@pytest.mark.gpu
+def test_param_grad_matches_oracle_finite_differences(small, thermal):
+    """The reference gradient: central differences (h = 1e-4 relative) of the CPU
+    oracle's FP64 total energy, the oracle being the reference's algorithm pinned
+    to the reference's own outputs."""
+    th0 = params_of(small)
+    g = param_grad(small, th0, thermal)
+    u0 = oracle_potential(small, th0, thermal)
+    rows = []
+    for j in range(N_PARAMS):
+        hj = 1e-4 * abs(th0[j])
+        tp, tm = th0.copy(), th0.copy()
+        tp[j] += hj
+        tm[j] -= hj
+        fd = (oracle_potential(small, tp, thermal) - oracle_potential(small, tm, thermal)) / (2 * hj)
+        tol = 1e-4 * abs(fd) + 1e-14 * abs(u0) / hj
+        rows.append(f"{PARAM_NAMES[j]:7s} adj {g[j]:+.9e} oracle fd {fd:+.9e}")
+        assert abs(g[j] - fd) <= tol, rows[-1]
+    print("\n".join(rows))
+
+
 @pytest.mark.gpu
 def test_param_grad_mixed_equals_fp64(small, thermal):
     """The derivatives are FP64 in both engine precisions; only the H-bond Monte
