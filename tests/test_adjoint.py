@@ -179,6 +179,41 @@ def test_traj_grad_matches_finite_differences(small, thermal, steps, every):
     assert abs(ad - fd) <= 1e-4 * abs(fd) + noise / h, rows[-2]
 
 
+def oracle_final_state(system, theta, state, steps):
+    from oracle_bridge import Oracle
+    o = Oracle(with_params(system, theta).to_dict(), seed=int(system["seed"][0]))
+    o.set_state(state)
+    o.populate_lists()
+    o.step(steps)
+    return o.get_state()
+
+
+@pytest.mark.gpu
+def test_traj_grad_matches_oracle_finite_differences(small, thermal):
+    """The reference gradient through 40 fixed-noise steps: central differences of
+    L = w . (x_T, v_T) over the CPU oracle's own trajectories (the reference's
+    algorithm and rand() stream), against tis_traj_grad on the FP64 engine."""
+    th0 = params_of(small)
+    seed = _loss_seed(thermal["x"].size, np.random.default_rng(11))
+    e = Engine([with_params(small, th0)], precision=PREC_FP64)
+    e.set_states(thermal)
+    dth = e.traj_grad(40, 10, seed)[0]
+    e.close()
+    L0 = _loss(oracle_final_state(small, th0, thermal, 40), seed)
+    rows = []
+    for j in range(N_PARAMS):
+        hj = (1e-4 if PARAM_NAMES[j].startswith("R_") else 1e-3) * abs(th0[j])
+        tp, tm = th0.copy(), th0.copy()
+        tp[j] += hj
+        tm[j] -= hj
+        fd = (_loss(oracle_final_state(small, tp, thermal, 40), seed) -
+              _loss(oracle_final_state(small, tm, thermal, 40), seed)) / (2 * hj)
+        tol = 1e-4 * abs(fd) + 1e-14 * abs(L0) / hj
+        rows.append(f"{PARAM_NAMES[j]:7s} adj {dth[j]:+.9e} oracle fd {fd:+.9e}")
+        assert abs(dth[j] - fd) <= tol, rows[-1]
+    print("\n".join(rows))
+
+
 @pytest.mark.gpu
 def test_traj_grad_batch_equals_single(synth_dir):
     """Three replicas (different seeds and ion counts) in two replica groups give
