@@ -99,6 +99,28 @@ def test_oracle_matches_live_reference_central(synth_dir, tmp_path):
         assert rel_err(t[k], T[k]) < 1e-12, k
 
 
+@needs_ref
+def test_oracle_matches_live_reference_large(tmp_path):
+    """The large system (1500-nt chain, 600 A box, 1300 Mg / 22100 Cl / 21000 K,
+    48,899 particles): the reference's own engine and the oracle give the same
+    cells, SR/LR pair sets and forces."""
+    from tis_gb300 import synth
+    w = synth.WORKLOADS["large"]
+    f = synth.generate(str(tmp_path), "large", w["n_nt"], seed=w["seed"], n_hb_pairs=w["n_hb_pairs"])
+    m, cl, k = w["ions"]
+    o_ = run_ref(f, str(tmp_path), "L", extra=("export-system", "lists", "terms"), box=w["box"], rc=30.0,
+                 T=0.59219, nMg=m, nCl=cl, nK=k, seed=1, center=500, rng="philox")
+    s, L, T = tisb.read(o_["export-system"]), tisb.read(o_["lists"]), tisb.read(o_["terms"])
+    o = Oracle(s, seed=1)
+    o.populate_lists()
+    assert np.array_equal(o.cells()[0], L["cell"])
+    assert np.array_equal(o.pairs(0), L["sr_pairs"])
+    assert np.array_equal(o.pairs(1), L["lr_pairs"])
+    t = o.terms()
+    for k in ["F_sr", "F_lr", "F_bonded", "F_stack", "F_hb"]:
+        assert rel_err(t[k], T[k]) < 1e-12, k
+
+
 SHIPPED = os.path.join(REF_SRC_DIR, "src")
 
 
