@@ -116,6 +116,10 @@ struct Group {
     bool lists_built = false;
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
+    cudaGraphExec_t tail = nullptr;  // the last remainder length (n % graph_steps) captured as its own graph
+    int tail_steps = 0;
+    cudaEvent_t *pev = nullptr;      // when set (tis_profile_in_step): events recorded around every kernel
+    int pev_next = 0;
     int base = 0;  // handle-wide index of the group's first replica
     long long launches = 0;
     double *d_scalar = nullptr;
@@ -133,6 +137,7 @@ struct Group {
     ~Group()
     {
         if (graph) cudaGraphExecDestroy(graph);
+        if (tail) cudaGraphExecDestroy(tail);
         for (void *p : owned) cudaFree(p);
         if (h_rs) cudaFreeHost(h_rs);
         if (h_peaks) cudaFreeHost(h_peaks);
@@ -173,6 +178,30 @@ int clear_flags(Group *h)
     return TIS_OK;
 }
 
+void enqueue_step(Group *h);
+
+// the captured step graphs hold the list pointers: dropped when the lists move
+void drop_graphs(Group *h)
+{
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    if (h->tail) cudaGraphExecDestroy(h->tail);
+    h->graph = h->tail = nullptr;
+    h->graph_steps = h->tail_steps = 0;
+}
+
+// `steps` fused steps of the group captured from its stream into *out
+int capture_steps(Group *h, int steps, cudaGraphExec_t *out)
+{
+    cudaGraph_t g;
+    TIS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < steps; ++s) enqueue_step(h);
+    TIS_CUDA(cudaStreamEndCapture(h->stream, &g));
+    const cudaError_t e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    return TIS_OK;
+}
+
 int grow_lists(Group *h, int cap_sr, int cap_lr)
 {
     // lists are the last allocations that depend on capacity; allocate anew
@@ -191,10 +220,7 @@ int grow_lists(Group *h, int cap_sr, int cap_lr)
     if ((rc = dalloc(h->owned, &h->dev.nbr_lr, (size_t)cap_lr * h->P))) return rc;
     h->dev.cap_sr = cap_sr;
     h->dev.cap_lr = cap_lr;
-    if (h->graph) {
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;
-    }
+    drop_graphs(h);
     return TIS_OK;
 }
 
@@ -271,14 +297,34 @@ int populate(Group *h)
 // deterministic_forces_MPI (E:2524-2586): the four force kernels are independent
 // (fixed-point atomics into one sum, the LR sum kept apart), so they run as
 // concurrent branches joined before the integrator
+// in-step profiling (tis_profile_in_step): an event recorded on s before stage k of
+// the step being captured (begin) or after it; no-op otherwise.  Event pair k of a
+// step sits at pev[2 * (step * TIS_N_STAGES + k)].
+void mark(Group *h, cudaStream_t s, int k, bool begin)
+{
+    if (!h->pev) return;
+    // External: captured as an event-record node of the graph (a plain record during
+    // capture only orders the streams)
+    cudaEventRecordWithFlags(h->pev[2 * (h->pev_next * TIS_N_STAGES + k) + (begin ? 0 : 1)], s,
+                             cudaEventRecordExternal);
+}
+
 void enqueue_forces(Group *h, bool make_noise)
 {
     cudaEventRecord(h->fork, h->stream);
     for (int k = 0; k < 3; ++k) cudaStreamWaitEvent(h->side[k], h->fork, 0);
+    mark(h, h->side[0], 1, true);
     tis::launch_pair_lr(h->dev, h->side[0], false, false);
+    mark(h, h->side[0], 1, false);
+    mark(h, h->side[1], 2, true);
     tis::launch_topology(h->dev, h->side[1], 4 | 8, false, false, true);
+    mark(h, h->side[1], 2, false);
+    mark(h, h->side[2], 3, true);
     tis::launch_topology(h->dev, h->side[2], 16, false, make_noise, true);
+    mark(h, h->side[2], 3, false);
+    mark(h, h->stream, 0, true);
     tis::launch_pair_sr(h->dev, h->stream, false, true);
+    mark(h, h->stream, 0, false);
     for (int k = 0; k < 3; ++k) {
         cudaEventRecord(h->join[k], h->side[k]);
         cudaStreamWaitEvent(h->stream, h->join[k], 0);
@@ -288,8 +334,21 @@ void enqueue_forces(Group *h, bool make_noise)
 void enqueue_step(Group *h)
 {
     enqueue_forces(h, true);                   // the H-bond kernel also draws full_forces' Gaussians
-    tis::launch_integrate(h->dev, h->stream);  // recentring shift; last block per replica: skin check
-    tis::launch_rebuild(h->dev, h->stream);
+    if (!h->pev) {
+        tis::launch_integrate(h->dev, h->stream);  // recentring shift; last block per replica: skin check
+        tis::launch_rebuild(h->dev, h->stream);
+        return;
+    }
+    // the same four launches with events between them (their programmatic
+    // dependent launch then waits for the event nodes like a plain dependency)
+    void (*chain[4])(const tis::Dev &, cudaStream_t) = {tis::launch_shift, tis::launch_move, tis::launch_cells,
+                                                         tis::launch_search};
+    for (int k = 0; k < 4; ++k) {
+        mark(h, h->stream, 4 + k, true);
+        chain[k](h->dev, h->stream);
+        mark(h, h->stream, 4 + k, false);
+    }
+    ++h->pev_next;
 }
 
 int valid_replica(Group *h, int r)
@@ -1284,19 +1343,27 @@ static int grp_step(Group *h, int64_t n)
     int64_t left = n;
     if (h->prm.use_graph && n >= h->prm.graph_steps) {
         if (!h->graph) {
-            cudaGraph_t g;
-            TIS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-            for (int s = 0; s < h->prm.graph_steps; ++s) enqueue_step(h);
-            TIS_CUDA(cudaStreamEndCapture(h->stream, &g));
-            cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+            if ((rc = capture_steps(h, h->prm.graph_steps, &h->graph))) return rc;
             h->graph_steps = h->prm.graph_steps;
         }
         while (left >= h->graph_steps) {
             TIS_CUDA(cudaGraphLaunch(h->graph, h->stream));
             left -= h->graph_steps;
         }
+    }
+    if (h->prm.use_graph && left > 0) {
+        // the remainder runs from a graph of its own length, kept for the next call
+        // with the same remainder (a caller stepping by a fixed count below the graph
+        // length replays it every call)
+        if (!h->tail || h->tail_steps != left) {
+            if (h->tail) cudaGraphExecDestroy(h->tail);
+            h->tail = nullptr;
+            h->tail_steps = 0;
+            if ((rc = capture_steps(h, (int)left, &h->tail))) return rc;
+            h->tail_steps = (int)left;
+        }
+        TIS_CUDA(cudaGraphLaunch(h->tail, h->stream));
+        left = 0;
     }
     for (int64_t s = 0; s < left; ++s) enqueue_step(h);
     TIS_CUDA(cudaGetLastError());
@@ -2006,19 +2073,10 @@ int tis_capture_graph(tis_handle *h, int32_t steps)
     return each_group(h, [steps](Group *g) -> int {
         int rc;
         if (!g->lists_built && (rc = populate(g))) return rc;
-        if (g->graph) {
-            TIS_CUDA(cudaGraphExecDestroy(g->graph));
-            g->graph = nullptr;
-        }
+        drop_graphs(g);
         g->prm.graph_steps = steps;
         g->prm.use_graph = 1;
-        cudaGraph_t gr;
-        TIS_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
-        for (int s = 0; s < steps; ++s) enqueue_step(g);
-        TIS_CUDA(cudaStreamEndCapture(g->stream, &gr));
-        const cudaError_t e = cudaGraphInstantiate(&g->graph, gr, 0);
-        cudaGraphDestroy(gr);
-        if (e != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        if ((rc = capture_steps(g, steps, &g->graph))) return rc;
         g->graph_steps = steps;
         return TIS_OK;
     });
@@ -2036,6 +2094,75 @@ int tis_profile_stages(tis_handle *h, int64_t n, double *ms)
         if (rc) return rc;
         for (int k = 0; k < TIS_N_STAGES; ++k) ms[k] += part[k];
     }
+    return TIS_OK;
+}
+
+// Every stage's kernel timed inside the concurrently replayed step graphs of all
+// groups: each group's `steps` steps captured once more with an event pair around
+// each of the eight kernels of every step, the groups' graphs forked from the
+// handle's stream and replayed together, the event pairs' durations averaged over
+// steps and groups.  Advances every replica by `steps` steps like tis_step.
+int tis_profile_in_step(tis_handle *h, int32_t steps, double *ms)
+{
+    if (!h || steps < 1 || steps > 1000 || !ms) return fail(TIS_ERR_ARG, "tis_profile_in_step: bad argument");
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    const size_t n_ev = 2 * (size_t)steps * TIS_N_STAGES;
+    const size_t G = h->groups.size();
+    std::vector<cudaEvent_t> ev(n_ev * G, nullptr);
+    std::vector<cudaGraphExec_t> exec(G, nullptr);
+    int rc = TIS_OK;
+    auto cleanup = [&]() {
+        for (auto e : exec)
+            if (e) cudaGraphExecDestroy(e);
+        for (auto e : ev)
+            if (e) cudaEventDestroy(e);
+        for (Group *g : h->groups) {
+            g->pev = nullptr;
+            g->pev_next = 0;
+        }
+    };
+    for (auto &e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            cleanup();
+            return fail(TIS_ERR_CUDA, "tis_profile_in_step: cudaEventCreate failed");
+        }
+    for (size_t gi = 0; gi < G && !rc; ++gi) {
+        Group *g = h->groups[gi];
+        if (!g->lists_built && (rc = populate(g))) break;
+        g->pev = &ev[gi * n_ev];
+        g->pev_next = 0;
+        rc = capture_steps(g, steps, &exec[gi]);
+        g->pev = nullptr;
+    }
+    if (!rc) rc = fork_groups(h);
+    for (size_t gi = 0; gi < G && !rc; ++gi)
+        if (cudaGraphLaunch(exec[gi], h->groups[gi]->stream) != cudaSuccess)
+            rc = fail(TIS_ERR_CUDA, "tis_profile_in_step: cudaGraphLaunch failed");
+    if (!rc) rc = join_groups(h);
+    if (!rc && cudaStreamSynchronize(h->stream) != cudaSuccess)
+        rc = fail(TIS_ERR_CUDA, "tis_profile_in_step: %s", cudaGetErrorString(cudaGetLastError()));
+    if (!rc) {
+        for (int k = 0; k < TIS_N_STAGES && !rc; ++k) {
+            double acc = 0;
+            for (size_t gi = 0; gi < G && !rc; ++gi)
+                for (int st = 0; st < steps; ++st) {
+                    float t = 0;
+                    const size_t b = gi * n_ev + 2 * ((size_t)st * TIS_N_STAGES + k);
+                    const cudaError_t e = cudaEventElapsedTime(&t, ev[b], ev[b + 1]);
+                    if (e != cudaSuccess) {
+                        rc = fail(TIS_ERR_CUDA, "tis_profile_in_step: cudaEventElapsedTime: %s", cudaGetErrorString(e));
+                        break;
+                    }
+                    acc += t;
+                }
+            ms[k] = acc / ((double)steps * G);
+        }
+        for (Group *g : h->groups) g->launches += (long long)steps * tis::kernel_launches_per_step();
+    }
+    cleanup();
+    if (rc) return rc;
+    for (Group *g : h->groups)
+        if ((rc = check_flags(g))) return rc;
     return TIS_OK;
 }
 

@@ -104,6 +104,7 @@ def _declare(L):
         "tis_get_launch_count": [vp, C.POINTER(C.c_int64)],
         "tis_rand_stream": [C.c_uint64, C.c_uint64, i64, ip],
         "tis_profile_stages": [vp, i64, dp],
+        "tis_profile_in_step": [vp, i32, dp],
         "tis_get_forces": [vp, i32, dp],
         "tis_pair_lists_noalloc": [vp, vp, vp, vp, C.c_int32, dp, C.c_double, C.c_double, vp, i64, vp, i64, vp, vp],
         "tis_param_grad": [vp, dp],
@@ -137,7 +138,7 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
             "tis_param_grad", "tis_traj_grad", "tis_autotune", "tis_density_create", "tis_density_add",
             "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd", "tis_capture_graph",
-            "tis_write_cgpdb", "tis_checkpoint_save", "tis_checkpoint_load"]
+            "tis_write_cgpdb", "tis_checkpoint_save", "tis_checkpoint_load", "tis_profile_in_step"]
 
 
 def read_last_frame(path, n):
@@ -533,6 +534,14 @@ class Engine:
         Gaussians, shift, integrator, cell binning, pair search."""
         ms = np.zeros(len(self.STAGES))
         _check(lib().tis_profile_stages(self.h, n, _dp(ms)))
+        return dict(zip(self.STAGES, ms))
+
+    def profile_in_step(self, steps):
+        """Mean ms per launch (one replica group, one step) of each stage's kernel timed
+        inside the graph-replayed step with all groups running concurrently; advances
+        every replica by `steps` steps."""
+        ms = np.zeros(len(self.STAGES))
+        _check(lib().tis_profile_in_step(self.h, steps, _dp(ms)))
         return dict(zip(self.STAGES, ms))
 
     def launches(self):

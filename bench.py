@@ -14,9 +14,17 @@ over all GPUs.  Inputs (the systems) are synthetic and generated here.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
---impl reference times the reference's own CPU engine (oracle/_ref/tis_ref, built
-from the reference sources; else the C oracle port) on the host cores, one
-replica per core, on a bounded sample of the same workload.
+--impl reference times the reference's own CPU engine (oracle/_ref/tis_ref_bench,
+built -O3 from the reference sources; else the C oracle port) on the host cores,
+one replica per core, on a bounded sample of the same workload.
+
+Besides the headline line's fields, the GPU arm reports the plain single-replica
+FP64 GPU path on the central system (the batching denominator), kernel times
+inside the replayed step, an end-to-end number through the C ABI over the same
+steps, the reference engine on the host cores, and the other configurations of
+the benchmark description: the 76-nt system in FP64 (GPU and one host core), the
+central single replica, the parameter gradient over 10^4 frames and through
+200-step trajectories, and the large system.
 """
 import argparse
 import json
@@ -194,10 +202,17 @@ NCU_DRAM_BYTES_PER_REPLICA = {"pair_sr": 3.04e6 / 8, "pair_lr": None, "bonded": 
                               "shift": 0.04e6 / 8, "integrate": 5.35e6 / 8, "cells": 0.03e6 / 8, "search": None}
 
 
+# FP32 (FMA) pipe and issue-slot use of each kernel from its committed ncu capture
+# (`--set full`, one launch over a group of 8 replicas): sm__pipe_fma_cycles_active
+# and sm__inst_issued (issue active) as fractions of their peaks.
+NCU_FMA_PIPE = {"pair_sr": 0.036}
+NCU_ISSUE_ACTIVE = {"pair_sr": 0.142}
+
+
 def cpu_sample(files, specs, steps, workers):
     """Reference CPU engine on `workers` replicas in parallel, `steps` steps each."""
     import build_ref
-    exe = build_ref.build()
+    exe = build_ref.build(bench=True)
     kind = "reference" if exe else "port"
     sample = specs[:: max(1, len(specs) // workers)][:workers]
 
@@ -205,7 +220,7 @@ def cpu_sample(files, specs, steps, workers):
         args = [exe, "--pdb", files["pdb"], "--bonds", files["bonds"], "--stacks", files["stacks"],
                 "--maxikey", files["maxikey"], "--box", str(BOX), "--rc", str(RC), "--T", str(T_298),
                 "--nMg", str(sp["n_mg"]), "--nCl", str(sp["n_cl"]), "--nK", str(sp["n_k"]),
-                "--seed", str(sp["seed"]), "--center", "500", "--rng", "philox", "--steps", str(steps), "--time"]
+                "--seed", str(sp["seed"]), "--center", "500", "--steps", str(steps), "--time"]
         out = subprocess.run(args, check=True, capture_output=True, text=True).stdout
         return json.loads(out.strip().splitlines()[-1])["seconds"]
 
@@ -224,9 +239,29 @@ def cpu_sample(files, specs, steps, workers):
     with ThreadPoolExecutor(max_workers=workers) as ex:
         secs = list(ex.map(fn, sample))
     value = len(sample) * steps / max(secs)
-    return {"value": value, "unit": UNIT, "cores": len(sample), "kind": kind,
+    build = ("the reference engine (src/16SCD_Mg_Cl_K_COPY_fast.cpp with the four-item hook patch table), g++ "
+             + " ".join(build_ref.BENCH_FLAGS) + ", single-rank MPI stub, glibc rand()") if exe else \
+        "the C oracle port (oracle/tis_oracle.c), one thread per replica"
+    return {"value": value, "unit": UNIT, "cores": len(sample), "kind": kind, "build": build,
             "sample": f"{len(sample)} of the {len(specs)} replicas ({steps} steps each, one per host core, "
                       f"concurrently; setup excluded)"}
+
+
+N_BEADS = 3 * N_NT - 1  # the chain starts with a nucleotide: 1037 beads for 346 nt
+
+
+def workload_config(specs):
+    """The workload both arms run, with the sizes and conditions it is quoted on
+    (identical dictionaries, so the two arms' lines name the same configuration)."""
+    parts = [N_BEADS + sp["n_mg"] + sp["n_cl"] + sp["n_k"] for sp in specs]
+    return {"workload": "64 replicas x 346-nt TIS chain (1037 beads) + Mg 0-20 mM sweep, 76 mM KCl, "
+                        "350 A box, T 298 K, rc 30 A",
+            "replicas_per_gpu": len(specs), "particles_per_gpu": int(sum(parts)),
+            "particles_per_replica": [int(min(parts)), int(max(parts))],
+            "box_A": BOX, "T_K": 298.0, "T_kcal_per_mol": T_298, "h": 0.05, "coulomb_cutoff_A": RC,
+            "sr_list_A": 15.0, "lr_list_A": RC + 3.0, "lr_every_steps": 10, "mg_mM": [0.0, 20.0], "kcl_mM": 76.0,
+            "seeds": [specs[0]["seed"], specs[-1]["seed"]],
+            "l2": "GPU arm: flushed (256 MB write) before every timed graph replay"}
 
 
 def reference_arm(args):
@@ -238,22 +273,147 @@ def reference_arm(args):
         specs = replica_specs()
         workers = min(len(specs), os.cpu_count() or 1)
         cpu = cpu_sample(files, specs, max(200, args.steps), workers)
-    cpu_line = dict(cpu)
     line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * N_REPLICAS / cpu["value"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "64 replicas x 346-nt TIS chain + Mg 0-20 mM sweep, 76 mM KCl, 350 A box",
-                       "replicas": N_REPLICAS},
-            "cpu_baseline": cpu_line,
+            "config": workload_config(specs),
+            "cpu_baseline": dict(cpu),
             "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def timed_steps(eng, K, W, flush, stream, world, clk_device):
+    """W warm-up steps, every graph the timed region replays captured, then exactly K
+    steps timed with CUDA events on the handle's stream: the step graph (graph_steps
+    long) replayed K // graph_steps times and a graph of the remaining steps once,
+    L2 flushed before each replay.  Returns (ms, launches, chunks, clock summary)."""
+    import torch
+    gs = eng.params.graph_steps
+    chunks = [gs] * (K // gs) + ([K % gs] if K % gs else [])
+    eng.step(W)
+    for c in sorted(set(chunks), reverse=True):  # captures (the last one stays as the tail graph)
+        eng.step(c)
+    eng.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in chunks]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = eng.launches()
+    with ClockSampler(clk_device) as clk:
+        for i, c in enumerate(chunks):
+            with torch.cuda.stream(stream):
+                flush.zero_()  # L2 flush between timed replays (256 MB > 129 MB L2)
+                ev[i][0].record(stream)
+            eng.step(c)
+            with torch.cuda.stream(stream):
+                ev[i][1].record(stream)
+        eng.sync()
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    return ms, eng.launches() - launches0, chunks, clk.summary()
+
+
+def e2e_measure(eng, K, n_rep, reps=3):
+    """End to end through the C ABI with host buffers, over the same K steps as the
+    timed region, `reps` times: every replica's state uploaded from pinned host
+    memory (tis_set_states), the lists rebuilt, K graph-replayed steps, a frame
+    (positions and the five energies of every replica) read back into pinned host
+    memory; host wall clock between device synchronisations."""
+    import torch
+    state = eng.get_states()
+    pinned = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in state.items()}
+    frame = {k: torch.zeros(v.size, dtype=torch.float64).pin_memory().numpy() for k, v in state.items()
+             if k in ("x", "y", "z")}
+    energies = torch.zeros((n_rep, 5), dtype=torch.float64).pin_memory().numpy()
+    h2d = sum(v.nbytes for v in pinned.values())
+    d2h = sum(v.nbytes for v in frame.values()) + energies.nbytes
+
+    def one():
+        eng.set_states(pinned)
+        eng.populate_lists()
+        eng.step(K)
+        eng.get_states(("x", "y", "z"), out=frame)
+        eng.all_energies(out=energies)
+
+    one()  # the same calls once untimed (graphs of these lengths captured)
+    eng.sync()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        one()
+    eng.sync()
+    dt = time.perf_counter() - t0
+    return {"value": n_rep * K * reps / dt, "unit": UNIT, "h2d_bytes_per_step": h2d // K,
+            "d2h_bytes_per_step": d2h // K, "steps_per_call": K, "repeats": reps,
+            "calls": "tis_set_states (pinned) + tis_populate_lists + tis_step(K) + tis_get_states (x, y, z) + "
+                     "tis_get_all_energies"}
+
+
+def plain_steps_per_s(system, local, n_steps=500, precision=None):
+    """One replica on its own handle, direct launches (no graph): the plain
+    single-replica GPU path, timed with CUDA events on its stream."""
+    import torch
+
+    from tis_gb300 import PREC_FP64, Engine
+    e = Engine([system], precision=PREC_FP64 if precision is None else precision, device=local, use_graph=0)
+    e.populate_lists()
+    e.step(50)
+    e.sync()
+    st = torch.cuda.ExternalStream(e.stream())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(st):
+        a.record(st)
+    e.step(n_steps)
+    with torch.cuda.stream(st):
+        b.record(st)
+    e.sync()
+    torch.cuda.synchronize()
+    sps = n_steps / (a.elapsed_time(b) / 1000.0)
+    e.close()
+    return sps
+
+
+def graph_steps_per_s(systems, local, n_steps, precision):
+    """All `systems` on one handle, graph-replayed steps, CUDA events on its stream."""
+    import torch
+
+    from tis_gb300 import Engine
+    e = Engine(systems, precision=precision, device=local, use_graph=1, graph_steps=n_steps)
+    e.populate_lists()
+    e.step(n_steps)
+    e.sync()
+    st = torch.cuda.ExternalStream(e.stream())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(st):
+        a.record(st)
+    e.step(2 * n_steps)
+    with torch.cuda.stream(st):
+        b.record(st)
+    e.sync()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    e.close()
+    return len(systems) * 2 * n_steps / (ms / 1000.0), ms / (2 * n_steps)
+
+
+def ref_one_core(files, kw, steps):
+    """The reference engine (timing build) on one host core: steps/s, set-up excluded."""
+    import build_ref
+    exe = build_ref.build(bench=True)
+    if not exe:
+        return None
+    args = [exe, "--pdb", files["pdb"], "--bonds", files["bonds"], "--stacks", files["stacks"],
+            "--maxikey", files["maxikey"], "--steps", str(steps), "--time"]
+    for k, v in kw.items():
+        args += ["--" + k, str(v)]
+    out = subprocess.run(args, check=True, capture_output=True, text=True).stdout
+    return json.loads(out.strip().splitlines()[-1])["steps_per_s"]
 
 
 def gpu_arm(args):
     import numpy as np
     import torch
 
-    from tis_gb300 import PREC_FP64, PREC_MIXED, Engine, autotune
+    from tis_gb300 import PREC_FP64, PREC_MIXED, Engine, System, autotune, synth
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -283,79 +443,54 @@ def gpu_arm(args):
                 tune_note = f"library defaults (tis_autotune failed: {exc})"
             tune_s = time.perf_counter() - t0
         eng = Engine(systems, precision=PREC_MIXED, device=local, use_graph=1, **tune)
-        graph_steps = eng.params.graph_steps
+        n_part = sum(eng.n)
+        config = workload_config(specs)
+        assert config["particles_per_gpu"] == n_part, (config["particles_per_gpu"], n_part)
         eng.populate_lists()
         stream = torch.cuda.ExternalStream(eng.stream())
         flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
         K = max(1, args.steps)
         W = max(3, args.warmup)
-        eng.step(W)                # W warm-up steps (direct launches) ...
-        eng.step(graph_steps)      # ... and one graph replay, so capture happens before timing
-        eng.sync()
-        chunks = [graph_steps] * (K // graph_steps) + ([K % graph_steps] if K % graph_steps else [])
-        iters = len(chunks)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(iters)]
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        launches0 = eng.launches()
-        with ClockSampler(local) as clk:
-            for i in range(iters):
-                with torch.cuda.stream(stream):
-                    flush.zero_()  # L2 flush between timed iterations (256 MB > 129 MB L2)
-                    ev[i][0].record(stream)
-                eng.step(chunks[i])
-                with torch.cuda.stream(stream):
-                    ev[i][1].record(stream)
-            eng.sync()
-            torch.cuda.synchronize()
-        ms = sum(a.elapsed_time(b) for a, b in ev)
-        launches = eng.launches() - launches0
+        ms, launches, chunks, clocks = timed_steps(eng, K, W, flush, stream, world, local)
         ms = max_over_ranks(ms, world, device=f"cuda:{local}")
         if world > 1:
             torch.distributed.barrier()
         ms_per_step = ms / K
         value = job_value(ms, world, N_REPLICAS, K)
+        graph_steps = eng.params.graph_steps
+        groups = eng.params.groups or (3 * N_REPLICAS + 15) // 16
+        launch = {"path": "CUDA graph replay", "graph_steps": graph_steps,
+                  "graph_replays_per_group": len(chunks), "chunks": chunks, "replica_groups": groups,
+                  "lanes_sr": eng.params.lanes_sr or 1, "lanes_lr": eng.params.lanes_lr or 4,
+                  "config_source": tune_note, "autotune_s": tune_s}
 
         if not args.extras:
             if rank == 0:
                 print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "steps": K,
-                                  "ms_per_step": ms_per_step, "note": "timed loop only (--no-extras)"}), flush=True)
+                                  "ms_per_step": ms_per_step, "launch": launch,
+                                  "note": "timed loop only (--no-extras)"}), flush=True)
             return
 
-        # end to end through the C ABI with host buffers: every 100 steps every
-        # replica's state is uploaded from pinned host memory (one call), the lists
-        # are rebuilt, 100 steps run, and a frame (positions + the five energies of
-        # every replica) is read back into pinned host memory
-        e2e = None
-        if rank == 0:
-            E2E_STEPS = max(100, graph_steps)  # whole graphs between frames
-            n_it = max(1, min(10, K // E2E_STEPS))
-            state = eng.get_states()
-            pinned = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in state.items()}
-            frame = {k: torch.zeros(v.size, dtype=torch.float64).pin_memory().numpy() for k, v in state.items()
-                     if k in ("x", "y", "z")}
-            energies = torch.zeros((N_REPLICAS, 5), dtype=torch.float64).pin_memory().numpy()
-            h2d = sum(v.nbytes for v in pinned.values())
-            d2h = sum(v.nbytes for v in frame.values()) + energies.nbytes
-            t0 = time.perf_counter()
-            for _ in range(n_it):
-                eng.set_states(pinned)
-                eng.populate_lists()
-                eng.step(E2E_STEPS)
-                eng.get_states(("x", "y", "z"), out=frame)
-                eng.all_energies(out=energies)
-            eng.sync()
-            dt = time.perf_counter() - t0
-            e2e = {"value": N_REPLICAS * E2E_STEPS * n_it / dt, "unit": UNIT,
-                   "h2d_bytes_per_step": h2d // E2E_STEPS, "d2h_bytes_per_step": d2h // E2E_STEPS,
-                   "frame_every_steps": E2E_STEPS}
+        e2e = e2e_measure(eng, K, N_REPLICAS) if rank == 0 else None
 
-        # per-stage device time: each stage's kernels alone, CUDA events between them on
-        # the group streams, ms per step summed over the replica groups
+        # the plain single-replica FP64 GPU path on the central system (346-nt chain,
+        # 129 Mg / 2219 Cl / 2307 K, 350 A box): the denominator of the batching target
+        w1 = synth.WORKLOADS["central"]
+        cfg1_sys = System.load(files["pdb"], files["bonds"], files["stacks"], files["maxikey"], T=T_298, box=BOX,
+                               rc=RC, n_mg=w1["ions"][0], n_cl=w1["ions"][1], n_k=w1["ions"][2], seed=1,
+                               center=500, rng=1)
+        plain_sps = plain_steps_per_s(cfg1_sys, local)
+
+        # in-step kernel times: every kernel timed inside the graph-replayed step with
+        # all groups running concurrently (tis_profile_in_step), and each stage alone
         stages = eng.profile_stages(50)
+        try:
+            in_step = eng.profile_in_step(min(K, 100))
+            in_step_src = "tis_profile_in_step"
+        except Exception as exc:  # the stages run alone, per group, if the in-step capture fails
+            in_step = {k: v / groups for k, v in stages.items()}
+            in_step_src = f"tis_profile_stages (in-step capture failed: {exc})"
         peak, peak_kind = measured_peaks()
-        n_part = sum(eng.n)
         cnt = [eng.counters(r) for r in range(N_REPLICAS)]
         reb_rep = sum(c[1] / max(1, c[0]) for c in cnt)  # replicas rebuilt per step
         nreb = reb_rep * n_part / N_REPLICAS
@@ -368,126 +503,169 @@ def gpu_arm(args):
         nhb = len(sd["hb_E"]) * N_REPLICAS
         alg = stage_bytes(n_part, sr, lr, 0.1 + reb_rep / N_REPLICAS, nreb, nrna, items, nhb, N_REPLICAS)
         per_stage = {}
-        for k, ms_k in stages.items():
-            gbs = alg[k] / (ms_k * 1e-3) / 1e9 if ms_k > 0 else None
-            per_stage[k] = {"ms": ms_k, "alg_bytes": alg[k], "achieved_gbs": gbs,
-                            "frac": gbs / peak if gbs is not None else None}
-        dom = max(stages, key=stages.get)
+        for k in in_step:
+            b = alg[k] / groups  # one launch = one replica group's kernel in one step
+            per_stage[k] = {"in_step_us": 1000 * in_step[k], "alone_us_per_group": 1000 * stages[k] / groups,
+                            "alg_bytes_per_launch": b,
+                            "achieved_gbs": b / (in_step[k] * 1e-3) / 1e9 if in_step[k] > 0 else None}
+        dom = max(in_step, key=in_step.get)
+        ach = per_stage[dom]["achieved_gbs"]
         traffic = NCU_DRAM_BYTES_PER_REPLICA.get(dom)
-        roofline = {"bound": "hbm", "kernel": dom, "achieved": per_stage[dom]["achieved_gbs"], "peak": peak,
-                    "unit": "GB/s", "frac": per_stage[dom]["frac"],
-                    "traffic": traffic * N_REPLICAS if traffic is not None else None,
-                    "alg_bytes_per_launch": alg[dom], "peak_source": peak_kind,
-                    "mean_neighbours": {"sr": sr, "lr": lr}, "stages": per_stage,
+        roofline = {"bound": "latency", "axis": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                    "frac": ach / peak, "peak_source": peak_kind,
+                    "traffic": traffic * N_REPLICAS / groups if traffic is not None else None,
+                    "alg_bytes_per_launch": per_stage[dom]["alg_bytes_per_launch"],
+                    "launch_us_in_step": per_stage[dom]["in_step_us"],
+                    "fp32_pipe_frac": NCU_FMA_PIPE.get(dom), "issue_active_frac": NCU_ISSUE_ACTIVE.get(dom),
+                    "mean_neighbours": {"sr": sr, "lr": lr}, "stages": per_stage, "in_step_source": in_step_src,
                     "step": {"alg_bytes": sum(alg.values()),
                              "achieved_gbs": sum(alg.values()) / (ms_per_step * 1e-3) / 1e9,
-                             "frac": sum(alg.values()) / (ms_per_step * 1e-3) / 1e9 / peak,
-                             "note": "every stage's algorithmic bytes of one step of the batch over the "
-                                     "graph-replayed step time"},
-                    "note": "stage = its kernels over all replica groups run alone; launch = one step of "
-                            "the batch; the integrator is FP64-pipe bound, the H-bond kernel latency bound "
-                            "(serial Monte Carlo per replica)"}
+                             "frac": sum(alg.values()) / (ms_per_step * 1e-3) / 1e9 / peak},
+                    "note": "kernel with the longest in-step launch (tis_profile_in_step: event pairs around each "
+                            "kernel inside the concurrently replayed graphs of all groups); one launch = one "
+                            "replica group (1/" + str(groups) + " of the batch) for one step; achieved = its "
+                            "algorithmic bytes / its in-step duration; bound: the kernels are latency bound "
+                            "(ncu: long-scoreboard stalls on dependent gathers, low DRAM and FP32-pipe use), "
+                            "the axis is the measured HBM copy rate; fp32_pipe_frac and issue_active_frac "
+                            "come from the committed ncu capture of that kernel; step: all stages' "
+                            "algorithmic bytes per step over the timed step"}
 
-        # the plain single-replica FP64 GPU path (the denominator of the batching target)
-        plain = Engine([systems[len(systems) // 2]], precision=PREC_FP64, device=local, use_graph=0)
-        plain.populate_lists()
-        plain.step(50)
-        plain.sync()
-        t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        pstream = torch.cuda.ExternalStream(plain.stream())
-        NP = 500
-        with torch.cuda.stream(pstream):
-            t0e.record(pstream)
-        plain.step(NP)
-        with torch.cuda.stream(pstream):
-            t1e.record(pstream)
-        plain.sync()
-        torch.cuda.synchronize()
-        plain_sps = NP / (t0e.elapsed_time(t1e) / 1000.0)
-        plain.close()
-
-        # the differentiation workload: 16 replicas of the chain, dU/dtheta of 15
-        # parameters at their current frames, and the gradient through a 200-step
-        # fixed-noise trajectory with a checkpoint every 10 steps (forward, recomputation
-        # and reverse pass in one call); host wall clock around synchronous calls
-        adjoint = None
+        extras = {}
         if rank == 0:
-            adj = Engine(systems[:16], precision=PREC_MIXED, device=local, groups=1)  # the adjoint runs group by group
-            adj.populate_lists()
-            adj.step(50)
-            adj.sync()
-            adj.param_grad()
-            t0 = time.perf_counter()
-            for _ in range(5):
-                adj.param_grad()
-            t_pg = (time.perf_counter() - t0) / 5
-            rng = np.random.default_rng(0)
-            seed = {k: rng.standard_normal(sum(adj.n)) for k in ("x", "y", "z")}
-            adj.traj_grad(20, 10, seed)
-            t0 = time.perf_counter()
-            adj.traj_grad(200, 10, seed)
-            t_tg = time.perf_counter() - t0
-            adjoint = {"replicas": 16, "param_grad_frames_per_s": 16 / t_pg,
-                       "traj_steps": 200, "checkpoint_every": 10, "traj_grad_s": t_tg,
-                       "traj_grad_replica_steps_per_s": 16 * 200 / t_tg,
-                       "precision": "mixed forward; adjoint in FP32 dual numbers with FP64 sums"}
-            adj.close()
-
-        # the large system: a 1500-nt chain in a 600 A box with 1300 Mg, 22100 Cl,
-        # 21000 K (48,899 particles per replica), 16 replicas with independent seeds
-        # (one set-up, the seed varied), mixed precision, graphs of GRAPH_STEPS steps
-        large = None
-        if rank == 0 and args.large:
-            from tis_gb300 import System, synth
-            w = synth.WORKLOADS["large"]
-            lf = synth.generate(tmp, "large", w["n_nt"], seed=w["seed"], n_hb_pairs=w["n_hb_pairs"])
-            m, cl, kk = w["ions"]
-            base = System.load(lf["pdb"], lf["bonds"], lf["stacks"], lf["maxikey"], T=T_298, box=w["box"], rc=RC,
-                               n_mg=m, n_cl=cl, n_k=kk, seed=1, center=500, rng=1).to_dict()
-            reps = [System.from_arrays(dict(base, seed=np.array([s], dtype=np.int64))) for s in range(1, 17)]
-            le = Engine(reps, precision=PREC_MIXED, device=local, use_graph=1, graph_steps=GRAPH_STEPS)
-            le.populate_lists()
-            le.step(GRAPH_STEPS)
-            le.sync()
-            ls = torch.cuda.ExternalStream(le.stream())
-            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            LN = 3 * GRAPH_STEPS
-            with torch.cuda.stream(ls):
-                a0.record(ls)
-            le.step(LN)
-            with torch.cuda.stream(ls):
-                a1.record(ls)
-            le.sync()
-            torch.cuda.synchronize()
-            lms = a0.elapsed_time(a1)
-            large = {"workload": "16 replicas x 1500-nt chain (4499 beads), 600 A box, 1300 Mg / 22100 Cl / 21000 K",
-                     "particles_per_replica": le.n[0], "steps": LN, "ms_per_step": lms / LN,
-                     "replica_steps_per_s": 16 * LN / (lms / 1000.0), "precision": "mixed"}
-            le.close()
+            extras = more_configs(args, files, tmp, systems, local, cfg1_sys)
 
     if rank != 0:
         return
     cpu = cpu_sample(files_for_cpu(), replica_specs(), 2000, min(N_REPLICAS, os.cpu_count() or 1)) \
         if args.cpu_baseline else None
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
+    line = {"metric": METRIC, "value": value, "unit": UNIT,
+            "plain_fp64_single_replica_steps_per_s": plain_sps, "batched_vs_plain": value / world / plain_sps,
+            "n_gpus": world, "steps": K, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+i64+f64", "data": "synthetic",
-            "config": {"workload": "64 replicas x 346-nt TIS chain (1037 beads) + Mg 0-20 mM sweep, 76 mM KCl, "
-                                   "350 A box, T 298 K, rc 30 A",
-                       "replicas_per_gpu": N_REPLICAS, "particles_per_gpu": n_part, "precision": "mixed",
-                       "graph_steps": graph_steps, "replica_groups": eng.params.groups or (3 * N_REPLICAS + 15) // 16,
-                       "lanes_sr": eng.params.lanes_sr or 1, "lanes_lr": eng.params.lanes_lr or 4,
-                       "launch_config": tune_note,
-                       "autotune_s": tune_s,
-                       "l2": "flushed (256 MB write) between timed iterations of "
-                                                         f"{graph_steps} steps", "parallelism": f"replicas x{world}"},
-            "plain_fp64_single_replica_steps_per_s": plain_sps,
-            "batched_vs_plain": value / world / plain_sps,
-            "stage_ms_per_step": stages,
-            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "adjoint": adjoint,
-            "large_system": large,
-            "clocks": clk.summary()}
+            "dtype": "f32+i64+f64", "data": "synthetic", "config": config, "launch": launch,
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "precision": "mixed: FP32 pair/bonded math on exact fixed-point differences, int64 fixed-point force "
+                         "sums, FP64 integration and energies"}
+    line.update(extras)
     print(json.dumps(line), flush=True)
+
+
+def n_particles(system):
+    import numpy as np
+    return int(np.asarray(system.to_dict()["n_particles"]).ravel()[0])
+
+
+def more_configs(args, files, tmp, systems, local, cfg1_sys):
+    """The benchmark description's other configurations, each on the GPU beside the
+    reference engine where it names one; a configuration that fails is reported
+    with its error instead of its numbers."""
+    out = {}
+    for name, fn in (("small_system_fp64", _cfg_small), ("central_single_replica", _cfg_central),
+                     ("adjoint", _cfg_adjoint), ("large_system", _cfg_large)):
+        if name == "large_system" and not args.large:
+            continue
+        try:
+            out[name] = fn(args, files, tmp, local, cfg1_sys)
+        except Exception as exc:
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+    return out
+
+
+def _cfg_small(args, files, tmp, local, cfg1_sys):
+    from tis_gb300 import System, synth
+    # cfg 0: the 76-nt chain (227 beads) in a 200 A box with 10 Mg / 261 Cl / 317 K
+    # (815 particles), FP64: the plain GPU path and the reference engine on one core
+    w0 = synth.WORKLOADS["small"]
+    f0 = synth.generate(tmp, "small", w0["n_nt"], seed=w0["seed"], n_hb_pairs=w0["n_hb_pairs"])
+    s0 = System.load(f0["pdb"], f0["bonds"], f0["stacks"], f0["maxikey"], T=T_298, box=w0["box"], rc=RC,
+                     n_mg=w0["ions"][0], n_cl=w0["ions"][1], n_k=w0["ions"][2], seed=1, center=100, rng=1)
+    ref0 = ref_one_core(f0, dict(box=w0["box"], rc=RC, T=T_298, nMg=w0["ions"][0], nCl=w0["ions"][1],
+                                 nK=w0["ions"][2], seed=1, center=100), 5000) if args.cpu_baseline else None
+    return {"workload": "1 replica x 76-nt chain (227 beads) + 10 Mg / 261 Cl / 317 K, 200 A box, FP64",
+            "particles": n_particles(s0), "plain_gpu_fp64_steps_per_s": plain_steps_per_s(s0, local, 1000),
+            "reference_one_core_steps_per_s": ref0}
+
+
+def _cfg_central(args, files, tmp, local, cfg1_sys):
+    from tis_gb300 import PREC_MIXED
+    # cfg 1: the central single replica (1037 beads + 129 Mg / 2219 Cl / 2307 K):
+    # mixed precision from a graph, the plain FP64 path, the reference on one core
+    mixed1, _ = graph_steps_per_s([cfg1_sys], local, 200, PREC_MIXED)
+    ref1 = ref_one_core(files, dict(box=BOX, rc=RC, T=T_298, nMg=129, nCl=2219, nK=2307, seed=1, center=500),
+                        1000) if args.cpu_baseline else None
+    return {"workload": "1 replica x 346-nt chain (1037 beads) + 129 Mg / 2219 Cl / 2307 K, 350 A box",
+            "particles": n_particles(cfg1_sys), "mixed_graph_steps_per_s": mixed1,
+            "plain_gpu_fp64_steps_per_s": plain_steps_per_s(cfg1_sys, local, 500),
+            "reference_one_core_steps_per_s": ref1}
+
+
+def _cfg_adjoint(args, files, tmp, local, cfg1_sys):
+    import numpy as np
+
+    from tis_gb300 import PREC_MIXED, Engine, System
+    # cfg 3: dU/dtheta of the 15 force-field parameters over 10^4 saved frames of the
+    # central system (64 replicas with independent seeds, a frame every 10 steps),
+    # uploaded 64 frames at a time from host memory; and the gradient through 200-step
+    # fixed-noise trajectories with a checkpoint every 10 steps, 16 replicas
+    base = cfg1_sys.to_dict()
+    reps = [System.from_arrays(dict(base, seed=np.array([s], dtype=np.int64))) for s in range(1, 65)]
+    fe = Engine(reps, precision=PREC_MIXED, device=local, use_graph=1, graph_steps=10)
+    fe.populate_lists()
+    n_frames = 10000
+    template = fe.get_states()  # x_old and v of the uploads (dU/dtheta reads positions only)
+    batches = []
+    for _ in range((n_frames + 63) // 64):
+        fe.step(10)
+        batches.append(fe.get_states(("x", "y", "z")))
+    fe.close()
+    ge = Engine(reps, precision=PREC_MIXED, device=local, groups=1)
+    ge.set_states(dict(template, **batches[0]))
+    ge.populate_lists()
+    ge.param_grad()
+    ge.sync()
+    t0 = time.perf_counter()
+    for b in batches:
+        ge.set_states(dict(template, **b))
+        ge.populate_lists()
+        ge.param_grad()
+    ge.sync()
+    t_pg = time.perf_counter() - t0
+    ge.close()
+    adj = Engine(reps[:16], precision=PREC_MIXED, device=local, groups=1)
+    adj.populate_lists()
+    adj.step(50)
+    adj.sync()
+    rng = np.random.default_rng(0)
+    seed = {k: rng.standard_normal(sum(adj.n)) for k in ("x", "y", "z")}
+    adj.traj_grad(20, 10, seed)
+    t0 = time.perf_counter()
+    adj.traj_grad(200, 10, seed)
+    t_tg = time.perf_counter() - t0
+    adj.close()
+    return {
+        "workload": "central system (346-nt chain + 129 Mg / 2219 Cl / 2307 K), 15 parameters",
+        "param_grad_frames": 64 * len(batches), "param_grad_frames_per_s": 64 * len(batches) / t_pg,
+        "param_grad_note": "frames uploaded from host memory 64 at a time, lists rebuilt, dU/dtheta; wall clock",
+        "traj_replicas": 16, "traj_steps": 200, "checkpoint_every": 10, "traj_grad_s": t_tg,
+        "traj_grad_replica_steps_per_s": 16 * 200 / t_tg,
+        "precision": "mixed forward; adjoint in FP32 dual numbers with FP64 sums"}
+
+
+def _cfg_large(args, files, tmp, local, cfg1_sys):
+    # the large system, 16 replicas x 48,899 particles, graphs of GRAPH_STEPS steps
+    import numpy as np
+
+    from tis_gb300 import PREC_MIXED, System, synth
+    w = synth.WORKLOADS["large"]
+    lf = synth.generate(tmp, "large", w["n_nt"], seed=w["seed"], n_hb_pairs=w["n_hb_pairs"])
+    m, cl, kk = w["ions"]
+    lb = System.load(lf["pdb"], lf["bonds"], lf["stacks"], lf["maxikey"], T=T_298, box=w["box"], rc=RC,
+                     n_mg=m, n_cl=cl, n_k=kk, seed=1, center=500, rng=1).to_dict()
+    lreps = [System.from_arrays(dict(lb, seed=np.array([s], dtype=np.int64))) for s in range(1, 17)]
+    sps, lms = graph_steps_per_s(lreps, local, GRAPH_STEPS, PREC_MIXED)
+    return {"workload": "16 replicas x 1500-nt chain (4499 beads), 600 A box, 1300 Mg / 22100 Cl / 21000 K",
+            "particles_per_replica": n_particles(lreps[0]), "ms_per_step": lms, "replica_steps_per_s": sps,
+            "precision": "mixed"}
 
 
 def files_for_cpu():

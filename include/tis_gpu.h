@@ -302,6 +302,14 @@ int tis_replica_size(tis_handle *h, int replica, int *n_particles);
 #define TIS_N_STAGES 8
 int tis_profile_stages(tis_handle *h, int64_t n, double *ms);
 
+/* The same eight kernels timed inside the step as it runs (no counterpart in the
+ * reference): `steps` (1..1000) fused steps of every group captured with CUDA
+ * events around each kernel, all groups' graphs replayed concurrently;
+ * ms[TIS_N_STAGES] receives each kernel's mean duration per launch (one group,
+ * one step), averaged over the steps and groups, with the other groups' work
+ * running beside it.  Advances every replica by `steps` steps. */
+int tis_profile_in_step(tis_handle *h, int32_t steps, double *ms);
+
 /* Kernel launches enqueued by tis_step since the handle was created. */
 int tis_get_launch_count(tis_handle *h, int64_t *n);
 

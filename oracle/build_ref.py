@@ -74,8 +74,28 @@ def make_patched_copy(src):
     return dst
 
 
-def build(verbose=False):
-    """Returns the path of oracle/_ref/tis_ref, or None when no source is available."""
+# The timing binary (oracle/_ref/tis_ref_bench): the same patched engine built
+# as the CPU baseline is timed, -O3 and with glibc's own rand() (no shim); the
+# harness's --rng philox is then ignored.  The parity binary (tis_ref) keeps -O2
+# and the shim.
+BENCH_FLAGS = ["-O3", "-ffp-contract=off", "-fno-fast-math"]
+
+
+def _compile_all(jobs, verbose):
+    from concurrent.futures import ThreadPoolExecutor
+
+    def run(c):
+        if verbose:
+            print(" ".join(c))
+        subprocess.run(c, check=True)
+
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        list(ex.map(run, jobs))
+
+
+def build(verbose=False, bench=False):
+    """Returns the path of oracle/_ref/tis_ref (bench=True: oracle/_ref/tis_ref_bench),
+    or None when no source is available.  Both binaries are (re)built together."""
     src = reference_source()
     patched = os.path.join(OUT, "engine_patched.cpp")
     if src is not None:
@@ -83,20 +103,27 @@ def build(verbose=False):
     elif not os.path.isfile(patched):
         return None
     exe = os.path.join(OUT, "tis_ref")
+    exe_b = os.path.join(OUT, "tis_ref_bench")
+    if os.path.isfile(exe) and os.path.isfile(exe_b) and \
+            min(os.path.getmtime(exe), os.path.getmtime(exe_b)) > max(
+                os.path.getmtime(patched), os.path.getmtime(os.path.join(HERE, "ref_harness.cpp"))):
+        return exe_b if bench else exe
     common = ["g++", "-O2", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", HERE]
+    common_b = ["g++", *BENCH_FLAGS, "-w", "-I", HERE]
+    mpi = ["-I", os.path.join(HERE, "mpi_stub")]
     eng_o = os.path.join(OUT, "engine.o")
+    eng_b = os.path.join(OUT, "engine_bench.o")
     har_o = os.path.join(OUT, "harness.o")
-    cmds = [
-        common + ["-I", os.path.join(HERE, "mpi_stub"), "-include", os.path.join(HERE, "ref_rng_shim.h"),
-                  "-Dmain=tis_ref_main", "-c", patched, "-o", eng_o],
+    har_b = os.path.join(OUT, "harness_bench.o")
+    _compile_all([
+        common + mpi + ["-include", os.path.join(HERE, "ref_rng_shim.h"), "-Dmain=tis_ref_main", "-c", patched,
+                        "-o", eng_o],
+        common_b + mpi + ["-Dmain=tis_ref_main", "-c", patched, "-o", eng_b],
         common + ["-c", os.path.join(HERE, "ref_harness.cpp"), "-o", har_o],
-        ["g++", eng_o, har_o, "-o", exe, "-lm"],
-    ]
-    for c in cmds:
-        if verbose:
-            print(" ".join(c))
-        subprocess.run(c, check=True)
-    return exe
+        common_b + ["-c", os.path.join(HERE, "ref_harness.cpp"), "-o", har_b],
+    ], verbose)
+    _compile_all([["g++", eng_o, har_o, "-o", exe, "-lm"], ["g++", eng_b, har_b, "-o", exe_b, "-lm"]], verbose)
+    return exe_b if bench else exe
 
 
 if __name__ == "__main__":

@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from oracle_bridge import Oracle
-from systems import CASES, golden_inputs, load, pair_set, rel_err
+from systems import CASES, golden_inputs, load, pair_set, rel_err, stiffness_atol
 from tis_gb300 import (PREC_FP64, PREC_MIXED, NOISE_OFF, NOISE_REFERENCE, TERM_BONDED, TERM_HB, TERM_LR, TERM_SR,
                        TERM_STACK, Engine, TisError)
 
@@ -108,11 +108,10 @@ def _frame(s, case, frame):
 @pytest.mark.parametrize("frame", ["thermal", "initial"])
 @pytest.mark.parametrize("case", ["small", "central"])
 def test_term_forces_and_energies(systems, case, frame, prec_name, prec, tol):
-    """Per-term forces and energies on identical coordinates.  On the set-up frame
-    every tertiary stack sits exactly at its native geometry, where its true force
-    is zero and the FP32 absolute error (~1e-6 of the restraint stiffness) is the
-    whole force: there the mixed stacking term is held to the max-norm criterion
-    at 1e-4 and reported."""
+    """Per-term forces and energies on identical coordinates: ||dF|| / ||F|| and
+    max |dF_i| / max |F_i| within tol, with, in mixed precision, the per-bead FP32
+    allowance of stiffness_atol added (it matters on the set-up frame, where the
+    stacks' and native H-bonds' true forces vanish)."""
     s = systems[case]
     st = _frame(s, case, frame)
     o = _oracle(s)
@@ -120,6 +119,7 @@ def test_term_forces_and_energies(systems, case, frame, prec_name, prec, tol):
         o.set_state(st)
     o.populate_lists()
     ref = o.terms()
+    atol = stiffness_atol(s.to_dict()) if prec == PREC_MIXED else 0.0
     report = []
     for name, mask in TERMS:
         e = Engine([s], precision=prec)  # fresh: the H-bond term consumes Monte Carlo draws
@@ -132,13 +132,11 @@ def test_term_forces_and_energies(systems, case, frame, prec_name, prec, tol):
             assert np.abs(f).max() < 1e-12, name
             continue
         rel = rel_err(f, want)
-        mx = np.abs(f - want).max() / np.abs(want).max()
-        report.append(f"{name} rel {rel:.2e} max {mx:.2e}")
-        if prec == PREC_MIXED and frame == "initial" and name == "F_stack":
-            assert mx <= 1e-4, (name, mx)
-        else:
-            assert rel <= tol, (name, rel)
-            assert mx <= tol, (name, mx)
+        dabs = np.abs(f - want).max()
+        fmax = np.abs(want).max()
+        report.append(f"{name} rel {rel:.2e} max|dF| {dabs:.2e} (|F|max {fmax:.2e}, atol {atol:.1e})")
+        assert dabs <= tol * fmax + atol, (name, dabs, fmax)
+        assert np.linalg.norm(f - want) <= tol * np.linalg.norm(want) + atol * np.sqrt(want.size), (name, rel)
         for k in E_TERM[name]:
             assert en[k] == pytest.approx(ref[k], rel=tol, abs=tol * max(1.0, abs(ref[k]))), (name, k)
     print(f"{case} {frame} {prec_name}: " + "; ".join(report))
@@ -148,7 +146,8 @@ def test_term_forces_and_energies(systems, case, frame, prec_name, prec, tol):
     e.populate_lists()
     f, en = e.forces(0, TERM_SR | TERM_LR | TERM_BONDED | TERM_STACK | TERM_HB)
     total = sum(ref[n] for n, _ in TERMS)
-    assert rel_err(f, total) <= (1e-4 if (prec == PREC_MIXED and frame == "initial") else tol)
+    assert np.abs(f - total).max() <= tol * np.abs(total).max() + atol
+    assert np.linalg.norm(f - total) <= tol * np.linalg.norm(total) + atol * np.sqrt(total.size)
     assert en["Rg"] == pytest.approx(ref["Rg"], rel=1e-12)
 
 
@@ -221,15 +220,25 @@ def test_noise_free_trajectory_tracks_oracle(systems, prec_name, prec, tol_pos):
     assert e.counters(0)[2] == o.draws()
 
 
-@pytest.mark.parametrize("prec_name,prec,tol_pos", [("fp64", PREC_FP64, 0.1), ("mixed", PREC_MIXED, 1.0)])
+# Per-checkpoint bounds (A) of the 10^4-step divergence curves, every 1000 steps:
+# about three times the measured curves (FP64 6e-10, 6e-9, 5e-8, 1e-7, 2e-6, 1e-5,
+# 9e-6, 4e-5, 8e-4, 5e-3; mixed 5e-6, 3e-5, 3e-4, 2e-3, 1e-2, 2e-2, 2e-2, 9e-3,
+# 3e-2, 4e-2), made non-decreasing.
+ENVELOPE_10K = {
+    "fp64": [2e-9, 2e-8, 2e-7, 5e-7, 6e-6, 3e-5, 3e-5, 1.5e-4, 2.5e-3, 2e-2],
+    "mixed": [2e-5, 1e-4, 1e-3, 6e-3, 3e-2, 6e-2, 6e-2, 6e-2, 0.1, 0.12],
+}
+
+
+@pytest.mark.parametrize("prec_name,prec,tol_pos", [("fp64", PREC_FP64, 2e-2), ("mixed", PREC_MIXED, 0.12)])
 def test_noise_free_trajectory_10k_steps(systems, prec_name, prec, tol_pos):
     """10^4 noise-free steps of the small system against the FP64 oracle: the
-    divergence curve (max position deviation every 1000 steps) is printed.  Any
-    difference grows with the dynamics' own sensitivity (about tenfold per 1000
-    steps): the FP64 path, which differs from the oracle only in the order of its
-    force sums (1e-13 A after 100 steps), reaches ~5e-3 A at 10^4 steps (held to
-    0.1 A); mixed precision, which rounds each pair force to FP32, levels off at a
-    few 1e-2 A (held to 1 A, a fraction of a bond length)."""
+    divergence curve (max position deviation every 1000 steps) is printed and held
+    to ENVELOPE_10K checkpoint by checkpoint.  Any difference grows with the
+    dynamics' own sensitivity (about tenfold per 1000 steps): the FP64 path, which
+    differs from the oracle only in the order of its force sums (1e-13 A after 100
+    steps), reaches ~5e-3 A at 10^4 steps; mixed precision, which rounds each pair
+    force to FP32, levels off at a few 1e-2 A."""
     s = systems["small"]
     o = _oracle(s, noise=False)
     o.populate_lists()
@@ -242,6 +251,8 @@ def test_noise_free_trajectory_10k_steps(systems, prec_name, prec, tol_pos):
         e.sync()
         dev.append(np.abs(_positions(e.get_state(0)) - _positions(o.get_state())).max())
     print(f"{prec_name} max |dx| every 1000 steps:", " ".join(f"{d:.2e}" for d in dev))
+    for k, (d, bound) in enumerate(zip(dev, ENVELOPE_10K[prec_name])):
+        assert d < bound, (k, d, bound)
     assert max(dev) < tol_pos
 
 
