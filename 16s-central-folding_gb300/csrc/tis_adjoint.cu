@@ -12,11 +12,14 @@
 // FP64, with the discrete choices (cutoffs, Monte Carlo outcome, stack switching,
 // dihedral imaging branch) taken from the values as the forward pass takes them.
 //
-// Parameter derivatives use that every parameter but the ion radii enters its
-// terms as a factor (E_LJ = sqrt(ELJ_i ELJ_j); Q_C lB; st_E; hb_E), so
-// lambda . dF/dtheta is lambda . F_term / theta times the factor's derivative;
-// a radius moves the LJ contact distance D = R_i + R_j (dF/dD in closed form) and
-// the ion's friction (K1, K2, sigma of E:2897-2903).
+// Parameter derivatives use that every parameter but the ion radii and the Debye
+// length enters its terms as a factor (E_LJ = sqrt(ELJ_i ELJ_j); Q_C lB; st_E;
+// hb_E), so lambda . dF/dtheta is lambda . F_term / theta times the factor's
+// derivative; a radius moves the LJ contact distance D = R_i + R_j (dF/dD in
+// closed form) and the ion's friction (K1, K2, sigma of E:2897-2903); the Debye
+// length lambda_D of the screened Coulomb term U = C exp(-r / lambda_D) / r enters
+// in closed form (dU/dlambda_D = C kappa^2 exp(-kappa r), d(F/r)/dlambda_D =
+// C kappa^3 exp(-kappa r) / r with kappa = 1 / lambda_D; both vanish unscreened).
 #include <cstdio>
 
 #include "tis_kernels.cuh"
@@ -334,7 +337,7 @@ template <bool LR, class T>
 __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const double *tan, int mode)
 {
     using DT = DualT<T>;
-    __shared__ double s_red[9 * 32];
+    __shared__ double s_red[10 * 32];
     const int p = blockIdx.x * kBlock + threadIdx.x;
     const int r = d.blk_rep[blockIdx.x];
     const RepParams *R = d.rp + r;
@@ -343,7 +346,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const doub
     const int4 qp = d.q[p];
     const int tp = qp.w & 0xff, kp = (qp.w >> 8) & 0xff, act = (qp.w >> 16) & 1;
     const bool chp = kp != 1 && kp != 2;
-    double g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // parameters 6 .. 14
+    double g[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // parameters 6 .. 15
     double jx = 0, jy = 0, jz = 0;
     if (act) {
         const int cnt = LR ? d.n_lr[p] : d.n_sr[p];
@@ -405,10 +408,23 @@ __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const doub
                 }
             }
             if (cou) {
-                const DT psi = (T)R->qclb_d[J] / (rr * r2);
+                const double kap = R->kappa;
+                DT psi;
+                double u;  // the pair's Coulomb energy
+                if (kap == 0.0) {
+                    psi = (T)R->qclb_d[J] / (rr * r2);
+                    u = R->qclb_d[J] / (double)rr.v;
+                } else {  // screened: F / r = C exp(-kappa r) (1 + kappa r) / r^3
+                    const DT ex = dexp((T)(-kap) * rr);
+                    psi = (T)R->qclb_d[J] * ex * ((T)1 + (T)kap * rr) / (rr * r2);
+                    u = R->qclb_d[J] * (double)ex.v / (double)rr.v;
+                    const double ek = R->qclb_d[J] * (double)ex.v * kap * kap;  // dU/dlambda_D
+                    if (mode == 0) g[9] += 0.5 * ek;
+                    else g[9] += wl * ek * kap / (double)rr.v;
+                }
                 F = F + psi;
                 if (R->lB != 0.0) {
-                    if (mode == 0) g[8] += 0.5 * R->qclb_d[J] / (double)rr.v / R->lB;
+                    if (mode == 0) g[8] += 0.5 * u / R->lB;
                     else g[8] += wl * (double)psi.v / R->lB;
                 }
             }
@@ -424,9 +440,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_pair(Dev d, AdjDev a, const doub
             a.jv[2 * P + p] += jz;
         }
     }
-    block_reduce<9>(g, s_red);
+    block_reduce<10>(g, s_red);
     if (threadIdx.x == 0)
-        for (int k = 0; k < 9; ++k)
+        for (int k = 0; k < 10; ++k)
             if (g[k] != 0.0) atomicAdd(a.dth + r * kNP + 6 + k, g[k]);
 }
 

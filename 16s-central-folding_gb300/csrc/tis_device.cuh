@@ -51,6 +51,8 @@ struct RepParams {
     int lr_interval;
     double T, h, lB, rc2, r2sr, r2lr, skin;
     float rc2f, r2srf, r2lrf, Tf;
+    double kappa;                // inverse Debye length of the screened Coulomb term (0: unscreened, the reference)
+    float kappaf;
     double mass[10], k1[10], k2[10], sigma[10], vcap[10];
     double k2fix[10], k2sig[10];  // K2 * 2^-32 (fixed-point force to velocity), K2 * sigma (noise)
     // pair tables, 1..45 (E:2908-2938); dm = D_LJ - 1.5852

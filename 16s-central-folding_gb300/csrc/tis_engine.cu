@@ -423,6 +423,10 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         const double T = scalar_f64(s, "T", 0.615), hstep = scalar_f64(s, "h", 0.05);
         const double lB = scalar_f64(s, "lB", 332.0637090 * (0.03273600947 * T - 0.00669625750));
         const double rc = scalar_f64(s, "rc", 50.0);
+        // Debye length of the screened Coulomb term q_i q_j lB exp(-r / debye) / r (no
+        // counterpart in the reference, whose truncated Coulomb E:825-855 is debye = 0
+        // or infinity: unscreened)
+        const double debye = scalar_f64(s, "debye", 0.0);
         if (rc < prm.sr) return bail(fail(TIS_ERR_ARG, "replica %d: Coulomb cutoff %g below the SR radius %g", base + r, rc, prm.sr));
         for (int k = 0; k < 3; ++k) {
             const double L = box->as<double>()[k];
@@ -448,6 +452,8 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         R.T = T;
         R.h = hstep;
         R.lB = lB;
+        R.kappa = (debye > 0.0 && std::isfinite(debye)) ? 1.0 / debye : 0.0;
+        R.kappaf = (float)R.kappa;
         R.rc2 = rc * rc;
         R.r2sr = (prm.sr + prm.skin) * (prm.sr + prm.skin);
         R.r2lr = (rc + prm.skin) * (rc + prm.skin);

@@ -406,6 +406,7 @@ __device__ void pair_block(const Dev &d, int b, int force_all)
             long long ax = 0, ay = 0, az = 0;
             const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
             const float rc2 = R->rc2f, lo = rc2 * (1.0f - kBand), hi = rc2 * (1.0f + kBand);
+            const float kap = R->kappaf;
             for (int k = lane4; k < cnt; k += L) {
                 const int raw = __ldg(nbr + nb_idx(k, p, P));
                 const int j = raw & kIdxMask;
@@ -438,8 +439,14 @@ __device__ void pair_block(const Dev &d, int b, int force_all)
                     bool in = r2 <= lo || exact_r2(d, R, p, j) <= R->rc2;
                     if (in) {
                         const float rr = sqrtf(r2);
-                        F += s_qclb[J] / (r2 * rr);
-                        if (EN) e_c += 0.5 * (double)(s_qclb[J] / rr);
+                        if (kap == 0.0f) {
+                            F += s_qclb[J] / (r2 * rr);
+                            if (EN) e_c += 0.5 * (double)(s_qclb[J] / rr);
+                        } else {  // screened: U = C exp(-kappa r) / r, F / r = U (1 + kappa r) / r^2
+                            const float kr = kap * rr, u = s_qclb[J] * expf(-kr) / rr;
+                            F += u * (1.0f + kr) / r2;
+                            if (EN) e_c += 0.5 * (double)u;
+                        }
                     }
                 }
                 if (F != 0.0f) {
@@ -494,8 +501,14 @@ __device__ void pair_block(const Dev &d, int b, int force_all)
                 }
                 if ((LR || (chp && is_charged(kj))) && r2 <= R->rc2) {
                     const double rr = sqrt(r2);
-                    F += R->qclb_d[J] / (rr * r2);
-                    if (EN) e_c += 0.5 * R->qclb_d[J] / rr;
+                    if (R->kappa == 0.0) {
+                        F += R->qclb_d[J] / (rr * r2);
+                        if (EN) e_c += 0.5 * R->qclb_d[J] / rr;
+                    } else {
+                        const double kr = R->kappa * rr, u = R->qclb_d[J] * exp(-kr) / rr;
+                        F += u * (1.0 + kr) / r2;
+                        if (EN) e_c += 0.5 * u;
+                    }
                 }
                 ax += v[0] * F;
                 ay += v[1] * F;

@@ -64,7 +64,7 @@ struct Dev {
 
 // Adjoint work of one handle (tis_adjoint.cu).  Arrays of 3P or 9P values are
 // component-major (c * P + p) like the state arrays.
-constexpr int kNParams = 15;    // force-field parameters (TIS_N_PARAMS)
+constexpr int kNParams = 16;    // force-field parameters (TIS_N_PARAMS)
 struct AdjDev {
     const double *st2_dss;      // d st_E / d ss_D of every secondary stack
     const int *st2_cls;         // its 5' base (0 A, 1 C, 2 G, 3 U; -1 none)

@@ -191,6 +191,230 @@ int tis_write_cgpdb(const tis_system *s, const double *x, const double *y, const
     return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
 }
 
+namespace {
+
+// the arrays of a loaded system the topology exporter reads
+struct SysView {
+    const tis_system *s;
+    template <class T>
+    const T *arr(const char *name, int dtype, int64_t *count) const
+    {
+        const tis::Array *a = s->get(name);
+        if (!a || a->dtype != dtype) return nullptr;
+        *count = a->count();
+        return a->as<T>();
+    }
+};
+
+constexpr double kPi = 3.14159265358979323846264338328;
+
+// dihedral angle i1-i2-i3-i4 (0-based beads; -1: the origin, as the exporter reads
+// its unused bead 0), atan2 of the triple product over the normals' dot product
+double dihedral_host(const double *x, const double *y, const double *z, int i1, int i2, int i3, int i4)
+{
+    auto P = [&](int i, int c) { return i < 0 ? 0.0 : (c == 0 ? x[i] : c == 1 ? y[i] : z[i]); };
+    double v1[3], v2[3], v3[3];
+    for (int c = 0; c < 3; ++c) {
+        v1[c] = P(i2, c) - P(i1, c);
+        v2[c] = P(i3, c) - P(i2, c);
+        v3[c] = P(i4, c) - P(i3, c);
+    }
+    const double m[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+    const double n[3] = {v2[1] * v3[2] - v2[2] * v3[1], v2[2] * v3[0] - v2[0] * v3[2], v2[0] * v3[1] - v2[1] * v3[0]};
+    const double l = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+    return atan2((v1[0] * n[0] + v1[1] * n[1] + v1[2] * n[2]) * l, m[0] * n[0] + m[1] * n[1] + m[2] * n[2]);
+}
+
+// the value of a native periodic coordinate nat imaged to within pi of psi
+double image_near(double psi, double nat)
+{
+    if (fabs(psi - nat) <= kPi) return nat;
+    return psi - nat > kPi ? nat + 2.0 * kPi : nat - 2.0 * kPi;
+}
+
+}  // namespace
+
+int tis_write_ninfo(const tis_system *s, const char *path)
+{
+    if (!s || !path) return fail(TIS_ERR_ARG, "tis_write_ninfo: bad argument");
+    const SysView V{s};
+    int64_t ne = 0, nb = 0, n3 = 0, n2 = 0, nh = 0, c = 0, nx = 0, nst = 0;
+    const int32_t *ea0 = V.arr<int32_t>("entry_a0", TIS_I32, &ne), *ea1 = V.arr<int32_t>("entry_a1", TIS_I32, &c),
+                  *ecode = V.arr<int32_t>("entry_code", TIS_I32, &c);
+    const int32_t *bk = V.arr<int32_t>("bt_kind", TIS_I32, &nb), *ba = V.arr<int32_t>("bt_a", TIS_I32, &c),
+                  *bb = V.arr<int32_t>("bt_b", TIS_I32, &c), *bc = V.arr<int32_t>("bt_c", TIS_I32, &c);
+    const double *bk0 = V.arr<double>("bt_k0", TIS_F64, &c), *bx0 = V.arr<double>("bt_x0", TIS_F64, &c);
+    const int32_t *i3 = V.arr<int32_t>("st3_idx", TIS_I32, &n3), *site = V.arr<int32_t>("st3_site", TIS_I32, &c),
+                  *exc = V.arr<int32_t>("st_excess", TIS_I32, &nst);
+    const double *nat3 = V.arr<double>("st3_native", TIS_F64, &c), *E3 = V.arr<double>("st3_E", TIS_F64, &c);
+    const int32_t *i2 = V.arr<int32_t>("st2_idx", TIS_I32, &n2), *e2 = V.arr<int32_t>("st2_entry_i", TIS_I32, &c);
+    const double *r02 = V.arr<double>("st2_r0", TIS_F64, &c), *E2 = V.arr<double>("st2_E", TIS_F64, &c);
+    const int32_t *ih = V.arr<int32_t>("hb_idx", TIS_I32, &nh), *dode = V.arr<int32_t>("hb_dode", TIS_I32, &c);
+    const double *nath = V.arr<double>("hb_native", TIS_F64, &c), *Eh = V.arr<double>("hb_E", TIS_F64, &c);
+    const double *x = V.arr<double>("x", TIS_F64, &nx), *y = V.arr<double>("y", TIS_F64, &c),
+                 *z = V.arr<double>("z", TIS_F64, &c);
+    if (!ea0 || !ea1 || !ecode || !bk || !ba || !bb || !bc || !bk0 || !bx0 || !i3 || !site || !exc || !nat3 || !E3 ||
+        !i2 || !e2 || !r02 || !E2 || !ih || !dode || !nath || !Eh || !x || !y || !z)
+        return fail(TIS_ERR_ARG, "tis_write_ninfo: the system lacks its topology arrays (a loaded system has them)");
+    n3 /= 6;
+    n2 /= 7;
+    nh /= 6;
+    // bond and angle parameters of the loaded topology, keyed by their beads
+    std::map<std::pair<int, int>, std::pair<double, double>> bonds;
+    std::map<std::array<int, 3>, std::pair<double, double>> angles;
+    for (int64_t t = 0; t < nb; ++t) {
+        if (bk[t] == 0) bonds[{std::min(ba[t], bb[t]), std::max(ba[t], bb[t])}] = {bk0[t], bx0[t]};
+        else angles[{bb[t], std::min(ba[t], bc[t]), std::max(ba[t], bc[t])}] = {bk0[t], bx0[t]};
+    }
+    auto bond = [&](int a, int b, std::pair<double, double> *kv) {
+        auto it = bonds.find({std::min(a, b), std::max(a, b)});
+        if (it == bonds.end()) return false;
+        *kv = it->second;
+        return true;
+    };
+    auto angle = [&](int a, int m, int b, std::pair<double, double> *kv) {
+        auto it = angles.find({m, std::min(a, b), std::max(a, b)});
+        if (it == angles.end()) return false;
+        *kv = it->second;
+        return true;
+    };
+    FILE *f = fopen(path, "w");
+    if (!f) return fail(TIS_ERR_IO, "cannot open %s", path);
+    bool missing = false;
+    // the exporter's records (analysis/make_ninfo/16SCD_ninfo.cpp): bonds and angles
+    // (:6083-6250), then stacks (:5840-5997), then H-bonds (:6000-6080); bead
+    // numbers 1-based, angles in degrees
+    int ibd = 0, iangl = 0;
+    auto put_bond = [&](int a, int b, const char *tag) {
+        std::pair<double, double> kv;
+        if (!bond(a, b, &kv)) {
+            missing = true;
+            return;
+        }
+        ++ibd;
+        fprintf(f, "bond %6i %2i %2i %4i %4i %4i %4i %12.4f %3.1f %3.1f %12.4f %s\n", ibd, 1, 1, a + 1, b + 1, a + 1,
+                b + 1, kv.second, 1.0, 1.0, kv.first, tag);
+    };
+    auto put_angle = [&](int a, int m, int b, const char *tag) {
+        std::pair<double, double> kv;
+        if (!angle(a, m, b, &kv)) {
+            missing = true;
+            return;
+        }
+        ++iangl;
+        fprintf(f, "angl %6i %2i %2i %4i %4i %4i %4i %4i %4i", iangl, 1, 1, a + 1, m + 1, b + 1, a + 1, m + 1, b + 1);
+        fprintf(f, "%12.4f %3.1f %3.1f %12.4f %s\n", kv.second / kPi * 180.0, 1.0, 1.0, kv.first, tag);
+    };
+    const int NBP = (int)ne;
+    for (int e = 1; e <= NBP; e += 2) {  // sugar-base bond, base angles of each nucleotide
+        const char b = (char)ecode[e - 1];
+        if (b != 'A' && b != 'C' && b != 'G' && b != 'U') continue;
+        const int si = ea0[e - 1], bi = ea1[e - 1];
+        char tag[8];
+        snprintf(tag, sizeof tag, "S%c", b);
+        put_bond(si, bi, tag);
+        if (e < NBP) {
+            snprintf(tag, sizeof tag, "%cSP", b);
+            put_angle(bi, si, ea0[e], tag);
+        }
+        if (e > 1) {
+            snprintf(tag, sizeof tag, "PS%c", b);
+            put_angle(ea0[e - 2], si, bi, tag);
+        }
+    }
+    for (int e = 2; e <= NBP; e += 2) {  // sugar-phosphate bonds, P-S-P angles
+        const int pi_ = ea0[e - 1], si = ea0[e - 2];
+        put_bond(si, pi_, "SP");
+        if (e > 2) put_angle(ea0[e - 3], si, pi_, "PSP");
+    }
+    for (int e = 3; e <= NBP; e += 2) {  // phosphate-sugar bonds, S-P-S angles
+        const int si = ea0[e - 1], pj = ea0[e - 2], sk = ea0[e - 3];
+        put_bond(pj, si, "PS");
+        put_angle(sk, pj, si, "SPS");
+    }
+    // tertiary stacks: distance, two angles, three dihedrals at their natives
+    int it = 0, itang = 0, itdih = 0;
+    for (int64_t k = 0; k < n3; ++k) {
+        const int *q = i3 + 6 * k;  // k10 k11 k12 k20 k21 k22
+        const double *nv = nat3 + 6 * k;
+        const int s0 = site[2 * k], s1 = site[2 * k + 1];
+        const int ii = (s0 >= 1 && s0 <= nst && exc[s0 - 1] == 1) ? 2 : 1;
+        const int jj = (s1 >= 1 && s1 <= nst && exc[s1 - 1] == 1) ? 2 : 1;
+        ++it;
+        fprintf(f, "tbs-dist %6i %2i %2i %4i %4i %4i %4i %9.3f %7.2f 5.0 %3i %3i\n", it, 1, 1, q[1] + 1, q[4] + 1,
+                q[1] + 1, q[4] + 1, E3[k], nv[0], ii, jj);
+        const int ang[2][3] = {{q[0], q[1], q[4]}, {q[3], q[4], q[1]}};
+        for (int a = 0; a < 2; ++a) {
+            ++itang;
+            fprintf(f, "tbs-angl %6i %6i %2i %2i %4i %4i %4i %4i %4i %4i", it, itang, 1, 1, ang[a][0] + 1,
+                    ang[a][1] + 1, ang[a][2] + 1, ang[a][0] + 1, ang[a][1] + 1, ang[a][2] + 1);
+            fprintf(f, " %7.2f %3.1f\n", nv[1 + a] / kPi * 180.0, 1.5);
+        }
+        const int dih[3][4] = {{q[0], q[1], q[4], q[3]}, {q[4], q[1], q[0], q[2]}, {q[1], q[4], q[3], q[5]}};
+        for (int a = 0; a < 3; ++a) {
+            ++itdih;
+            fprintf(f, "tbs-dihd %6i %6i %2i %2i", it, itdih, 1, 1);
+            for (int r = 0; r < 2; ++r)
+                for (int u = 0; u < 4; ++u) fprintf(f, " %4i", dih[a][u] + 1);
+            fprintf(f, " %7.2f %4.2f\n", nv[3 + a] / kPi * 180.0, 0.15);
+        }
+    }
+    // secondary stacks: distance, and the two backbone dihedrals imaged near their
+    // fixed natives (-2.58684, 3.07135) from the loaded positions
+    int is = 0, isdih = 0;
+    for (int64_t k = 0; k < n2; ++k) {
+        const int *q = i2 + 7 * k;  // k_10 k00 k01 k10 k20 k21 k30
+        const int e = e2[k];
+        const char l0 = e >= 1 && e <= NBP ? (char)ecode[e - 1] : 'N';
+        const char l1 = e + 2 >= 1 && e + 2 <= NBP ? (char)ecode[e + 1] : 'N';
+        const double psi1 = dihedral_host(x, y, z, q[0], q[1], q[3], q[4]);
+        const double psi2 = dihedral_host(x, y, z, q[6], q[4], q[3], q[1]);
+        const double p10 = image_near(psi1, -2.58684), p20 = image_near(psi2, 3.07135);
+        ++is;
+        fprintf(f, "bs-dist %6i %2i %2i %4i %4i %4i %4i %9.3f %7.2f 1.40 %c-%c\n", is, 1, 1, q[2] + 1, q[5] + 1,
+                q[2] + 1, q[5] + 1, E2[k], r02[k], l0, l1);
+        const int dih[2][4] = {{q[0], q[1], q[3], q[4]}, {q[1], q[3], q[4], q[6]}};
+        const double nat[2] = {p10, p20};
+        const char *tag[2] = {"PSPS", "SPSP"};
+        for (int a = 0; a < 2; ++a) {
+            ++isdih;
+            fprintf(f, "bs-dihd %6i %6i %2i %2i", is, isdih, 1, 1);
+            for (int r = 0; r < 2; ++r)
+                for (int u = 0; u < 4; ++u) fprintf(f, " %4i", dih[a][u] + 1);
+            fprintf(f, " %7.2f %3.1f %s\n", nat[a] / kPi * 180.0, 4.0, tag[a]);
+        }
+    }
+    // hydrogen-bond candidates: distance (T tertiary, S secondary), two angles,
+    // three dihedrals at their natives
+    int ihb = 0, ihang = 0, ihdih = 0;
+    for (int64_t k = 0; k < nh; ++k) {
+        const int *q = ih + 6 * k;  // k10 k11 k12 k20 k21 k22
+        const double *nv = nath + 6 * k;
+        ++ihb;
+        fprintf(f, "hb-dist %6i %2i %2i %4i %4i %4i %4i %9.3f %7.2f 5.0 %c\n", ihb, 1, 1, q[1] + 1, q[4] + 1,
+                q[1] + 1, q[4] + 1, Eh[k], nv[0], dode[k] ? 'T' : 'S');
+        const int ang[2][3] = {{q[0], q[1], q[4]}, {q[3], q[4], q[1]}};
+        for (int a = 0; a < 2; ++a) {
+            ++ihang;
+            fprintf(f, "hb-angl %6i %6i %2i %2i %4i %4i %4i %4i %4i %4i", ihb, ihang, 1, 1, ang[a][0] + 1,
+                    ang[a][1] + 1, ang[a][2] + 1, ang[a][0] + 1, ang[a][1] + 1, ang[a][2] + 1);
+            fprintf(f, " %7.2f %3.1f\n", nv[1 + a] / kPi * 180.0, 1.5);
+        }
+        const int dih[3][4] = {{q[0], q[1], q[4], q[3]}, {q[4], q[1], q[0], q[2]}, {q[1], q[4], q[3], q[5]}};
+        for (int a = 0; a < 3; ++a) {
+            ++ihdih;
+            fprintf(f, "hb-dihd %6i %6i %2i %2i", ihb, ihdih, 1, 1);
+            for (int r = 0; r < 2; ++r)
+                for (int u = 0; u < 4; ++u) fprintf(f, " %4i", dih[a][u] + 1);
+            fprintf(f, " %7.2f %4.2f\n", nv[3 + a] / kPi * 180.0, 0.15);
+        }
+    }
+    const bool ok = !ferror(f);
+    fclose(f);
+    if (missing) return fail(TIS_ERR_FORMAT, "tis_write_ninfo: a bond or angle of the chain is not in the topology");
+    return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
+}
+
 int tis_write_dcd(tis_handle *h, int replica, const char *path, int32_t nsavc, double delta)
 {
     if (!h || !path || nsavc < 1) return fail(TIS_ERR_ARG, "tis_write_dcd: bad argument");

@@ -3,7 +3,7 @@
 //   tis_run [-D<ss_D>] [-E<hs_D>] [-d<st_D>] [-T<T>] [-c<c_Mg>] [-f<c_K>] [-s<seed>]
 //           [--steps N] [--every N] [--replicas R] [--precision mixed|fp64] [--device K]
 //           [--pdb F] [--bonds F] [--stacks F] [--maxikey F] [--box L] [--rc A] [--center B]
-//           [--checkpoint FILE] [--dcd] [--tune]
+//           [--checkpoint FILE] [--dcd] [--tune] [--debye A]
 //
 // The single-letter flags are the reference's (E:6082-6099) with its defaults;
 // the input files default to the reference's names in the working directory.
@@ -17,7 +17,9 @@
 // engine state at every frame and, when FILE exists at start, continues from it
 // bit for bit instead of the positions-only restart; --dcd also appends every frame
 // to a DCD trajectory per replica (Trajectory_..._s<seed>.dcd); --tune measures the
-// launch configuration first (cached in tis_tune.txt).
+// launch configuration first (cached in tis_tune.txt); --debye A screens the
+// Coulomb term as q_i q_j lB exp(-r / A) / r (0, the default: the reference's plain
+// truncated Coulomb).
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -92,6 +94,7 @@ int main(int argc, char **argv)
     int replicas = 1;
     std::string ckpt;
     bool dcd = false, tune = false;
+    double debye = 0.0;  // Debye length of a screened Coulomb term (0: the reference's plain Coulomb)
     for (int i = 1; i < argc; ++i) {
         const char *a = argv[i];
         auto next = [&](const char *flag) -> const char * {
@@ -117,6 +120,7 @@ int main(int argc, char **argv)
         else if (!strcmp(a, "--checkpoint")) ckpt = next(a);
         else if (!strcmp(a, "--dcd")) dcd = true;
         else if (!strcmp(a, "--tune")) tune = true;
+        else if (!strcmp(a, "--debye")) debye = atof(next(a));
         else if (a[0] == '-' && a[1] != '-') {
             switch (a[1]) {  // E:6082-6099
             case 'D': lp.ss_D = atof(a + 2); break;
@@ -145,6 +149,7 @@ int main(int argc, char **argv)
         tis_load_params q = lp;
         q.seed = seed0 + r;
         if (report(tis_system_load(&q, &sys[r]), "set-up")) return 1;
+        if (debye != 0.0 && report(tis_system_set(sys[r], "debye", TIS_F64, &debye, 1), "--debye")) return 1;
         files[r] = names(lp, q.seed);
     }
     if (tune) {

@@ -17,7 +17,7 @@ ENERGY_NAMES = ["E_lj", "E_coul_sr", "E_coul_lr", "E_bond", "E_angle", "E_excl",
 TERM_SR, TERM_LR, TERM_BONDED, TERM_STACK, TERM_HB = 1, 2, 4, 8, 16
 # force-field parameters of tis_param_grad / tis_traj_grad (TIS_N_PARAMS, in order)
 PARAM_NAMES = ["ss_D_A", "ss_D_C", "ss_D_G", "ss_D_U", "st_D", "hs_D", "eps_P", "eps_S", "eps_B", "eps_Mg", "eps_Cl",
-               "eps_K", "R_Mg", "R_K", "lB"]
+               "eps_K", "R_Mg", "R_K", "lB", "debye"]
 N_PARAMS = len(PARAM_NAMES)
 PREC_MIXED, PREC_FP64 = 0, 1
 NOISE_REFERENCE, NOISE_OFF = 0, 1

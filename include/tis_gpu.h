@@ -344,12 +344,16 @@ int tis_autotune(const tis_system *const *systems, int n_replicas, const tis_run
  *   12-13 RLJ of Mg and K (the contact distance R_i + R_j of pairs with an ion,
  *        E:2918-2922, and the friction 0.555 RLJ of the ion, E:2897-2903)
  *   14   lB, the Coulomb strength 332.06 (0.0327 T - 0.0067) (E:6109)
+ *   15   the Debye length lambda_D of the screened Coulomb term
+ *        q_i q_j lB exp(-r / lambda_D) / r (system scalar "debye"; 0 or infinity:
+ *        unscreened, the reference's truncated Coulomb E:825-855, where the
+ *        derivative is 0)
  * Derivatives follow the forces: the LJ energy is the shifted WCA form
  * E_LJ (s^12 - 2 s^6 + 1) without the reporting clamp below D2_LJ_MINIMUM, bonded
  * pairs carry the net LJ weight of the force path, and discrete events (H-bond
  * Monte Carlo choices, stack switching, list membership, velocity cap, ion wrap)
  * are held as the forward pass took them. */
-#define TIS_N_PARAMS 15
+#define TIS_N_PARAMS 16
 
 /* dU/dtheta of every replica at its current state: out[TIS_N_PARAMS * replica + j],
  * U the total potential (pairs, bonded, stacks, H-bonds).  The H-bond term uses

@@ -156,10 +156,17 @@ static double lj_force(const tis_o *o, double r2, int J) /* LJ_FORCE (E:801-821)
     return o->F_LJ[J] * (s14 - s8) * dr / r1;
 }
 
-static double coulomb_force(const tis_o *o, double r2, int J) /* COULOMB_TRUNCATED_FORCE (E:841-855) */
+/* COULOMB_TRUNCATED_FORCE (E:841-855); with a Debye length lambda (no counterpart in
+ * the reference) the screened form U = Q lB exp(-r / lambda) / r, whose force over
+ * r is U (1 + r / lambda) / r^2 */
+static double coulomb_force(const tis_o *o, double r2, int J)
 {
     if (r2 > o->D2_CT) return 0;
     double r1 = sqrt(r2);
+    if (o->d.debye > 0.0 && isfinite(o->d.debye)) {
+        double kr = r1 / o->d.debye, u = o->Q_C[J] * o->d.lB * exp(-kr) / r1;
+        return u * (1.0 + kr) / r2;
+    }
     return o->Q_C[J] * o->d.lB / (r1 * r2);
 }
 
@@ -177,6 +184,10 @@ static double wca_energy(const tis_o *o, double r2, int J) /* WCA_ENERGY (E:749-
 static double coulomb_energy(const tis_o *o, double r2, int J) /* COULOMB_TRUNCATED_ENERGY (E:825-837) */
 {
     if (r2 > o->D2_CT) return 0;
+    if (o->d.debye > 0.0 && isfinite(o->d.debye)) {
+        double r1 = sqrt(r2);
+        return o->Q_C[J] * o->d.lB * exp(-r1 / o->d.debye) / r1;
+    }
     return o->Q_C[J] * o->d.lB / sqrt(r2);
 }
 

@@ -42,6 +42,8 @@ typedef struct tis_o_desc {
     const int32_t *hb_dode, *hb_atom_off, *hb_atom_idx;
     int32_t n_hba;                       /* hydrogen-bonding atoms */
     const int32_t *hba_valence, *hba_cand_off, *hba_cand_idx;
+    double debye;                        /* Debye length of the screened Coulomb term, A (0: unscreened,
+                                            the reference's truncated Coulomb) */
 } tis_o_desc;
 
 typedef struct tis_o tis_o;

@@ -59,6 +59,7 @@ class _Desc(C.Structure):
         ("hb_dode", I32P), ("hb_atom_off", I32P), ("hb_atom_idx", I32P),
         ("n_hba", C.c_int32),
         ("hba_valence", I32P), ("hba_cand_off", I32P), ("hba_cand_idx", I32P),
+        ("debye", C.c_double),
     ]
 
 
@@ -144,6 +145,7 @@ class Oracle:
         d.n_hba = len(s["hba_valence"])
         d.hba_valence = i32("hba_valence"); d.hba_cand_off = i32("hba_cand_off")
         d.hba_cand_idx = i32("hba_cand_idx")
+        d.debye = float(np.asarray(s["debye"]).ravel()[0]) if "debye" in s else 0.0
         self._keep = keep
         self.h = C.c_void_p(lib.tis_o_create(C.byref(d)))
         self.n_hb = d.n_hb

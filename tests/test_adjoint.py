@@ -55,7 +55,7 @@ def param_grad(system, theta, state, prec=PREC_FP64):
 
 @pytest.mark.gpu
 def test_param_grad_matches_finite_differences(small, thermal):
-    """dU/dtheta of all 15 parameters at a thermal frame against central differences
+    """dU/dtheta of all 16 parameters at a thermal frame against central differences
     (h = 1e-4 relative) of the engine's total FP64 energy."""
     th0 = params_of(small)
     g = param_grad(small, th0, thermal)
@@ -64,6 +64,9 @@ def test_param_grad_matches_finite_differences(small, thermal):
     noise = max(abs(u1 - u0), 1e-14 * uabs)
     rows = []
     for j in range(N_PARAMS):
+        if th0[j] == 0.0:  # the Debye length of an unscreened system: no derivative
+            assert g[j] == 0.0, PARAM_NAMES[j]
+            continue
         hj = 1e-4 * abs(th0[j])
         tp, tm = th0.copy(), th0.copy()
         tp[j] += hj
@@ -96,6 +99,9 @@ def test_param_grad_matches_oracle_finite_differences(small, thermal):
     u0 = oracle_potential(small, th0, thermal)
     rows = []
     for j in range(N_PARAMS):
+        if th0[j] == 0.0:  # the Debye length of an unscreened system: no derivative
+            assert g[j] == 0.0, PARAM_NAMES[j]
+            continue
         hj = 1e-4 * abs(th0[j])
         tp, tm = th0.copy(), th0.copy()
         tp[j] += hj
@@ -152,6 +158,9 @@ def test_traj_grad_matches_finite_differences(small, thermal, steps, every):
     rows = [f"L {L[0]:.6e}, spread over 4 runs {max(L) - min(L):.2e}"]
     worst = 0.0
     for j in range(N_PARAMS):
+        if th0[j] == 0.0:  # the Debye length of an unscreened system: no derivative
+            assert dth[0, j] == 0.0, PARAM_NAMES[j]
+            continue
         hj = (1e-4 if PARAM_NAMES[j].startswith("R_") else 1e-3) * abs(th0[j])
         tp, tm = th0.copy(), th0.copy()
         tp[j] += hj
@@ -202,6 +211,9 @@ def test_traj_grad_matches_oracle_finite_differences(small, thermal):
     L0 = _loss(oracle_final_state(small, th0, thermal, 40), seed)
     rows = []
     for j in range(N_PARAMS):
+        if th0[j] == 0.0:  # the Debye length of an unscreened system: no derivative
+            assert dth[j] == 0.0, PARAM_NAMES[j]
+            continue
         hj = (1e-4 if PARAM_NAMES[j].startswith("R_") else 1e-3) * abs(th0[j])
         tp, tm = th0.copy(), th0.copy()
         tp[j] += hj

@@ -10,12 +10,27 @@ from tis_gb300 import N_PARAMS, STATE_NAMES, Engine, System
 EPS_TYPES = [[0], [1], [2, 3, 4, 5], [6], [7], [8]]
 
 
+def debye_of(system):
+    """The system's Debye length (0: unscreened, the reference's Coulomb)."""
+    d = system.to_dict()
+    return float(np.asarray(d["debye"]).ravel()[0]) if "debye" in d else 0.0
+
+
 def params_of(system):
-    """theta of a loaded system: ss_D (x4), st_D, hs_D, ELJ of P S B Mg Cl K, RLJ of Mg K, lB."""
+    """theta of a loaded system: ss_D (x4), st_D, hs_D, ELJ of P S B Mg Cl K, RLJ of Mg K, lB,
+    Debye length."""
     ss, st, hs = (float(system[k][0]) for k in ("ss_D", "st_D", "hs_D"))
     elj, rlj = system["elj"], system["rlj"]
     eps = [float(elj[t[0]]) for t in EPS_TYPES]
-    return np.array([ss] * 4 + [st, hs] + eps + [float(rlj[6]), float(rlj[8]), float(system["lB"][0])])
+    return np.array([ss] * 4 + [st, hs] + eps + [float(rlj[6]), float(rlj[8]), float(system["lB"][0]),
+                                                 debye_of(system)])
+
+
+def screened(system, debye):
+    """A copy of `system` with the Debye length of its Coulomb term set (0: unscreened)."""
+    arrays = system.to_dict()
+    arrays["debye"] = np.array([float(debye)])
+    return System.from_arrays(arrays)
 
 
 def with_params(system, theta):
@@ -38,6 +53,7 @@ def with_params(system, theta):
     rlj[6], rlj[8] = theta[12], theta[13]
     arrays["rlj"] = rlj
     arrays["lB"] = np.array([theta[14]])
+    arrays["debye"] = np.array([theta[15]])
     arrays["ss_D"] = np.array([theta[0]])
     arrays["st_D"] = np.array([theta[4]])
     arrays["hs_D"] = np.array([theta[5]])
@@ -91,4 +107,4 @@ def make_trajectory_function(system, steps, checkpoint_every, **engine_kw):
     return Trajectory, state_template
 
 
-assert N_PARAMS == 15 and len(STATE_NAMES) == 9
+assert N_PARAMS == 16 and len(STATE_NAMES) == 9
