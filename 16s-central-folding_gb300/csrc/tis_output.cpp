@@ -1,6 +1,10 @@
 // The reference's output files (E:6276-6312) and its restart read (E:6181-6211).
+#include <algorithm>
+#include <array>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "tis_host.h"
@@ -191,6 +195,8 @@ int tis_write_cgpdb(const tis_system *s, const double *x, const double *y, const
     return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
 }
 
+}  // extern "C"
+
 namespace {
 
 // the arrays of a loaded system the topology exporter reads
@@ -233,6 +239,8 @@ double image_near(double psi, double nat)
 }
 
 }  // namespace
+
+extern "C" {
 
 int tis_write_ninfo(const tis_system *s, const char *path)
 {

@@ -116,6 +116,7 @@ def _declare(L):
         "tis_density_destroy": [vp],
         "tis_write_psf": [vp, cp],
         "tis_write_cgpdb": [vp, dp, dp, dp, cp],
+        "tis_write_ninfo": [vp, cp],
         "tis_capture_graph": [vp, i32],
         "tis_checkpoint_save": [vp, cp],
         "tis_checkpoint_load": [vp, cp],
@@ -138,7 +139,7 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
             "tis_param_grad", "tis_traj_grad", "tis_autotune", "tis_density_create", "tis_density_add",
             "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd", "tis_capture_graph",
-            "tis_write_cgpdb", "tis_checkpoint_save", "tis_checkpoint_load", "tis_profile_in_step"]
+            "tis_write_cgpdb", "tis_checkpoint_save", "tis_checkpoint_load", "tis_profile_in_step", "tis_write_ninfo"]
 
 
 def read_last_frame(path, n):
@@ -251,6 +252,10 @@ class System:
     def write_psf(self, path):
         """The topology in the PSF layout of the reference's exporter (tis_write_psf)."""
         _check(lib().tis_write_psf(self.h, os.fsencode(path)))
+
+    def write_ninfo(self, path):
+        """The native-structure information (.ninfo) file of the reference's exporter (tis_write_ninfo)."""
+        _check(lib().tis_write_ninfo(self.h, os.fsencode(path)))
 
     def __del__(self):
         try:

@@ -236,6 +236,14 @@ int tis_write_psf(const tis_system *s, const char *path);
  * RECORD count lines, the beads (S, <base>b, P of residue R<base>), TER, the ions,
  * TER; coordinates x, y, z of n_particles each (NULL: the system's own). */
 int tis_write_cgpdb(const tis_system *s, const double *x, const double *y, const double *z, const char *path);
+/* The native-structure information file (CafeMol .ninfo) of the same exporter
+ * (analysis/make_ninfo/16SCD_ninfo.cpp:6473-6477, its write_ninfo_bond_angle,
+ * write_ninfo_basestack and write_ninfo_basepair): bond and angl records of the
+ * chain, tbs-dist/angl/dihd of the tertiary stacks and bs-dist/dihd of the
+ * secondary stacks, hb-dist/angl/dihd of every H-bond candidate, with the loaded
+ * system's parameters and natives (the record layout the exporter writes, before
+ * the hand edits of its do.sh). */
+int tis_write_ninfo(const tis_system *s, const char *path);
 int tis_write_dcd(tis_handle *h, int replica, const char *path, int32_t nsavc, double delta);
 
 /* Ion density grid of one replica accumulated on the device over frames (the

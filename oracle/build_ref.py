@@ -126,6 +126,32 @@ def build(verbose=False, bench=False):
     return exe_b if bench else exe
 
 
+EXPORTER_REL = os.path.join("analysis", "make_ninfo", "16SCD_ninfo.cpp")
+
+
+def build_exporter(verbose=False):
+    """The reference's topology exporter (analysis/make_ninfo/16SCD_ninfo.cpp, which
+    writes 16SCD_ninfo.ninfo, .psf and .cg.pdb from the four input files in its
+    working directory) compiled unmodified from where it lies, with the single-rank
+    MPI stub, into oracle/_ref/tis_ref_exporter.  Returns its path, or None when the
+    reference is absent (the exporter pins are CPU tests of this container)."""
+    roots = [os.environ.get("TIS_REFERENCE_ROOT"), "/root/reference"]
+    src = next((os.path.join(r, EXPORTER_REL) for r in roots if r and os.path.isfile(os.path.join(r, EXPORTER_REL))),
+               None)
+    if src is None:
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    exe = os.path.join(OUT, "tis_ref_exporter")
+    if os.path.isfile(exe) and os.path.getmtime(exe) > os.path.getmtime(src):
+        return exe
+    cmd = ["g++", "-O2", "-ffp-contract=off", "-w", "-include", os.path.join(HERE, "mpi_stub", "mpi.h"), src, "-o",
+           exe, "-lm"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
+    return exe
+
+
 if __name__ == "__main__":
     p = build(verbose="-v" in sys.argv)
     print(p if p else "reference source not available; oracle/_ref not built")
