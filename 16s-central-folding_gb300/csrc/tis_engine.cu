@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -120,6 +121,7 @@ struct Group {
     int tail_steps = 0;
     cudaEvent_t *pev = nullptr;      // when set (tis_profile_in_step): events recorded around every kernel
     int pev_next = 0;
+    long long list_gen = 0;          // advanced whenever the lists move (graphs holding their pointers go stale)
     int base = 0;  // handle-wide index of the group's first replica
     long long launches = 0;
     double *d_scalar = nullptr;
@@ -183,6 +185,7 @@ void enqueue_step(Group *h);
 // the captured step graphs hold the list pointers: dropped when the lists move
 void drop_graphs(Group *h)
 {
+    ++h->list_gen;
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->tail) cudaGraphExecDestroy(h->tail);
     h->graph = h->tail = nullptr;
@@ -1497,9 +1500,19 @@ struct tis_handle {
     std::vector<cudaEvent_t> join;
     std::vector<int> grp_of, loc_of;
     std::vector<tis_density *> densities;  // grids on this handle: released with it
+    // step graphs of the whole handle (every group's branch, forked from and joined
+    // into the handle's stream): the graph length and the last remainder length
+    struct StepGraph {
+        int steps = 0;
+        cudaGraphExec_t exec = nullptr;
+        std::vector<long long> gens;  // the groups' list generations it was captured with
+    };
+    StepGraph full, tail;
 
     ~tis_handle()
     {
+        for (StepGraph *sg : {&full, &tail})
+            if (sg->exec) cudaGraphExecDestroy(sg->exec);
         for (Group *g : groups) delete g;
         for (cudaEvent_t e : join) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
@@ -1957,75 +1970,158 @@ int tis_get_forces(tis_handle *h, int r, double *forces)
 // Bit-exact checkpoint: every array a step reads and leaves for the next one
 // (step_state: x, x_old, v, fixed-point positions, the held LR force, replica
 // counters with the rand() position, neighbour lists, H-bond status), per group.
+}  // extern "C"
+
+namespace {
+
+// FNV-1a over the replicas' constants that define the simulated system: sizes, box,
+// temperature, step, Coulomb strength and screening, cutoffs, centre bead, seeds,
+// per-type masses and friction factors, pair tables.  A checkpoint carries it so that
+// a handle made from other systems (or seeds) of the same sizes refuses it.
+struct Fnv {
+    uint64_t h = 1469598103934665603ull;
+    template <class T>
+    void add(const T *v, size_t n)
+    {
+        const unsigned char *b = reinterpret_cast<const unsigned char *>(v);
+        for (size_t i = 0; i < n * sizeof(T); ++i) h = (h ^ b[i]) * 1099511628211ull;
+    }
+};
+
+int system_hash(tis_handle *h, uint64_t *out)
+{
+    Fnv f;
+    for (Group *g : h->groups) {
+        std::vector<tis::RepParams> rp(g->R);
+        TIS_CUDA(cudaMemcpy(rp.data(), g->dev.rp, sizeof(tis::RepParams) * g->R, cudaMemcpyDeviceToHost));
+        for (const auto &R : rp) {
+            const int ints[6] = {R.n, R.npad, R.nrna, R.center - R.p0, R.lr_interval, R.nc};
+            f.add(ints, 6);
+            f.add(R.box, 3);
+            const double sc[8] = {R.T, R.h, R.lB, R.kappa, R.rc2, R.r2sr, R.r2lr, R.skin};
+            f.add(sc, 8);
+            f.add(&R.seed, 1);
+            f.add(R.mass, 10);
+            f.add(R.k1, 10);
+            f.add(R.k2, 10);
+            f.add(R.sigma, 10);
+            f.add(R.dlj2_d, 46);
+            f.add(R.flj_d, 46);
+            f.add(R.elj_d, 46);
+            f.add(R.qclb_d, 46);
+        }
+    }
+    *out = f.h;
+    return TIS_OK;
+}
+
+struct FileCloser {
+    void operator()(FILE *f) const
+    {
+        if (f) fclose(f);
+    }
+};
+using File = std::unique_ptr<FILE, FileCloser>;
+
+}  // namespace
+
+extern "C" {
+
+// Bit-exact checkpoint, format TISCKPT2: magic, groups and replicas, the system hash,
+// then per group its sizes, list capacity, lists-built flag and every step_state array
+// (size, bytes).
 int tis_checkpoint_save(tis_handle *h, const char *path)
 {
     Range range("tis_checkpoint_save");
     if (!h || !path) return fail(TIS_ERR_ARG, "tis_checkpoint_save: bad argument");
     TIS_CUDA(cudaSetDevice(h->prm.device));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
-    FILE *f = fopen(path, "wb");
+    uint64_t hash = 0;
+    int rc;
+    if ((rc = system_hash(h, &hash))) return rc;
+    File f(fopen(path, "wb"));
     if (!f) return fail(TIS_ERR_IO, "cannot open %s", path);
-    bool ok = fwrite("TISCKPT1", 1, 8, f) == 8;
+    bool ok = fwrite("TISCKPT2", 1, 8, f.get()) == 8;
     const int32_t head[2] = {(int32_t)h->groups.size(), h->R};
-    ok = ok && fwrite(head, 4, 2, f) == 2;
+    ok = ok && fwrite(head, 4, 2, f.get()) == 2 && fwrite(&hash, 8, 1, f.get()) == 1;
     std::vector<char> buf;
     for (Group *g : h->groups) {
         if (!ok) break;
         TIS_CUDA(cudaStreamSynchronize(g->stream));
         const int32_t gh[5] = {g->R, g->P, g->dev.cap_sr, g->dev.cap_lr, g->lists_built ? 1 : 0};
-        ok = ok && fwrite(gh, 4, 5, f) == 5;
+        ok = ok && fwrite(gh, 4, 5, f.get()) == 5;
         for (const auto &e : step_state(g)) {
             const uint64_t n = e.second;
             buf.resize(n);
             if (n) TIS_CUDA(cudaMemcpy(buf.data(), e.first, n, cudaMemcpyDeviceToHost));
-            ok = ok && fwrite(&n, 8, 1, f) == 1 && fwrite(buf.data(), 1, n, f) == n;
+            ok = ok && fwrite(&n, 8, 1, f.get()) == 1 && fwrite(buf.data(), 1, n, f.get()) == n;
         }
     }
-    ok = fclose(f) == 0 && ok;
+    ok = fclose(f.release()) == 0 && ok;
     return ok ? TIS_OK : fail(TIS_ERR_IO, "short write to %s", path);
 }
 
+// The whole file is read and checked against the handle (format, groups, sizes,
+// system hash, every array's size) before anything on the device changes; only then
+// do the lists take the saved capacity and the arrays their saved contents.
 int tis_checkpoint_load(tis_handle *h, const char *path)
 {
     Range range("tis_checkpoint_load");
     if (!h || !path) return fail(TIS_ERR_ARG, "tis_checkpoint_load: bad argument");
     TIS_CUDA(cudaSetDevice(h->prm.device));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
-    FILE *f = fopen(path, "rb");
+    File f(fopen(path, "rb"));
     if (!f) return fail(TIS_ERR_IO, "cannot open %s", path);
-    auto bad = [&](const char *why) {
-        fclose(f);
-        return fail(TIS_ERR_FORMAT, "%s: %s", path, why);
-    };
+    auto bad = [&](const char *why) { return fail(TIS_ERR_FORMAT, "%s: %s", path, why); };
     char magic[8];
     int32_t head[2];
-    if (fread(magic, 1, 8, f) != 8 || memcmp(magic, "TISCKPT1", 8) != 0 || fread(head, 4, 2, f) != 2)
+    if (fread(magic, 1, 8, f.get()) != 8 || memcmp(magic, "TISCKPT2", 8) != 0 || fread(head, 4, 2, f.get()) != 2)
         return bad("not a checkpoint written by tis_checkpoint_save");
     if (head[0] != (int32_t)h->groups.size() || head[1] != h->R)
         return bad("replica groups or replicas differ from the handle's");
-    std::vector<char> buf;
-    for (Group *g : h->groups) {
+    uint64_t saved = 0, mine = 0;
+    int rc;
+    if (fread(&saved, 8, 1, f.get()) != 1) return bad("truncated");
+    if ((rc = system_hash(h, &mine))) return rc;
+    if (saved != mine) return bad("written for other systems, parameters or seeds than the handle's");
+    struct GroupData {
         int32_t gh[5];
-        if (fread(gh, 4, 5, f) != 5) return bad("truncated");
-        if (gh[0] != g->R || gh[1] != g->P) return bad("a replica group's size differs from the handle's");
-        TIS_CUDA(cudaStreamSynchronize(g->stream));
-        if (gh[2] != g->dev.cap_sr || gh[3] != g->dev.cap_lr) {
-            const int rc = grow_lists(g, gh[2], gh[3]);  // the saved list capacity
-            if (rc) {
-                fclose(f);
-                return rc;
-            }
+        std::vector<std::vector<char>> arrays;
+    };
+    std::vector<GroupData> data(h->groups.size());
+    for (size_t gi = 0; gi < h->groups.size(); ++gi) {
+        Group *g = h->groups[gi];
+        GroupData &D = data[gi];
+        if (fread(D.gh, 4, 5, f.get()) != 5) return bad("truncated");
+        if (D.gh[0] != g->R || D.gh[1] != g->P) return bad("a replica group's size differs from the handle's");
+        if (D.gh[2] < 1 || D.gh[3] < 1) return bad("bad list capacity");
+        // step_state's sizes at the saved list capacity (the lists are its last two arrays)
+        std::vector<std::pair<void *, size_t>> want = step_state(g);
+        for (auto &e : want) {
+            if (e.first == (void *)g->dev.nbr_sr) e.second = sizeof(int) * (size_t)D.gh[2] * g->P;
+            if (e.first == (void *)g->dev.nbr_lr) e.second = sizeof(int) * (size_t)D.gh[3] * g->P;
         }
-        for (const auto &e : step_state(g)) {
+        for (const auto &e : want) {
             uint64_t n = 0;
-            if (fread(&n, 8, 1, f) != 1 || n != e.second) return bad("an array's size differs from the handle's");
-            buf.resize(n);
-            if (fread(buf.data(), 1, n, f) != n) return bad("truncated");
-            if (n) TIS_CUDA(cudaMemcpy(e.first, buf.data(), n, cudaMemcpyHostToDevice));
+            if (fread(&n, 8, 1, f.get()) != 1 || n != e.second) return bad("an array's size differs from the handle's");
+            D.arrays.emplace_back(n);
+            if (n && fread(D.arrays.back().data(), 1, n, f.get()) != n) return bad("truncated");
         }
-        g->lists_built = gh[4] != 0;
     }
-    fclose(f);
+    if (fgetc(f.get()) != EOF) return bad("trailing bytes after the last group");
+    f.reset();
+    for (size_t gi = 0; gi < h->groups.size(); ++gi) {
+        Group *g = h->groups[gi];
+        const GroupData &D = data[gi];
+        TIS_CUDA(cudaStreamSynchronize(g->stream));
+        if (D.gh[2] != g->dev.cap_sr || D.gh[3] != g->dev.cap_lr) {
+            if ((rc = grow_lists(g, D.gh[2], D.gh[3]))) return rc;  // the saved list capacity
+        }
+        const auto st = step_state(g);
+        for (size_t k = 0; k < st.size(); ++k)
+            if (st[k].second) TIS_CUDA(cudaMemcpy(st[k].first, D.arrays[k].data(), st[k].second, cudaMemcpyHostToDevice));
+        g->lists_built = D.gh[4] != 0;
+    }
     return TIS_OK;
 }
 
@@ -2064,11 +2160,84 @@ int tis_check_shifts(tis_handle *h)
     return each_group(h, [](Group *g) { return grp_check_shifts(g); });
 }
 
+}  // extern "C"
+
+namespace {
+
+// `steps` fused steps of every group captured from the handle's stream into one
+// graph: the fork, each group's steps on its own streams, the join
+int capture_handle(tis_handle *h, int steps, tis_handle::StepGraph *sg)
+{
+    if (sg->exec) cudaGraphExecDestroy(sg->exec);
+    sg->exec = nullptr;
+    sg->steps = 0;
+    TIS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = fork_groups(h);
+    for (Group *g : h->groups)
+        for (int s = 0; s < steps && rc == TIS_OK; ++s) enqueue_step(g);
+    if (rc == TIS_OK) rc = join_groups(h);
+    cudaGraph_t gr = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
+    if (rc) {
+        if (gr) cudaGraphDestroy(gr);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(TIS_ERR_CUDA, "capture of the step graph: %s", cudaGetErrorString(e));
+    const cudaError_t ei = cudaGraphInstantiate(&sg->exec, gr, 0);
+    cudaGraphDestroy(gr);
+    if (ei != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
+    sg->steps = steps;
+    sg->gens.clear();
+    for (Group *g : h->groups) sg->gens.push_back(g->list_gen);
+    return TIS_OK;
+}
+
+// list builds of the groups whose lists are not built, ordered after the work
+// queued on the handle's stream
+int build_missing_lists(tis_handle *h)
+{
+    bool need = false;
+    for (Group *g : h->groups) need = need || !g->lists_built;
+    if (!need) return TIS_OK;
+    return each_group(h, [](Group *g) { return g->lists_built ? TIS_OK : populate(g); });
+}
+
+// the handle's graph of `steps` steps in slot sg, captured again when its length
+// differs or a group's lists moved since its capture
+int handle_graph(tis_handle *h, int steps, tis_handle::StepGraph *sg)
+{
+    bool fresh = sg->exec && sg->steps == steps && sg->gens.size() == h->groups.size();
+    for (size_t k = 0; fresh && k < h->groups.size(); ++k) fresh = sg->gens[k] == h->groups[k]->list_gen;
+    return fresh ? TIS_OK : capture_handle(h, steps, sg);
+}
+
+}  // namespace
+
+extern "C" {
+
+// n fused steps of every replica.  With use_graph, from CUDA graphs of the whole
+// handle (one launch for all groups): the graph_steps-long graph replayed
+// n / graph_steps times, then a graph of the remaining steps (kept for the next
+// call with the same remainder); else direct launches.
 int tis_step(tis_handle *h, int64_t n)
 {
     Range range("tis_step");
     if (!h || n < 0) return fail(TIS_ERR_ARG, "tis_step: bad argument");
-    return each_group(h, [n](Group *g) { return grp_step(g, n); });
+    if (!h->prm.use_graph || n == 0) return each_group(h, [n](Group *g) { return grp_step(g, n); });
+    int rc;
+    if ((rc = build_missing_lists(h))) return rc;
+    const int gs = std::max(1, (int)h->prm.graph_steps);
+    const int64_t full = n / gs, rem = n % gs;
+    if (full > 0) {
+        if ((rc = handle_graph(h, gs, &h->full))) return rc;
+        for (int64_t k = 0; k < full; ++k) TIS_CUDA(cudaGraphLaunch(h->full.exec, h->stream));
+    }
+    if (rem > 0) {
+        if ((rc = handle_graph(h, (int)rem, &h->tail))) return rc;
+        TIS_CUDA(cudaGraphLaunch(h->tail.exec, h->stream));
+    }
+    for (Group *g : h->groups) g->launches += n * tis::kernel_launches_per_step();
+    return TIS_OK;
 }
 
 int tis_capture_graph(tis_handle *h, int32_t steps)
@@ -2076,16 +2245,13 @@ int tis_capture_graph(tis_handle *h, int32_t steps)
     if (!h || steps < 1) return fail(TIS_ERR_ARG, "tis_capture_graph: bad argument");
     h->prm.graph_steps = steps;
     h->prm.use_graph = 1;
-    return each_group(h, [steps](Group *g) -> int {
-        int rc;
-        if (!g->lists_built && (rc = populate(g))) return rc;
-        drop_graphs(g);
+    for (Group *g : h->groups) {
         g->prm.graph_steps = steps;
         g->prm.use_graph = 1;
-        if ((rc = capture_steps(g, steps, &g->graph))) return rc;
-        g->graph_steps = steps;
-        return TIS_OK;
-    });
+    }
+    int rc;
+    if ((rc = build_missing_lists(h))) return rc;
+    return capture_handle(h, steps, &h->full);
 }
 
 int tis_profile_stages(tis_handle *h, int64_t n, double *ms)

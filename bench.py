@@ -299,18 +299,21 @@ def timed_steps(eng, K, W, flush, stream, world, clk_device):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = eng.launches()
+    host_s = 0.0
     with ClockSampler(clk_device) as clk:
         for i, c in enumerate(chunks):
             with torch.cuda.stream(stream):
                 flush.zero_()  # L2 flush between timed replays (256 MB > 129 MB L2)
                 ev[i][0].record(stream)
+            t0 = time.perf_counter()
             eng.step(c)
+            host_s += time.perf_counter() - t0
             with torch.cuda.stream(stream):
                 ev[i][1].record(stream)
         eng.sync()
         torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in ev)
-    return ms, eng.launches() - launches0, chunks, clk.summary()
+    return ms, eng.launches() - launches0, chunks, clk.summary(), 1000.0 * host_s
 
 
 def e2e_measure(eng, K, n_rep, reps=3):
@@ -451,7 +454,7 @@ def gpu_arm(args):
         flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
         K = max(1, args.steps)
         W = max(3, args.warmup)
-        ms, launches, chunks, clocks = timed_steps(eng, K, W, flush, stream, world, local)
+        ms, launches, chunks, clocks, host_ms = timed_steps(eng, K, W, flush, stream, world, local)
         ms = max_over_ranks(ms, world, device=f"cuda:{local}")
         if world > 1:
             torch.distributed.barrier()
@@ -459,8 +462,9 @@ def gpu_arm(args):
         value = job_value(ms, world, N_REPLICAS, K)
         graph_steps = eng.params.graph_steps
         groups = eng.params.groups or (3 * N_REPLICAS + 15) // 16
-        launch = {"path": "CUDA graph replay", "graph_steps": graph_steps,
-                  "graph_replays_per_group": len(chunks), "chunks": chunks, "replica_groups": groups,
+        launch = {"path": "CUDA graph replay (one graph holds every replica group's branch)",
+                  "graph_steps": graph_steps, "graph_launches": len(chunks), "chunks": chunks,
+                  "host_enqueue_ms": host_ms, "replica_groups": groups,
                   "lanes_sr": eng.params.lanes_sr or 1, "lanes_lr": eng.params.lanes_lr or 4,
                   "config_source": tune_note, "autotune_s": tune_s}
 

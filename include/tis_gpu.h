@@ -193,13 +193,17 @@ int tis_check_shifts(tis_handle *h);         /* check_shifts              E:1741
  * the reference's fx,fy,fz after the Allreduce, E:2576-2585), x,y,z interleaved. */
 int tis_get_forces(tis_handle *h, int replica, double *forces);
 
-/* n steps of the whole sequence for every replica (CUDA-graph replay when
- * use_graph is set); asynchronous: returns after enqueueing. */
+/* n steps of the whole sequence for every replica; asynchronous: returns after
+ * enqueueing.  With use_graph the steps replay CUDA graphs that hold every replica
+ * group's branch (one launch for the whole handle): the graph of graph_steps
+ * steps n / graph_steps times, then a graph of the remaining n % graph_steps steps,
+ * kept for the next call with the same remainder; the graphs are captured on first
+ * use and again after the lists grow. */
 int tis_step(tis_handle *h, int64_t n);
-/* Captures (again) the CUDA graph of `steps` fused steps of every replica group,
- * building the lists first when needed; later tis_step calls replay it for every
- * whole `steps` (no counterpart in the reference; tis_step captures on its first
- * call otherwise). */
+/* Captures (again) the CUDA graph of `steps` fused steps of the whole handle,
+ * building the lists first when needed, and makes `steps` the graph length;
+ * later tis_step calls replay it for every whole `steps` (no counterpart in the
+ * reference; tis_step captures on its first call otherwise). */
 int tis_capture_graph(tis_handle *h, int32_t steps);
 /* Waits for the handle's stream; reports device-side error flags. */
 int tis_sync(tis_handle *h);
@@ -294,7 +298,10 @@ int tis_get_counters(tis_handle *h, int replica, int64_t *klok, int64_t *rebuild
  * the held LR force, every replica's counters and rand() position, the neighbour
  * lists and H-bond status of every replica group.  A handle created with the same
  * systems and run parameters continues from a loaded checkpoint exactly as the
- * saving handle would have continued (bit for bit in mixed precision). */
+ * saving handle would have continued (bit for bit in mixed precision).  The file
+ * records a hash of the replicas' sizes, parameters and seeds; tis_checkpoint_load
+ * reads and checks the whole file (format, groups, sizes, that hash) before it
+ * changes anything, and on TIS_ERR_FORMAT / TIS_ERR_IO leaves the handle as it was. */
 int tis_checkpoint_save(tis_handle *h, const char *path);
 int tis_checkpoint_load(tis_handle *h, const char *path);
 

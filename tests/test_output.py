@@ -257,6 +257,37 @@ def test_checkpoint_resumes_bit_for_bit(tmp_path):
 
 
 @pytest.mark.gpu
+def test_checkpoint_load_refuses_other_systems_and_damaged_files(tmp_path):
+    """A checkpoint loads only onto a handle of the same systems, parameters and
+    seeds; a truncated file or one with trailing bytes is refused; a refused load
+    leaves the handle's state untouched."""
+    systems = [load(golden_inputs(), "small", seed=s) for s in (3, 4)]
+    path = str(tmp_path / "run.ckpt")
+    a = Engine(systems)
+    a.populate_lists()
+    a.step(60)
+    a.checkpoint_save(path)
+    data = open(path, "rb").read()
+    other = Engine([load(golden_inputs(), "small", seed=s) for s in (3, 5)])  # same sizes, another seed
+    other.populate_lists()
+    other.step(10)
+    before = other.get_states()
+    cases = {"seed": path}
+    for name, blob in (("truncated", data[:-1000]), ("trailing", data + b"x")):
+        cases[name] = str(tmp_path / f"{name}.ckpt")
+        open(cases[name], "wb").write(blob)
+    for name, p in cases.items():
+        with pytest.raises(TisError) as err:
+            other.checkpoint_load(p)
+        assert err.value.code == 3, name  # TIS_ERR_FORMAT
+        after = other.get_states()
+        for k in before:
+            assert np.array_equal(after[k], before[k]), (name, k)
+    b = Engine(systems)
+    b.checkpoint_load(cases["seed"])  # the saving handle's systems accept it
+
+
+@pytest.mark.gpu
 def test_cli_checkpoint_continues_bit_for_bit(tmp_path):
     """tis_run --checkpoint: a run stopped at step 200 and started again to 400
     writes the same files, frame for frame, as one run to 400; --dcd appends every
