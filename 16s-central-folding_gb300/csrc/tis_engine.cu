@@ -1591,6 +1591,8 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
     if (prm.sr <= 0) prm.sr = 12.0;
     if (prm.skin <= 0) prm.skin = 3.0;
     if (prm.groups < 0) return fail(TIS_ERR_ARG, "tis_create: negative group count");
+    if (prm.fused_ctas < 0 || prm.fused_ctas > 8)
+        return fail(TIS_ERR_ARG, "tis_create: fused_ctas %d is not 0 .. 8", prm.fused_ctas);
     if (prm.lanes_sr == 0) prm.lanes_sr = tis::kLanesSR;
     if (prm.lanes_lr == 0) prm.lanes_lr = tis::kLanesLR;
     if (prm.lanes_sr != 1 && prm.lanes_sr != 2 && prm.lanes_sr != 4)
@@ -2164,6 +2166,20 @@ int tis_check_shifts(tis_handle *h)
 
 namespace {
 
+// `steps` steps of the group as launches of the persistent fused step kernel (at
+// most kFusedChunk steps per launch)
+constexpr int kFusedChunk = 1000;
+int enqueue_fused(Group *g, int64_t steps, int ctas)
+{
+    for (int64_t done = 0; done < steps;) {
+        const int n = (int)std::min<int64_t>(kFusedChunk, steps - done);
+        const int e = tis::launch_step_fused(g->dev, g->stream, n, ctas);
+        if (e != 0) return fail(TIS_ERR_CUDA, "fused step kernel launch: %s", cudaGetErrorString((cudaError_t)e));
+        done += n;
+    }
+    return TIS_OK;
+}
+
 // `steps` fused steps of every group captured from the handle's stream into one
 // graph: the fork, each group's steps on its own streams, the join
 int capture_handle(tis_handle *h, int steps, tis_handle::StepGraph *sg)
@@ -2173,8 +2189,12 @@ int capture_handle(tis_handle *h, int steps, tis_handle::StepGraph *sg)
     sg->steps = 0;
     TIS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     int rc = fork_groups(h);
-    for (Group *g : h->groups)
-        for (int s = 0; s < steps && rc == TIS_OK; ++s) enqueue_step(g);
+    for (Group *g : h->groups) {
+        if (rc) break;
+        if (h->prm.fused_ctas > 0) rc = enqueue_fused(g, steps, h->prm.fused_ctas);
+        else
+            for (int s = 0; s < steps; ++s) enqueue_step(g);
+    }
     if (rc == TIS_OK) rc = join_groups(h);
     cudaGraph_t gr = nullptr;
     const cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
@@ -2186,6 +2206,8 @@ int capture_handle(tis_handle *h, int steps, tis_handle::StepGraph *sg)
     const cudaError_t ei = cudaGraphInstantiate(&sg->exec, gr, 0);
     cudaGraphDestroy(gr);
     if (ei != cudaSuccess) return fail(TIS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
+    // the graph's work moved to the device now, not at its first launch
+    TIS_CUDA(cudaGraphUpload(sg->exec, h->stream));
     sg->steps = steps;
     sg->gens.clear();
     for (Group *g : h->groups) sg->gens.push_back(g->list_gen);
@@ -2223,8 +2245,17 @@ int tis_step(tis_handle *h, int64_t n)
 {
     Range range("tis_step");
     if (!h || n < 0) return fail(TIS_ERR_ARG, "tis_step: bad argument");
-    if (!h->prm.use_graph || n == 0) return each_group(h, [n](Group *g) { return grp_step(g, n); });
     int rc;
+    if (n == 0) return TIS_OK;
+    if (h->prm.fused_ctas > 0 && !h->prm.use_graph) {
+        if ((rc = build_missing_lists(h))) return rc;
+        const int ctas = h->prm.fused_ctas;
+        rc = each_group(h, [n, ctas](Group *g) { return enqueue_fused(g, n, ctas); });
+        if (rc) return rc;
+        for (Group *g : h->groups) g->launches += (n + kFusedChunk - 1) / kFusedChunk;
+        return TIS_OK;
+    }
+    if (!h->prm.use_graph) return each_group(h, [n](Group *g) { return grp_step(g, n); });
     if ((rc = build_missing_lists(h))) return rc;
     const int gs = std::max(1, (int)h->prm.graph_steps);
     const int64_t full = n / gs, rem = n % gs;
@@ -2236,7 +2267,9 @@ int tis_step(tis_handle *h, int64_t n)
         if ((rc = handle_graph(h, (int)rem, &h->tail))) return rc;
         TIS_CUDA(cudaGraphLaunch(h->tail.exec, h->stream));
     }
-    for (Group *g : h->groups) g->launches += n * tis::kernel_launches_per_step();
+    for (Group *g : h->groups)  // kernel launches: per step, or per graph of the fused kernel
+        g->launches += h->prm.fused_ctas > 0 ? full * ((gs + kFusedChunk - 1) / kFusedChunk) + (rem > 0 ? 1 : 0)
+                                             : n * tis::kernel_launches_per_step();
     return TIS_OK;
 }
 
@@ -2335,6 +2368,43 @@ int tis_profile_in_step(tis_handle *h, int32_t steps, double *ms)
     if (rc) return rc;
     for (Group *g : h->groups)
         if ((rc = check_flags(g))) return rc;
+    return TIS_OK;
+}
+
+// The persistent fused step kernel run for `steps` steps with its phase timer on:
+// out[0..5] the mean microseconds per step of its phases (forces, of them the H-bond
+// chain, shift, move, control, and the rebuild per step that rebuilds), out[6] the
+// share of steps with an LR refresh, out[7] rebuilds per step; means over replicas.
+int tis_profile_fused(tis_handle *h, int32_t steps, int32_t ctas, double *out)
+{
+    if (!h || steps < 1 || ctas < 1 || ctas > 8 || !out) return fail(TIS_ERR_ARG, "tis_profile_fused: bad argument");
+    int rc;
+    if ((rc = build_missing_lists(h))) return rc;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    std::vector<double> acc(tis::kFusedPhases, 0.0);
+    for (Group *g : h->groups) {
+        unsigned long long *buf = nullptr;
+        const size_t n = (size_t)g->R * tis::kFusedPhases;
+        TIS_CUDA(cudaMalloc(&buf, n * sizeof(unsigned long long)));
+        cudaMemsetAsync(buf, 0, n * sizeof(unsigned long long), g->stream);
+        g->dev.fprof = buf;
+        const int e = tis::launch_step_fused(g->dev, g->stream, steps, ctas);
+        g->dev.fprof = nullptr;
+        std::vector<unsigned long long> hb(n);
+        cudaError_t ce = e ? (cudaError_t)e : cudaStreamSynchronize(g->stream);
+        if (ce == cudaSuccess) ce = cudaMemcpy(hb.data(), buf, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+        cudaFree(buf);
+        if (ce != cudaSuccess) return fail(TIS_ERR_CUDA, "tis_profile_fused: %s", cudaGetErrorString(ce));
+        for (int r = 0; r < g->R; ++r)
+            for (int k = 0; k < tis::kFusedPhases; ++k) acc[k] += (double)hb[(size_t)r * tis::kFusedPhases + k];
+        g->launches += 1;
+        if ((rc = check_flags(g))) return rc;
+    }
+    const double reps = (double)h->R, st = (double)steps;
+    for (int k = 0; k < 5; ++k) out[k] = acc[k] / reps / st * 1e-3;
+    out[5] = acc[7] > 0 ? acc[5] / acc[7] * 1e-3 : 0.0;
+    out[6] = acc[6] / reps / st;
+    out[7] = acc[7] / reps / st;
     return TIS_OK;
 }
 

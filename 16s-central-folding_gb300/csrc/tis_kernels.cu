@@ -371,6 +371,167 @@ __global__ void __launch_bounds__(kBlock) k_get_state(Dev d, double *stage, int 
 // ---------------------------------------------------------------------------
 // pair forces over the full (both-direction) neighbour lists
 // ---------------------------------------------------------------------------
+// Loads of data that the fused step kernel rewrites while it runs (positions,
+// lists) go through L2, the coherent path; the step's separate kernels read them
+// through the read-only path.
+template <bool CO, class T>
+__device__ __forceinline__ T ld_in(const T *ptr)
+{
+    if (CO) return __ldcg(ptr);
+    return __ldg(ptr);
+}
+
+// the replica's FP32 pair tables as the pair code reads them (shared memory copies)
+struct PairTables {
+    const float *dlj2, *dm, *flj, *qclb;
+};
+
+// The pair forces of particle p over its full list, by L threads (lane4 = its lane
+// among them): slot k of the list goes to lane k % L; lane 0 adds the sum (LR: stores
+// the held LR force).  err, e_lj, e_c accumulate per thread.
+template <bool D, bool LR, bool EN, bool EX, int L, bool CO>
+__device__ __forceinline__ void pair_particle(const Dev &d, const RepParams *R, int p, int lane4, const PairTables &tb,
+                                              int &err, double &e_lj, double &e_c)
+{
+    const int P = d.P;
+    const int4 qp = d.q[p];
+    const int tp = qp.w & 0xff, kp = (qp.w >> 8) & 0xff, act = (qp.w >> 16) & 1;
+    const bool chp = is_charged(kp);
+    const int cnt = act ? (LR ? d.n_lr[p] : d.n_sr[p]) : 0;
+    const int *nbr = LR ? d.nbr_lr : d.nbr_sr;
+    if (!D) {
+        long long ax = 0, ay = 0, az = 0;
+        const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
+        const float rc2 = R->rc2f, lo = rc2 * (1.0f - kBand), hi = rc2 * (1.0f + kBand);
+        const float kap = R->kappaf;
+        for (int k = lane4; k < cnt; k += L) {
+            const int raw = ld_in<CO>(nbr + nb_idx(k, p, P));
+            const int j = raw & kIdxMask;
+            const float ljw = EX ? (float)(1 - (raw >> kExclShift)) : 1.0f;
+            const int4 qj = ld_in<CO>(d.q + j);
+            const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
+            const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
+            const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const int tj = qj.w & 0xff, kj = (qj.w >> 8) & 0xff;
+            const int J = jn12(tp, tj);
+            float F = 0.0f;
+            if (!LR && ljw != 0.0f && r2 <= tb.dlj2[J]) {  // LJ_FORCE (E:801-821)
+                const float rr = sqrtf(r2);
+                const float dr = rr - tb.dm[J];
+                const float s = 1.5852f / dr;
+                const float s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+                F = ljw * (tb.flj[J] * (s14 - s8) * dr / rr);
+                if (EN) {
+                    double e;
+                    if ((double)r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
+                    else {
+                        const float s6 = s4 * s2, s12 = s6 * s6;
+                        e = (double)(R->elj[J] * (s12 - 2.0f * s6 + 1.0f));
+                    }
+                    e_lj += 0.5 * (double)ljw * e;
+                }
+            }
+            if ((LR || (chp && is_charged(kj))) && r2 <= hi) {  // COULOMB_TRUNCATED_FORCE (E:841-855)
+                bool in = r2 <= lo || exact_r2(d, R, p, j) <= R->rc2;
+                if (in) {
+                    const float rr = sqrtf(r2);
+                    if (kap == 0.0f) {
+                        F += tb.qclb[J] / (r2 * rr);
+                        if (EN) e_c += 0.5 * (double)(tb.qclb[J] / rr);
+                    } else {  // screened: U = C exp(-kappa r) / r, F / r = U (1 + kappa r) / r^2
+                        const float kr = kap * rr, u = tb.qclb[J] * expf(-kr) / rr;
+                        F += u * (1.0f + kr) / r2;
+                        if (EN) e_c += 0.5 * (double)u;
+                    }
+                }
+            }
+            if (F != 0.0f) {
+                ax += to_fix(F * dx, err);
+                ay += to_fix(F * dy, err);
+                az += to_fix(F * dz, err);
+            }
+        }
+        for (int o = 1; o < L; o <<= 1) {
+            ax += __shfl_xor_sync(kFull, ax, o);
+            ay += __shfl_xor_sync(kFull, ay, o);
+            az += __shfl_xor_sync(kFull, az, o);
+        }
+        if (lane4 == 0) {
+            if (LR) {  // the LR force is kept for the MTS interval: overwrite
+                d.flr[p] = (unsigned long long)ax;
+                d.flr[P + p] = (unsigned long long)ay;
+                d.flr[2 * P + p] = (unsigned long long)az;
+            } else if (act) {  // other force kernels run concurrently: accumulate
+                atomic_add_fix(d.f + p, ax);
+                atomic_add_fix(d.f + P + p, ay);
+                atomic_add_fix(d.f + 2 * P + p, az);
+            }
+        }
+    } else {
+        double ax = 0, ay = 0, az = 0;
+        for (int k = lane4; k < cnt; k += L) {
+            const int raw = ld_in<CO>(nbr + nb_idx(k, p, P));
+            const int j = raw & kIdxMask;
+            const double ljw = EX ? (double)(1 - (raw >> kExclShift)) : 1.0;
+            const int tj = d.q[j].w & 0xff, kj = (d.q[j].w >> 8) & 0xff;
+            const int J = jn12(tp, tj);
+            double v[3];
+            exact_vec(d, R, p, j, v);
+            const double r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+            double F = 0.0;
+            if (!LR && ljw != 0.0 && r2 <= R->dlj2_d[J]) {
+                const double rr = sqrt(r2);
+                const double dr = rr + kSig0 - R->dlj_d[J];
+                const double s = kSig0 / dr;
+                const double s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
+                F = ljw * (R->flj_d[J] * (s14 - s8) * dr / rr);
+                if (EN) {
+                    double e;
+                    if (r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
+                    else {
+                        const double s6 = s4 * s2, s12 = s6 * s6;
+                        e = R->elj_d[J] * (s12 - 2.0 * s6 + 1.0);
+                    }
+                    e_lj += 0.5 * ljw * e;
+                }
+            }
+            if ((LR || (chp && is_charged(kj))) && r2 <= R->rc2) {
+                const double rr = sqrt(r2);
+                if (R->kappa == 0.0) {
+                    F += R->qclb_d[J] / (rr * r2);
+                    if (EN) e_c += 0.5 * R->qclb_d[J] / rr;
+                } else {
+                    const double kr = R->kappa * rr, u = R->qclb_d[J] * exp(-kr) / rr;
+                    F += u * (1.0 + kr) / r2;
+                    if (EN) e_c += 0.5 * u;
+                }
+            }
+            ax += v[0] * F;
+            ay += v[1] * F;
+            az += v[2] * F;
+        }
+        for (int o = 1; o < L; o <<= 1) {
+            ax += __shfl_xor_sync(kFull, ax, o);
+            ay += __shfl_xor_sync(kFull, ay, o);
+            az += __shfl_xor_sync(kFull, az, o);
+        }
+        if (lane4 == 0) {
+            if (LR) {
+                double *out = (double *)d.flr;
+                out[p] = ax;
+                out[P + p] = ay;
+                out[2 * P + p] = az;
+            } else if (act) {
+                double *out = (double *)d.f;
+                atomicAdd(out + p, ax);
+                atomicAdd(out + P + p, ay);
+                atomicAdd(out + 2 * P + p, az);
+            }
+        }
+    }
+}
+
 // Particle block b (kBlock particles) by T threads, L per particle: slot k of a
 // particle's list goes to its thread k % L; the block's particles in kBlock L / T passes.
 template <bool D, bool LR, bool EN, bool EX, int L, int T>
@@ -389,150 +550,15 @@ __device__ void pair_block(const Dev &d, int b, int force_all)
         }
         __syncthreads();
     }
+    const PairTables tb{s_dlj2, s_dm, s_flj, s_qclb};
     const int lane4 = threadIdx.x & (L - 1);
-    const int P = d.P;
     int err = 0;
     double e_lj = 0, e_c = 0;
     constexpr int kPasses = kBlock * L / T;
 #pragma unroll
     for (int pass = 0; pass < kPasses; ++pass) {
         const int p = b * kBlock + pass * (T / L) + (int)threadIdx.x / L;
-        const int4 qp = d.q[p];
-        const int tp = qp.w & 0xff, kp = (qp.w >> 8) & 0xff, act = (qp.w >> 16) & 1;
-        const bool chp = is_charged(kp);
-        const int cnt = act ? (LR ? d.n_lr[p] : d.n_sr[p]) : 0;
-        const int *nbr = LR ? d.nbr_lr : d.nbr_sr;
-        if (!D) {
-            long long ax = 0, ay = 0, az = 0;
-            const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
-            const float rc2 = R->rc2f, lo = rc2 * (1.0f - kBand), hi = rc2 * (1.0f + kBand);
-            const float kap = R->kappaf;
-            for (int k = lane4; k < cnt; k += L) {
-                const int raw = __ldg(nbr + nb_idx(k, p, P));
-                const int j = raw & kIdxMask;
-                const float ljw = EX ? (float)(1 - (raw >> kExclShift)) : 1.0f;
-                const int4 qj = __ldg(d.q + j);
-                const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
-                const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
-                const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                const int tj = qj.w & 0xff, kj = (qj.w >> 8) & 0xff;
-                const int J = jn12(tp, tj);
-                float F = 0.0f;
-                if (!LR && ljw != 0.0f && r2 <= s_dlj2[J]) {  // LJ_FORCE (E:801-821)
-                    const float rr = sqrtf(r2);
-                    const float dr = rr - s_dm[J];
-                    const float s = 1.5852f / dr;
-                    const float s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
-                    F = ljw * (s_flj[J] * (s14 - s8) * dr / rr);
-                    if (EN) {
-                        double e;
-                        if ((double)r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
-                        else {
-                            const float s6 = s4 * s2, s12 = s6 * s6;
-                            e = (double)(R->elj[J] * (s12 - 2.0f * s6 + 1.0f));
-                        }
-                        e_lj += 0.5 * (double)ljw * e;
-                    }
-                }
-                if ((LR || (chp && is_charged(kj))) && r2 <= hi) {  // COULOMB_TRUNCATED_FORCE (E:841-855)
-                    bool in = r2 <= lo || exact_r2(d, R, p, j) <= R->rc2;
-                    if (in) {
-                        const float rr = sqrtf(r2);
-                        if (kap == 0.0f) {
-                            F += s_qclb[J] / (r2 * rr);
-                            if (EN) e_c += 0.5 * (double)(s_qclb[J] / rr);
-                        } else {  // screened: U = C exp(-kappa r) / r, F / r = U (1 + kappa r) / r^2
-                            const float kr = kap * rr, u = s_qclb[J] * expf(-kr) / rr;
-                            F += u * (1.0f + kr) / r2;
-                            if (EN) e_c += 0.5 * (double)u;
-                        }
-                    }
-                }
-                if (F != 0.0f) {
-                    ax += to_fix(F * dx, err);
-                    ay += to_fix(F * dy, err);
-                    az += to_fix(F * dz, err);
-                }
-            }
-            for (int o = 1; o < L; o <<= 1) {
-                ax += __shfl_xor_sync(kFull, ax, o);
-                ay += __shfl_xor_sync(kFull, ay, o);
-                az += __shfl_xor_sync(kFull, az, o);
-            }
-            if (lane4 == 0) {
-                if (LR) {  // the LR force is kept for the MTS interval: overwrite
-                    d.flr[p] = (unsigned long long)ax;
-                    d.flr[P + p] = (unsigned long long)ay;
-                    d.flr[2 * P + p] = (unsigned long long)az;
-                } else if (act) {  // other force kernels run concurrently: accumulate
-                    atomic_add_fix(d.f + p, ax);
-                    atomic_add_fix(d.f + P + p, ay);
-                    atomic_add_fix(d.f + 2 * P + p, az);
-                }
-            }
-        } else {
-            double ax = 0, ay = 0, az = 0;
-            for (int k = lane4; k < cnt; k += L) {
-                const int raw = __ldg(nbr + nb_idx(k, p, P));
-                const int j = raw & kIdxMask;
-                const double ljw = EX ? (double)(1 - (raw >> kExclShift)) : 1.0;
-                const int tj = d.q[j].w & 0xff, kj = (d.q[j].w >> 8) & 0xff;
-                const int J = jn12(tp, tj);
-                double v[3];
-                exact_vec(d, R, p, j, v);
-                const double r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
-                double F = 0.0;
-                if (!LR && ljw != 0.0 && r2 <= R->dlj2_d[J]) {
-                    const double rr = sqrt(r2);
-                    const double dr = rr + kSig0 - R->dlj_d[J];
-                    const double s = kSig0 / dr;
-                    const double s2 = s * s, s4 = s2 * s2, s8 = s4 * s4, s14 = s8 * s4 * s2;
-                    F = ljw * (R->flj_d[J] * (s14 - s8) * dr / rr);
-                    if (EN) {
-                        double e;
-                        if (r2 < R->d2min_d[J]) e = R->elj_d[J] * 1001.0;
-                        else {
-                            const double s6 = s4 * s2, s12 = s6 * s6;
-                            e = R->elj_d[J] * (s12 - 2.0 * s6 + 1.0);
-                        }
-                        e_lj += 0.5 * ljw * e;
-                    }
-                }
-                if ((LR || (chp && is_charged(kj))) && r2 <= R->rc2) {
-                    const double rr = sqrt(r2);
-                    if (R->kappa == 0.0) {
-                        F += R->qclb_d[J] / (rr * r2);
-                        if (EN) e_c += 0.5 * R->qclb_d[J] / rr;
-                    } else {
-                        const double kr = R->kappa * rr, u = R->qclb_d[J] * exp(-kr) / rr;
-                        F += u * (1.0 + kr) / r2;
-                        if (EN) e_c += 0.5 * u;
-                    }
-                }
-                ax += v[0] * F;
-                ay += v[1] * F;
-                az += v[2] * F;
-            }
-            for (int o = 1; o < L; o <<= 1) {
-                ax += __shfl_xor_sync(kFull, ax, o);
-                ay += __shfl_xor_sync(kFull, ay, o);
-                az += __shfl_xor_sync(kFull, az, o);
-            }
-            if (lane4 == 0) {
-                if (LR) {
-                    double *out = (double *)d.flr;
-                    out[p] = ax;
-                    out[P + p] = ay;
-                    out[2 * P + p] = az;
-                } else if (act) {
-                    double *out = (double *)d.f;
-                    atomicAdd(out + p, ax);
-                    atomicAdd(out + P + p, ay);
-                    atomicAdd(out + 2 * P + p, az);
-                }
-            }
-        }
+        pair_particle<D, LR, EN, EX, L, false>(d, R, p, lane4, tb, err, e_lj, e_c);
     }
     if (EN) {
         if (!LR) atomicAdd(d.eterm + r * kNE + 0, e_lj);
@@ -550,17 +576,28 @@ __global__ void __launch_bounds__(T) k_pair(Dev d, int force_all)
 // ---------------------------------------------------------------------------
 // block reductions
 // ---------------------------------------------------------------------------
-template <int NV>
-__device__ void block_sum(double (&v)[NV], double *smem /* NV * 32 */)
+// barriers of the threads that run a block-level part: the whole CTA, or warps
+// 0 .. n/32-1 of it on a named barrier (the fused step kernel's H-bond warps)
+struct CtaBar {
+    __device__ void operator()() const { __syncthreads(); }
+};
+struct NamedBar {
+    int id, n;
+    __device__ void operator()() const { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+};
+
+// sum of NV doubles over threads tid = 0 .. nthr-1 (a multiple of 32) into tid 0
+template <int NV, class Bar>
+__device__ void block_sum_t(double (&v)[NV], double *smem /* NV * 32 */, int tid, int nthr, Bar bar)
 {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    const int lane = tid & 31, w = tid >> 5, nw = (nthr + 31) >> 5;
 #pragma unroll
     for (int i = 0; i < NV; ++i)
         for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_down_sync(kFull, v[i], o);
-    __syncthreads();
+    bar();
     if (lane == 0)
         for (int i = 0; i < NV; ++i) smem[i * 32 + w] = v[i];
-    __syncthreads();
+    bar();
     if (w == 0) {
         for (int i = 0; i < NV; ++i) {
             double t = lane < nw ? smem[i * 32 + lane] : 0.0;
@@ -568,7 +605,13 @@ __device__ void block_sum(double (&v)[NV], double *smem /* NV * 32 */)
             v[i] = t;
         }
     }
-    __syncthreads();
+    bar();
+}
+
+template <int NV>
+__device__ void block_sum(double (&v)[NV], double *smem /* NV * 32 */)
+{
+    block_sum_t<NV>(v, smem, (int)threadIdx.x, (int)blockDim.x, CtaBar{});
 }
 
 // ---------------------------------------------------------------------------
@@ -629,11 +672,11 @@ __device__ inline void leap_frog(const Dev &d, const RepParams *R, int r, int p,
 // full_forces' Gaussians (E:2594-2606) of one replica from draw c0 on, by the
 // threads of one block
 template <bool D>
-__device__ void gen_noise(const Dev &d, int r, unsigned long long c0)
+__device__ void gen_noise(const Dev &d, int r, unsigned long long c0, int tid, int nthr)
 {
     const RepParams *R = d.rp + r;
     if (d.noise != 0) return;
-    for (int t = threadIdx.x; t < kNoise / 2; t += blockDim.x) {
+    for (int t = tid; t < kNoise / 2; t += nthr) {
         const uint32_t v1 = rand_value(R->seed, c0 + 2 * t);
         const uint32_t v2 = rand_value(R->seed, c0 + 2 * t + 1);
         if (D) {  // Box-Muller as the reference forms it (E:2598-2606), in FP64
@@ -660,7 +703,7 @@ __global__ void k_noise(Dev d)
 {
     const int r = blockIdx.x;
     const unsigned long long c0 = d.rs[r].ctr;
-    gen_noise<D>(d, r, c0);
+    gen_noise<D>(d, r, c0, (int)threadIdx.x, (int)blockDim.x);
     __syncthreads();
     if (threadIdx.x == 0) d.rs[r].ctr = c0 + kNoise;
 }
@@ -712,11 +755,11 @@ __device__ void exclusion_lj(const Dev &d, const RepParams *R, const Pos<D> &P, 
 // A secondary stack is off this step when a tertiary stack sharing one of its
 // sites (ST_EXCESS == 1) is within 10 A of its native distance (E:1960-1981);
 // each secondary stack checks the few tertiary stacks that can do that.
+// item t of the handle's bonded terms and stacks (above), by one thread
 template <bool D, bool EN>
-__global__ void __launch_bounds__(kTopoThreads) k_bonded_stack(Dev d, int mask, int excl_in_list)
+__device__ __forceinline__ void topo_item(const Dev &d, int t, int mask, int excl_in_list)
 {
     using Rl = Real<D>;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int r, kind;  // kind: 0 bonded, 1 tertiary, 2 secondary
     int item;
     if (t < d.nbt) { kind = 0; item = t; r = d.rep_of[d.bt_idx[t].x]; }
@@ -785,6 +828,12 @@ __global__ void __launch_bounds__(kTopoThreads) k_bonded_stack(Dev d, int mask, 
     if (A.err) atomicOr(&d.rs[r].err, A.err);
 }
 
+template <bool D, bool EN>
+__global__ void __launch_bounds__(kTopoThreads) k_bonded_stack(Dev d, int mask, int excl_in_list)
+{
+    topo_item<D, EN>(d, blockIdx.x * blockDim.x + threadIdx.x, mask, excl_in_list);
+}
+
 // ---------------------------------------------------------------------------
 // hydrogen bonds of one replica per block: energies, the valence-limited Monte
 // Carlo, forces; then (fused step) this step's Gaussians
@@ -832,15 +881,14 @@ __device__ inline void fill_draws(uint32_t *v, unsigned long long seed, unsigned
 // as (chunk of 32 bonds, term) warp tasks, so that the lanes of a warp evaluate
 // the same term; the Monte Carlo runs on one warp; then the step's Gaussians,
 // drawn by the block while its warps finish the force tasks.
-template <bool D, bool EN>
-__global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make_noise)
+template <bool D, bool EN, class Bar>
+__device__ __forceinline__ void hbond_block(const Dev &d, int r, int do_hb, int make_noise, int tid, int bd, Bar bar)
 {
     using Rl = Real<D>;
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ uint32_t s_v[64];  // draws vbase .. vbase + 63 of the replica's rand() stream
     __shared__ unsigned long long s_ctr;
     __shared__ double s_red[2 * 32];
-    const int r = blockIdx.x;
     const RepParams *R = d.rp + r;
     RepState *S = d.rs + r;
     const Pos<D> P = make_pos<D>(d, R);
@@ -848,13 +896,13 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
     A.f = (decltype(A.f))d.f;
     A.P = d.P;
     A.err = 0;
-    if (threadIdx.x == 0) s_ctr = S->ctr;
+    if (tid == 0) s_ctr = S->ctr;
     double e2hb = 0, e3hb = 0;
     const int hb0 = R->hb0, nhb = R->hb1 - R->hb0, ca0 = R->ca0, nca = R->ca1 - R->ca0;
-    const int tid = threadIdx.x, bd = blockDim.x, warp = tid >> 5, nwarp = bd >> 5, lane = tid & 31;
+    const int warp = tid >> 5, nwarp = bd >> 5, lane = tid & 31;
     HbWork w;
     const int nact = do_hb ? S->n_active : 0;
-    __syncthreads();
+    bar();
 
     // ---- hydrogen_bonds_interactions (E:2145-2350) ----
     if (do_hb) {
@@ -891,7 +939,7 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
             w.hb_off = d.hb_coff + hb0; w.hb_pos = d.hb_cpos;
         }
         for (int i = tid; i < nca; i += bd) w.exc[i] = d.hb_excess[d.ca_list[ca0 + i]];
-        __syncthreads();
+        bar();
         // a live bond whose central distance strays more than 2 A from native breaks (E:2165-2175)
         for (int t = tid; t < nact; t += bd) {
             const int k = d.hb_active[hb0 + t], kl = k - hb0;
@@ -916,7 +964,7 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
                 if (s >= 3) w.br[3 * kl + s - 3] = br;
             }
         }
-        __syncthreads();
+        bar();
         for (int t = tid; t < nact; t += bd) {
             const int k = d.hb_active[hb0 + t], kl = k - hb0;
             if (w.st[kl] == 1) continue;
@@ -925,7 +973,7 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
             w.en[kl] = (double)((Rl)d.hb_E[k] * exp_(-q));
             w.code[kl] = (w.br[3 * kl] + 1) + 3 * (w.br[3 * kl + 1] + 1) + 9 * (w.br[3 * kl + 2] + 1);
         }
-        __syncthreads();
+        bar();
         if (tid < 32) {  // valence-limited Monte Carlo (E:2239-2315), one warp
             const unsigned lt = (1u << lane) - 1u;
             unsigned long long ctr = s_ctr, vbase = ctr;
@@ -1004,7 +1052,7 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
             }
             if (lane == 0) s_ctr = ctr;
         }
-        __syncthreads();
+        bar();
         // forces of the bonds still formed: warp task (chunk of 32 live bonds, term 0..5)
         for (int task = warp; task < 6 * nchunk; task += nwarp) {
             const int s = task % 6, t = (task / 6) * 32 + lane;
@@ -1025,16 +1073,16 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
         for (int i = tid; i < nhb; i += bd) d.hb_rec[hb0 + i] = w.st[i] == 0 ? 1 : 0;
     // ---- full_forces: the step's Gaussians follow the Monte Carlo draws ----
     const unsigned long long c1 = s_ctr;
-    if (make_noise) gen_noise<D>(d, r, c1);
+    if (make_noise) gen_noise<D>(d, r, c1, tid, bd);
 
     double v[2] = {e2hb, e3hb};
-    block_sum<2>(v, s_red);
+    block_sum_t<2>(v, s_red, tid, bd, bar);
     if (do_hb)
         for (int t = tid; t < nact; t += bd) {  // every live bond is formed again for the next step
             const int kl = d.hb_active[hb0 + t] - hb0;
             if (w.st[kl] == 1) w.st[kl] = 0;
         }
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         S->ctr = make_noise ? c1 + kNoise : c1;
         if (do_hb) { S->e2hb = v[0]; S->e3hb = v[1]; }
         if (EN) {
@@ -1043,6 +1091,12 @@ __global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make
         }
     }
     if (A.err) atomicOr(&S->err, A.err);
+}
+
+template <bool D, bool EN>
+__global__ void __launch_bounds__(kHbThreads) k_hbond(Dev d, int do_hb, int make_noise)
+{
+    hbond_block<D, EN>(d, blockIdx.x, do_hb, make_noise, (int)threadIdx.x, (int)blockDim.x, CtaBar{});
 }
 
 __device__ void control_step(const Dev &d, int r);
@@ -1077,6 +1131,51 @@ __global__ void k_shift(Dev d)
     }
 }
 
+// move_rigid_units for particle p of replica r (leap-frog, the recentring shift
+// sh, the ions' periodic wrap, the new fixed-point position, its force sum zeroed);
+// bits: max |x - x_old|^2 as bit pattern, err: flags
+template <bool D>
+__device__ __forceinline__ void integrate_particle(const Dev &d, const RepParams *R, int r, int p, const double sh[3],
+                                                   unsigned long long &bits, int &err)
+{
+    const int4 qp = d.q[p];
+    if (!((qp.w >> 16) & 1)) return;
+    double xn[3], vn[3];
+    leap_frog<D>(d, R, r, p, xn, vn);
+    double xo[3] = {d.x[p], d.y[p], d.z[p]};
+    for (int c = 0; c < 3; ++c) {
+        xn[c] = xn[c] + sh[c];
+        xo[c] = xo[c] + sh[c];
+    }
+    if (p - R->p0 >= R->nrna) {  // periodic wrap of the ions (E:2676-2731)
+        for (int c = 0; c < 3; ++c) {
+            if (below_zero(xn[c])) { xn[c] += R->box[c]; xo[c] += R->box[c]; }
+            if (above(xn[c], R->box[c])) { xn[c] -= R->box[c]; xo[c] -= R->box[c]; }
+        }
+    }
+    double e2 = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        const double e = xn[c] - xo[c];
+        e2 += e * e;
+    }
+    bits = max(bits, (unsigned long long)__double_as_longlong(e2));
+    // a runaway or non-finite particle (|x| or |v| component >= 2^20) stops the run
+    bool ok = true;
+    for (int c = 0; c < 3; ++c) ok = ok && bounded(xn[c]) && bounded(vn[c]);
+    if (!ok) err |= kErrNonFinite;
+    d.x[p] = xn[0]; d.y[p] = xn[1]; d.z[p] = xn[2];
+    d.xo[p] = xo[0]; d.yo[p] = xo[1]; d.zo[p] = xo[2];
+    d.vx[p] = vn[0]; d.vy[p] = vn[1]; d.vz[p] = vn[2];
+    d.f[p] = 0ull;  // consumed: the next step's force kernels accumulate from zero
+    d.f[d.P + p] = 0ull;
+    d.f[2 * d.P + p] = 0ull;
+    int4 q = qp;  // floor(x L / 2^32) modulo 2^32, one rounding conversion per axis
+    q.x = (int)(unsigned)__double2ll_rd(xn[0] * R->qinv[0]);
+    q.y = (int)(unsigned)__double2ll_rd(xn[1] * R->qinv[1]);
+    q.z = (int)(unsigned)__double2ll_rd(xn[2] * R->qinv[2]);
+    d.q[p] = q;
+}
+
 // move_rigid_units (E:2660-2731) of one particle per thread: leap-frog, the
 // recentring shift, the periodic wrap of the ions; the replica's last block to
 // finish runs the skin check
@@ -1094,46 +1193,8 @@ __global__ void __launch_bounds__(kBlock / kIntPer) k_integrate(Dev d)
     unsigned long long bits = 0ull;  // max |x - x_old|^2 of the thread's particles (non-negative doubles order as integers)
     int err = 0;
 #pragma unroll
-    for (int j = 0; j < kIntPer; ++j) {
-    const int p = blockIdx.x * kBlock + j * (kBlock / kIntPer) + threadIdx.x;
-    const int4 qp = d.q[p];
-    if ((qp.w >> 16) & 1) {
-        double xn[3], vn[3];
-        leap_frog<D>(d, R, r, p, xn, vn);
-        double xo[3] = {d.x[p], d.y[p], d.z[p]};
-        for (int c = 0; c < 3; ++c) {
-            xn[c] = xn[c] + sh[c];
-            xo[c] = xo[c] + sh[c];
-        }
-        if (p - R->p0 >= R->nrna) {  // periodic wrap of the ions (E:2676-2731)
-            for (int c = 0; c < 3; ++c) {
-                if (below_zero(xn[c])) { xn[c] += R->box[c]; xo[c] += R->box[c]; }
-                if (above(xn[c], R->box[c])) { xn[c] -= R->box[c]; xo[c] -= R->box[c]; }
-            }
-        }
-        double e2 = 0.0;
-        for (int c = 0; c < 3; ++c) {
-            const double e = xn[c] - xo[c];
-            e2 += e * e;
-        }
-        bits = max(bits, (unsigned long long)__double_as_longlong(e2));
-        // a runaway or non-finite particle (|x| or |v| component >= 2^20) stops the run
-        bool ok = true;
-        for (int c = 0; c < 3; ++c) ok = ok && bounded(xn[c]) && bounded(vn[c]);
-        if (!ok) err |= kErrNonFinite;
-        d.x[p] = xn[0]; d.y[p] = xn[1]; d.z[p] = xn[2];
-        d.xo[p] = xo[0]; d.yo[p] = xo[1]; d.zo[p] = xo[2];
-        d.vx[p] = vn[0]; d.vy[p] = vn[1]; d.vz[p] = vn[2];
-        d.f[p] = 0ull;  // consumed: the next step's force kernels accumulate from zero
-        d.f[d.P + p] = 0ull;
-        d.f[2 * d.P + p] = 0ull;
-        int4 q = qp;  // floor(x L / 2^32) modulo 2^32, one rounding conversion per axis
-        q.x = (int)(unsigned)__double2ll_rd(xn[0] * R->qinv[0]);
-        q.y = (int)(unsigned)__double2ll_rd(xn[1] * R->qinv[1]);
-        q.z = (int)(unsigned)__double2ll_rd(xn[2] * R->qinv[2]);
-        d.q[p] = q;
-    }
-    }
+    for (int j = 0; j < kIntPer; ++j)
+        integrate_particle<D>(d, R, r, blockIdx.x * kBlock + j * (kBlock / kIntPer) + threadIdx.x, sh, bits, err);
     // check_shifts (E:1745-1762): max |x - x_old|^2 over the block
     for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long b = __shfl_down_sync(kFull, bits, o);
@@ -1259,13 +1320,11 @@ __device__ inline bool rebuild_item(const Dev &d, int per, int i, int &r, int &o
 constexpr int kCellThreads = 1024;
 
 template <bool D>
-__global__ void __launch_bounds__(kCellThreads) k_cells(Dev d)
+__device__ __forceinline__ void cells_block(const Dev &d, int r)
 {
-    wait_prior_grid();
     extern __shared__ int s_cells[];
     __shared__ int s_warp[32];
     __shared__ int s_carry;
-    const int r = blockIdx.x;
     RepState *S = d.rs + r;
     if (!S->rebuild) return;
     const RepParams *R = d.rp + r;
@@ -1405,6 +1464,13 @@ __global__ void __launch_bounds__(kCellThreads) k_cells(Dev d)
     }
 }
 
+template <bool D>
+__global__ void __launch_bounds__(kCellThreads) k_cells(Dev d)
+{
+    wait_prior_grid();
+    cells_block<D>(d, blockIdx.x);
+}
+
 // distinct periodic neighbours of cell index i (1..m) along one axis
 __device__ inline int axis_neighbours(int i, int m, int out[3])
 {
@@ -1428,129 +1494,281 @@ __device__ inline int axis_neighbours(int i, int m, int out[3])
 // One warp per particle: the lanes scan a neighbour cell's candidates together
 // (contiguous in cell order) and append hits in candidate order by ballot.  The
 // warps stride over the particles of the replicas that rebuild this step.
+// populate_lists' pair search for particle `off` of replica r by one warp; pre, beg:
+// the warp's 32 + 32 ints of shared memory
+template <bool D>
+__device__ __forceinline__ void search_particle(const Dev &d, int r, int off, int lane, int *pre, int *beg)
+{
+    const unsigned lt = (1u << lane) - 1u;
+    const int P = d.P;
+    const RepParams *R = d.rp + r;
+    const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
+    const float sr_lo = R->r2srf * (1.0f - kBand), sr_hi = R->r2srf * (1.0f + kBand);
+    const float lr_lo = R->r2lrf * (1.0f - kBand), lr_hi = R->r2lrf * (1.0f + kBand);
+    {
+        const int p = R->p0 + off;
+        const int c = d.cell_of[p];
+        if (c < 0) {
+            if (lane == 0) { d.n_sr[p] = 0; d.n_lr[p] = 0; }
+            return;
+        }
+        const int4 qp = d.q[p];
+        const bool chp = is_charged((qp.w >> 8) & 0xff);
+        const int i1 = c / (R->mc[1] * R->mc[2]) + 1, i2 = (c / R->mc[2]) % R->mc[1] + 1, i3 = c % R->mc[2] + 1;
+        int n1[3], n2[3], n3[3];
+        const int m1 = axis_neighbours(i1, R->mc[0], n1);
+        const int m2 = axis_neighbours(i2, R->mc[1], n2);
+        const int m3 = axis_neighbours(i3, R->mc[2], n3);
+        int exl[kExcl];
+        const int nex = d.n_excl[p];
+        for (int t2 = 0; t2 < kExcl; ++t2) exl[t2] = t2 < nex ? d.excl[(size_t)t2 * P + p] : -1;
+        // the neighbour cells' candidate ranges laid end to end, in the reference's
+        // cell order (lane s < 27 holds cell s of the 3 x 3 x 3 block)
+        const int nseg = m1 * m2 * m3;
+        __syncwarp();  // the previous particle's reads of pre/beg are done
+        int cnt_l = 0, start_l = 0;
+        if (lane < nseg) {
+            const int a = lane / (m2 * m3), b = (lane / m3) % m2, e = lane % m3;
+            const int cc = (n1[a] - 1) * R->mc[1] * R->mc[2] + (n2[b] - 1) * R->mc[2] + (n3[e] - 1);
+            start_l = R->p0 + d.cell_start[R->c0 + cc];
+            cnt_l = d.cell_count[R->c0 + cc];
+        }
+        int incl = cnt_l;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        if (lane < nseg) {
+            pre[lane] = incl - cnt_l;
+            beg[lane] = start_l;
+        }
+        if (lane == 0) pre[nseg] = total;
+        __syncwarp();
+        int nsr = 0, nlr = 0, seg = 0;
+        constexpr int kU = 4;  // candidate chunks of 32 whose loads are issued together
+        for (int t0 = 0; t0 < total; t0 += 32 * kU) {
+            int jv[kU];
+            int4 qv[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int t = t0 + 32 * u + lane;
+                jv[u] = -1;
+                qv[u] = make_int4(0, 0, 0, 0);
+                if (t < total) {
+                    while (t >= pre[seg + 1]) ++seg;
+                    const int slot = beg[seg] + (t - pre[seg]);
+                    jv[u] = d.cell_list[slot];
+                    qv[u] = d.qs[slot];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                if (t0 + 32 * u >= total) break;
+                const int j = jv[u];
+                const int4 qj = qv[u];
+                int cls = 0;  // 0 none, 1 SR, 2 LR
+                if (j >= 0 && j != p) {
+                    const bool ch = chp && is_charged((qj.w >> 8) & 0xff);
+                    const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
+                    const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
+                    const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
+                    const float r2f = dx * dx + dy * dy + dz * dz;
+                    if (D) {
+                        const double r2 = exact_r2(d, R, p, j);
+                        cls = r2 <= R->r2sr ? 1 : ((ch && r2 <= R->r2lr) ? 2 : 0);
+                    } else {
+                        if (r2f < sr_lo) cls = 1;
+                        else if (r2f > sr_hi && (!ch || r2f > lr_hi)) cls = 0;
+                        else if (r2f > sr_hi && r2f < lr_lo) cls = 2;
+                        else {
+                            const double e2 = exact_r2(d, R, p, j);
+                            cls = e2 <= R->r2sr ? 1 : ((ch && e2 <= R->r2lr) ? 2 : 0);
+                        }
+                    }
+                    // pruned list: a pair with an uncharged bead can only exert LJ, which
+                    // vanishes beyond D_LJ; the skin keeps it exact until the next rebuild
+                    if (cls == 1 && !d.full_lists && !ch && r2f > R->ljkeep2[jn12(qp.w & 0xff, qj.w & 0xff)])
+                        cls = 0;
+                }
+                const unsigned bs = __ballot_sync(kFull, cls == 1), bl = __ballot_sync(kFull, cls == 2);
+                if (cls == 1) {
+                    int m = 0;  // how often the reference subtracts this pair's LJ again
+                    for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
+                    const int pos = nsr + __popc(bs & lt);
+                    if (pos < d.cap_sr) d.nbr_sr[nb_idx(pos, p, P)] = j | (m << kExclShift);
+                } else if (cls == 2) {
+                    const int pos = nlr + __popc(bl & lt);
+                    if (pos < d.cap_lr) d.nbr_lr[nb_idx(pos, p, P)] = j;
+                }
+                nsr += __popc(bs);
+                nlr += __popc(bl);
+            }
+        }
+        if (lane == 0) {
+            if (nsr > d.cap_sr || nlr > d.cap_lr) atomicOr(&d.rs[r].err, kErrCapacity);
+            d.n_sr[p] = min(nsr, d.cap_sr);
+            d.n_lr[p] = min(nlr, d.cap_lr);
+        }
+    }
+}
+
 template <bool D>
 __global__ void __launch_bounds__(128) k_pair_search(Dev d)
 {
     wait_prior_grid();
     __shared__ int s_pre[4][32], s_beg[4][32];  // per warp: candidate offsets and first slots of its cells
     const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int P = d.P;
     int r, off;
-    for (int item = wid; rebuild_item(d, 0, item, r, off); item += d.search_warps) {
-        const RepParams *R = d.rp + r;
-        const float sx = R->qstep[0], sy = R->qstep[1], sz = R->qstep[2];
-        const float sr_lo = R->r2srf * (1.0f - kBand), sr_hi = R->r2srf * (1.0f + kBand);
-        const float lr_lo = R->r2lrf * (1.0f - kBand), lr_hi = R->r2lrf * (1.0f + kBand);
-        {
-            const int p = R->p0 + off;
-            const int c = d.cell_of[p];
-            if (c < 0) {
-                if (lane == 0) { d.n_sr[p] = 0; d.n_lr[p] = 0; }
-                continue;
-            }
-            const int4 qp = d.q[p];
-            const bool chp = is_charged((qp.w >> 8) & 0xff);
-            const int i1 = c / (R->mc[1] * R->mc[2]) + 1, i2 = (c / R->mc[2]) % R->mc[1] + 1, i3 = c % R->mc[2] + 1;
-            int n1[3], n2[3], n3[3];
-            const int m1 = axis_neighbours(i1, R->mc[0], n1);
-            const int m2 = axis_neighbours(i2, R->mc[1], n2);
-            const int m3 = axis_neighbours(i3, R->mc[2], n3);
-            int exl[kExcl];
-            const int nex = d.n_excl[p];
-            for (int t2 = 0; t2 < kExcl; ++t2) exl[t2] = t2 < nex ? d.excl[(size_t)t2 * P + p] : -1;
-            // the neighbour cells' candidate ranges laid end to end, in the reference's
-            // cell order (lane s < 27 holds cell s of the 3 x 3 x 3 block)
-            const int nseg = m1 * m2 * m3;
-            __syncwarp();  // the previous particle's reads of pre/beg are done
-            int cnt_l = 0, start_l = 0;
-            if (lane < nseg) {
-                const int a = lane / (m2 * m3), b = (lane / m3) % m2, e = lane % m3;
-                const int cc = (n1[a] - 1) * R->mc[1] * R->mc[2] + (n2[b] - 1) * R->mc[2] + (n3[e] - 1);
-                start_l = R->p0 + d.cell_start[R->c0 + cc];
-                cnt_l = d.cell_count[R->c0 + cc];
-            }
-            int incl = cnt_l;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(kFull, incl, o);
-                if (lane >= o) incl += t;
-            }
-            const int total = __shfl_sync(kFull, incl, 31);
-            int *pre = s_pre[threadIdx.x >> 5], *beg = s_beg[threadIdx.x >> 5];
-            if (lane < nseg) {
-                pre[lane] = incl - cnt_l;
-                beg[lane] = start_l;
-            }
-            if (lane == 0) pre[nseg] = total;
-            __syncwarp();
-            int nsr = 0, nlr = 0, seg = 0;
-            constexpr int kU = 4;  // candidate chunks of 32 whose loads are issued together
-            for (int t0 = 0; t0 < total; t0 += 32 * kU) {
-                int jv[kU];
-                int4 qv[kU];
-#pragma unroll
-                for (int u = 0; u < kU; ++u) {
-                    const int t = t0 + 32 * u + lane;
-                    jv[u] = -1;
-                    qv[u] = make_int4(0, 0, 0, 0);
-                    if (t < total) {
-                        while (t >= pre[seg + 1]) ++seg;
-                        const int slot = beg[seg] + (t - pre[seg]);
-                        jv[u] = d.cell_list[slot];
-                        qv[u] = d.qs[slot];
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < kU; ++u) {
-                    if (t0 + 32 * u >= total) break;
-                    const int j = jv[u];
-                    const int4 qj = qv[u];
-                    int cls = 0;  // 0 none, 1 SR, 2 LR
-                    if (j >= 0 && j != p) {
-                        const bool ch = chp && is_charged((qj.w >> 8) & 0xff);
-                        const float dx = (float)(int)((unsigned)qp.x - (unsigned)qj.x) * sx;
-                        const float dy = (float)(int)((unsigned)qp.y - (unsigned)qj.y) * sy;
-                        const float dz = (float)(int)((unsigned)qp.z - (unsigned)qj.z) * sz;
-                        const float r2f = dx * dx + dy * dy + dz * dz;
-                        if (D) {
-                            const double r2 = exact_r2(d, R, p, j);
-                            cls = r2 <= R->r2sr ? 1 : ((ch && r2 <= R->r2lr) ? 2 : 0);
-                        } else {
-                            if (r2f < sr_lo) cls = 1;
-                            else if (r2f > sr_hi && (!ch || r2f > lr_hi)) cls = 0;
-                            else if (r2f > sr_hi && r2f < lr_lo) cls = 2;
-                            else {
-                                const double e2 = exact_r2(d, R, p, j);
-                                cls = e2 <= R->r2sr ? 1 : ((ch && e2 <= R->r2lr) ? 2 : 0);
-                            }
-                        }
-                        // pruned list: a pair with an uncharged bead can only exert LJ, which
-                        // vanishes beyond D_LJ; the skin keeps it exact until the next rebuild
-                        if (cls == 1 && !d.full_lists && !ch && r2f > R->ljkeep2[jn12(qp.w & 0xff, qj.w & 0xff)])
-                            cls = 0;
-                    }
-                    const unsigned bs = __ballot_sync(kFull, cls == 1), bl = __ballot_sync(kFull, cls == 2);
-                    if (cls == 1) {
-                        int m = 0;  // how often the reference subtracts this pair's LJ again
-                        for (int t2 = 0; t2 < nex; ++t2) m += (exl[t2] == j);
-                        const int pos = nsr + __popc(bs & lt);
-                        if (pos < d.cap_sr) d.nbr_sr[nb_idx(pos, p, P)] = j | (m << kExclShift);
-                    } else if (cls == 2) {
-                        const int pos = nlr + __popc(bl & lt);
-                        if (pos < d.cap_lr) d.nbr_lr[nb_idx(pos, p, P)] = j;
-                    }
-                    nsr += __popc(bs);
-                    nlr += __popc(bl);
-                }
-            }
-            if (lane == 0) {
-                if (nsr > d.cap_sr || nlr > d.cap_lr) atomicOr(&d.rs[r].err, kErrCapacity);
-                d.n_sr[p] = min(nsr, d.cap_sr);
-                d.n_lr[p] = min(nlr, d.cap_lr);
+    for (int item = wid; rebuild_item(d, 0, item, r, off); item += d.search_warps)
+        search_particle<D>(d, r, off, lane, s_pre[threadIdx.x >> 5], s_beg[threadIdx.x >> 5]);
+}
+
+// ---------------------------------------------------------------------------
+// persistent fused step kernel: one thread-block cluster per replica runs `steps`
+// whole steps (the sequence of E:6380-6386) without leaving the kernel
+// ---------------------------------------------------------------------------
+// A replica's cluster of C CTAs (cluster dimension C, grid R x C) shares its work;
+// phases are separated by the cluster's hardware barrier (all CTAs of a cluster are
+// resident together, so no wait depends on another cluster).  Per step:
+//   forces   warps 0-7 of the first CTA: H-bond terms, the valence-limited Monte
+//            Carlo and the step's Gaussians (hbond_block on a named barrier); all
+//            other threads: SR pairs (one thread per particle), LR pairs when due
+//            (four per particle), bonded terms and stacks (one thread per item)
+//   shift    every CTA forms the recentring shift from the centre bead
+//   move     each CTA integrates its share of the particles; max |x - x_old|^2
+//   control  check_shifts and the LR gate (control_step) by the first CTA
+//   rebuild  when due: cell binning by the first CTA, pair search by every warp
+// Data the kernel rewrites while it runs is read through L2 (ld_in<true>, __ldcg).
+constexpr int kFusedThreads = 512;
+constexpr int kFusedHbThreads = 256;
+constexpr int kFusedWarps = kFusedThreads / 32;
+
+__device__ __forceinline__ int cluster_rank()
+{
+    unsigned v;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(v));
+    return (int)v;
+}
+__device__ __forceinline__ int cluster_ctas()
+{
+    unsigned v;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(v));
+    return (int)v;
+}
+// every thread of the cluster; writes before it (global and shared) are visible to
+// every thread of the cluster after it
+__device__ __forceinline__ void cluster_barrier()
+{
+    __threadfence();
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <bool D>
+__global__ void __launch_bounds__(kFusedThreads, 1) k_step_fused(Dev d, int steps)
+{
+    const int cs = cluster_ctas(), rank = cluster_rank();
+    const int r = blockIdx.x / cs;
+    const RepParams *R = d.rp + r;
+    RepState *S = d.rs + r;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ float s_dlj2[46], s_dm[46], s_flj[46], s_qclb[46];
+    __shared__ int s_pre[kFusedWarps][32], s_beg[kFusedWarps][32];
+    __shared__ double s_shift[3];
+    __shared__ unsigned long long s_max;
+    for (int t = tid; t < 46; t += kFusedThreads) {
+        s_dlj2[t] = R->dlj2[t];
+        s_dm[t] = R->dm[t];
+        s_flj[t] = R->flj[t];
+        s_qclb[t] = R->qclb[t];
+    }
+    __syncthreads();
+    const PairTables tb{s_dlj2, s_dm, s_flj, s_qclb};
+    const bool hbt = rank == 0 && tid < kFusedHbThreads;  // the H-bond threads
+    const int nwk = cs * kFusedThreads - kFusedHbThreads;  // pair workers (a multiple of 32)
+    const int wk = rank * kFusedThreads + tid - kFusedHbThreads;  // this thread's worker index (when !hbt)
+    const int npad = R->npad, p0 = R->p0;
+    const int nb = R->bt1 - R->bt0, n3 = R->s31 - R->s30, n2 = R->s21 - R->s20;
+    const int per = (npad / kBlock + cs - 1) / cs * kBlock;  // particles integrated per CTA
+    int err = 0;
+    // phase times (tis_profile_fused): the first thread of the cluster's first CTA
+    const bool timer = d.fprof && rank == 0 && tid == 0;
+    unsigned long long ph[kFusedPhases] = {0, 0, 0, 0, 0, 0, 0, 0}, t0 = timer ? global_ns() : 0ull, t1;
+    auto lap = [&](int k) {
+        if (timer) {
+            t1 = global_ns();
+            ph[k] += t1 - t0;
+            t0 = t1;
+        }
+    };
+    for (int step = 0; step < steps; ++step) {
+        const int lr_now = __ldcg(&S->lr_now);
+        if (hbt) {
+            hbond_block<D, false>(d, r, 1, 1, tid, kFusedHbThreads, NamedBar{1, kFusedHbThreads});
+            if (timer) ph[1] += global_ns() - t0;
+        } else {
+            double e0 = 0, e1 = 0;
+            for (int i = wk; i < npad; i += nwk) pair_particle<D, false, false, true, 1, true>(d, R, p0 + i, 0, tb, err, e0, e1);
+            if (lr_now)  // groups of four workers per particle (every group of a warp runs the same passes)
+                for (int i = wk >> 2; i < npad; i += nwk >> 2)
+                    pair_particle<D, true, false, false, 4, true>(d, R, p0 + i, wk & 3, tb, err, e0, e1);
+            for (int i = wk; i < nb + n3 + n2; i += nwk) {
+                const int t = i < nb ? R->bt0 + i
+                                     : (i < nb + n3 ? d.nbt + R->s30 + (i - nb) : d.nbt + d.nst3 + R->s20 + (i - nb - n3));
+                topo_item<D, false>(d, t, 4 | 8, 1);
             }
         }
+        cluster_barrier();
+        lap(0);
+        ph[6] += lr_now ? 1 : 0;
+        if (tid == 0) {  // adjust_box's shift (E:2632-2656) from the centre bead's new position
+            double xn[3], vn[3];
+            leap_frog<D>(d, R, r, R->center, xn, vn);
+            for (int c = 0; c < 3; ++c) s_shift[c] = R->hbox[c] - xn[c];
+            if (rank == 0)
+                for (int c = 0; c < 3; ++c) d.shift[3 * r + c] = s_shift[c];  // as k_shift leaves it
+            s_max = 0ull;
+        }
+        cluster_barrier();  // no CTA moves the centre bead before every CTA has read it
+        lap(2);
+        {
+            const double sh[3] = {s_shift[0], s_shift[1], s_shift[2]};
+            unsigned long long bits = 0ull;
+            const int i1 = min(npad, (rank + 1) * per);
+            for (int i = rank * per + tid; i < i1; i += kFusedThreads) integrate_particle<D>(d, R, r, p0 + i, sh, bits, err);
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long b = __shfl_down_sync(kFull, bits, o);
+                bits = b > bits ? b : bits;
+            }
+            if (lane == 0) atomicMax(&s_max, bits);
+            __syncthreads();
+            if (tid == 0) atomicMax(&S->maxd2, s_max);
+        }
+        cluster_barrier();
+        lap(3);
+        if (rank == 0) control_step(d, r);  // thread 0: check_shifts, the next step's LR gate
+        cluster_barrier();
+        lap(4);
+        if (__ldcg(&S->rebuild)) {  // populate_lists (E:1546-1737)
+            if (rank == 0) cells_block<D>(d, r);
+            cluster_barrier();
+            for (int off = rank * kFusedWarps + warp; off < npad; off += cs * kFusedWarps)
+                search_particle<D>(d, r, off, lane, s_pre[warp], s_beg[warp]);
+            cluster_barrier();
+            lap(5);
+            ph[7] += 1;
+        }
     }
+    if (err) atomicOr(&S->err, err);
+    if (timer)
+        for (int k = 0; k < kFusedPhases; ++k) atomicAdd(d.fprof + (size_t)r * kFusedPhases + k, ph[k]);
 }
 
 // radius_of_gyration (E:2844-2876) of the RNA beads of one replica
@@ -1764,6 +1982,11 @@ void launch_topology(const Dev &d, cudaStream_t s, int mask, bool en, bool make_
 int configure_kernels(const Dev &d)
 {
     cudaError_t e = cudaSuccess;
+    if (fused_smem(d) > 48 * 1024) {
+        const int b = (int)fused_smem(d);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    }
     if (d.cell_smem > 48 * 1024) {
         const int b = d.cell_smem;
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cells<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
@@ -1845,5 +2068,25 @@ void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out) { k_rg<<<
 
 // pair SR, pair LR, bonded+stacking, H-bonds (+Gaussians), shift, integrate (+skin check), cells, pair search
 int kernel_launches_per_step() { return 8; }
+
+size_t fused_smem(const Dev &d) { return (size_t)max(d.hb_smem, d.cell_smem); }
+
+int launch_step_fused(const Dev &d, cudaStream_t s, int steps, int ctas)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(d.R * ctas));
+    cfg.blockDim = dim3(kFusedThreads);
+    cfg.dynamicSmemBytes = fused_smem(d);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)ctas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return (int)(d.fp64 ? cudaLaunchKernelEx(&cfg, k_step_fused<true>, d, steps)
+                        : cudaLaunchKernelEx(&cfg, k_step_fused<false>, d, steps));
+}
 
 }  // namespace tis

@@ -60,7 +60,9 @@ struct Dev {
     const int *cell_rep;        // replica of every cell
     int *hb_rec;                // when not null: 1 per H-bond candidate formed after the step's Monte Carlo, else 0
     int lanes_sr, lanes_lr;     // threads per particle of the step's SR (1, 2, 4) and LR (2, 4, 8) pair launches
+    unsigned long long *fprof;  // when not null: the fused step kernel's phase times, kFusedPhases per replica (ns)
 };
+constexpr int kFusedPhases = 8;  // forces, H-bond chain, shift, move, control, rebuild, steps with LR, rebuild steps
 
 // Adjoint work of one handle (tis_adjoint.cu).  Arrays of 3P or 9P values are
 // component-major (c * P + p) like the state arrays.
@@ -135,6 +137,10 @@ void launch_search(const Dev &d, cudaStream_t s);
 void launch_force_all_rebuild(const Dev &d, cudaStream_t s);
 void launch_rg(const Dev &d, cudaStream_t s, int replica, double *out);
 int kernel_launches_per_step();
+// the persistent fused step kernel: `steps` whole steps of every replica, a cluster
+// of `ctas` CTAs (1..8) per replica; returns the launch's cudaError_t
+int launch_step_fused(const Dev &d, cudaStream_t s, int steps, int ctas);
+size_t fused_smem(const Dev &d);
 
 // ion density grids (tis_density.cu): the least-squares fit of replica r's beads idx
 // (replica-local) onto ref (3 per bead) into out[16] (R, frame centroid, reference

@@ -42,7 +42,7 @@ class RunParams(C.Structure):
                 ("lr_interval", C.c_int32), ("cap_sr", C.c_int32), ("cap_lr", C.c_int32), ("device", C.c_int32),
                 ("use_graph", C.c_int32), ("graph_steps", C.c_int32), ("full_lists", C.c_int32),
                 ("groups", C.c_int32), ("lanes_sr", C.c_int32), ("lanes_lr", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("fused_ctas", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
 _lib = None
@@ -105,6 +105,7 @@ def _declare(L):
         "tis_rand_stream": [C.c_uint64, C.c_uint64, i64, ip],
         "tis_profile_stages": [vp, i64, dp],
         "tis_profile_in_step": [vp, i32, dp],
+        "tis_profile_fused": [vp, i32, i32, dp],
         "tis_get_forces": [vp, i32, dp],
         "tis_pair_lists_noalloc": [vp, vp, vp, vp, C.c_int32, dp, C.c_double, C.c_double, vp, i64, vp, i64, vp, vp],
         "tis_param_grad": [vp, dp],
@@ -139,7 +140,7 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
             "tis_param_grad", "tis_traj_grad", "tis_autotune", "tis_density_create", "tis_density_add",
             "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd", "tis_capture_graph",
-            "tis_write_cgpdb", "tis_checkpoint_save", "tis_checkpoint_load", "tis_profile_in_step", "tis_write_ninfo"]
+            "tis_write_cgpdb", "tis_checkpoint_save", "tis_checkpoint_load", "tis_profile_in_step", "tis_write_ninfo", "tis_profile_fused"]
 
 
 def read_last_frame(path, n):
@@ -548,6 +549,15 @@ class Engine:
         ms = np.zeros(len(self.STAGES))
         _check(lib().tis_profile_in_step(self.h, steps, _dp(ms)))
         return dict(zip(self.STAGES, ms))
+
+    def profile_fused(self, steps, ctas):
+        """Phase times of the persistent fused step kernel (tis_profile_fused): dict of
+        microseconds per step and the LR and rebuild rates; advances every replica."""
+        out = np.zeros(8)
+        _check(lib().tis_profile_fused(self.h, steps, ctas, _dp(out)))
+        names = ["forces_us", "hbond_chain_us", "shift_us", "move_us", "control_us", "rebuild_us_per_rebuild",
+                 "lr_share", "rebuilds_per_step"]
+        return dict(zip(names, out.tolist()))
 
     def launches(self):
         n = C.c_int64()

@@ -19,11 +19,19 @@ def _flags():
             "-I", os.path.join(PKG, "..", "include")]
 
 
+# The step's kernels are compiled without implicit multiply-add contraction: the
+# same device functions run in the separate kernels and in the persistent fused
+# kernel, and contraction chosen per surrounding code would round them
+# differently; explicit fma() calls stay fused.
+NO_FMAD = {"tis_kernels.cu"}
+
+
 def _compile(src):
     obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
     inp = os.path.join(CSRC, src)
     lang = ["-x", "cu"] if src.endswith(".cu") else ["-x", "c++"]
-    cmd = [NVCC, *_flags(), *lang, "-c", inp, "-o", obj]
+    extra = ["-fmad=false"] if src in NO_FMAD else []
+    cmd = [NVCC, *_flags(), *extra, *lang, "-c", inp, "-o", obj]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return obj
 

@@ -433,7 +433,7 @@ def gpu_arm(args):
         # graph, threads per particle of the pair launches; 1000 steps per trial), or
         # fixed by --groups
         tune = {"groups": args.groups, "graph_steps": args.graph_steps, "lanes_sr": args.lanes_sr,
-                "lanes_lr": args.lanes_lr}
+                "lanes_lr": args.lanes_lr, "fused_ctas": args.fused_ctas}
         tune_s = None
         tune_note = "--groups"
         if args.groups == 0:
@@ -466,6 +466,7 @@ def gpu_arm(args):
                   "graph_steps": graph_steps, "graph_launches": len(chunks), "chunks": chunks,
                   "host_enqueue_ms": host_ms, "replica_groups": groups,
                   "lanes_sr": eng.params.lanes_sr or 1, "lanes_lr": eng.params.lanes_lr or 4,
+                  "fused_ctas": eng.params.fused_ctas,
                   "config_source": tune_note, "autotune_s": tune_s}
 
         if not args.extras:
@@ -689,6 +690,8 @@ def main():
     ap.add_argument("--graph-steps", type=int, default=GRAPH_STEPS, help="steps per graph with --groups")
     ap.add_argument("--lanes-sr", type=int, default=1, help="SR pair threads per particle with --groups")
     ap.add_argument("--lanes-lr", type=int, default=4, help="LR pair threads per particle with --groups")
+    ap.add_argument("--fused-ctas", type=int, default=0,
+                    help="with --groups: CTAs per replica of the persistent fused step kernel (0: separate kernels)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the large-system (48,899 particles x 16 replicas) throughput line")

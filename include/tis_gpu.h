@@ -124,7 +124,12 @@ typedef struct tis_run_params {
     int32_t lanes_sr;      /* threads per particle of the step's SR pair launch: 1, 2, 4 (0: 1) */
     int32_t lanes_lr;      /* threads per particle of the step's LR pair launch: 2, 4, 8 (0: 4); in mixed
                               precision results do not depend on either (fixed-point sums) */
-    int32_t reserved[2];
+    int32_t fused_ctas;    /* 0: a step is the chain of separate kernels (pair, bonded, H-bond, integrator,
+                              rebuild); 1..8: tis_step runs the persistent fused step kernel, in which one
+                              thread-block cluster of fused_ctas CTAs per replica runs whole steps back to
+                              back (one launch per replica group and call, or per graph replay with
+                              use_graph); mixed-precision results are the same bit for bit */
+    int32_t reserved[1];
 } tis_run_params;
 
 int tis_run_params_default(tis_run_params *p);
@@ -324,6 +329,16 @@ int tis_profile_stages(tis_handle *h, int64_t n, double *ms);
  * one step), averaged over the steps and groups, with the other groups' work
  * running beside it.  Advances every replica by `steps` steps. */
 int tis_profile_in_step(tis_handle *h, int32_t steps, double *ms);
+
+/* The persistent fused step kernel (tis_run_params.fused_ctas) run for `steps`
+ * steps of every replica, with `ctas` CTAs per replica and its phase timer on (no
+ * counterpart in the reference): out[0..5] = mean microseconds per step of the
+ * force phase, of the H-bond chain inside it (terms, Monte Carlo, Gaussians),
+ * the recentring shift, the integration, the control step, and the list rebuild
+ * per step that rebuilds; out[6] = share of steps that refresh the LR force,
+ * out[7] = list rebuilds per step; means over the replicas.  Advances every
+ * replica by `steps` steps. */
+int tis_profile_fused(tis_handle *h, int32_t steps, int32_t ctas, double *out);
 
 /* Kernel launches enqueued by tis_step since the handle was created. */
 int tis_get_launch_count(tis_handle *h, int64_t *n);
