@@ -1508,6 +1508,7 @@ struct tis_handle {
         std::vector<long long> gens;  // the groups' list generations it was captured with
     };
     StepGraph full, tail;
+    tis_frame_ring *ring = nullptr;  // frames written from inside the step (tis_frames_start)
 
     ~tis_handle()
     {
@@ -1640,11 +1641,15 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
 
 static void density_release(tis_density *d);
 
+static void ring_free(tis_frame_ring *f);
+
 int tis_destroy(tis_handle *h)
 {
     if (h) {
         cudaSetDevice(h->prm.device);
         cudaStreamSynchronize(h->stream);
+        if (h->ring) ring_free(h->ring);  // a ring does not outlive its handle
+        h->ring = nullptr;
         for (tis_density *d : h->densities) density_release(d);  // the grids stay valid handles, now empty
         h->densities.clear();
         for (Group *g : h->groups) grp_destroy(g);
@@ -2405,6 +2410,137 @@ int tis_profile_fused(tis_handle *h, int32_t steps, int32_t ctas, double *out)
     out[5] = acc[7] > 0 ? acc[5] / acc[7] * 1e-3 : 0.0;
     out[6] = acc[6] / reps / st;
     out[7] = acc[7] / reps / st;
+    return TIS_OK;
+}
+
+}  // extern "C"
+
+// The frame ring: pinned, device-mapped host memory the step's kernels write frames
+// into (layout in tis::FrameRing), and what the host needs to read it back.
+struct tis_frame_ring {
+    tis_handle *h = nullptr;
+    int every = 0, depth = 0, R = 0;
+    int64_t n = 0;
+    double *pos = nullptr, *en = nullptr;
+    long long *done = nullptr;
+};
+
+static void ring_free(tis_frame_ring *f)
+{
+    if (!f) return;
+    if (f->pos) cudaFreeHost(f->pos);
+    if (f->en) cudaFreeHost(f->en);
+    if (f->done) cudaFreeHost(f->done);
+    delete f;
+}
+
+namespace {
+
+// the ring's device view in every group (NULL detaches); the step graphs hold the
+// kernels' arguments, so they are captured again
+int ring_attach(tis_handle *h, const tis_frame_ring *f)
+{
+    int64_t pk_base = 0;
+    for (Group *g : h->groups) {
+        tis::FrameRing fr{};
+        if (f) {
+            TIS_CUDA(cudaHostGetDevicePointer((void **)&fr.pos, f->pos, 0));
+            TIS_CUDA(cudaHostGetDevicePointer((void **)&fr.en, f->en, 0));
+            TIS_CUDA(cudaHostGetDevicePointer((void **)&fr.done, f->done, 0));
+            fr.n_total = f->n;
+            fr.pk_base = pk_base;
+            fr.R_total = f->R;
+            fr.rep_base = g->base;
+            fr.every = f->every;
+            fr.depth = f->depth;
+        }
+        g->dev.fr = fr;
+        drop_graphs(g);
+        pk_base += g->npk;
+    }
+    return TIS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tis_frames_start(tis_handle *h, int32_t every, int32_t depth, tis_frame_ring **out)
+{
+    if (!h || every < 1 || depth < 2 || !out) return fail(TIS_ERR_ARG, "tis_frames_start: bad argument");
+    if (h->ring) return fail(TIS_ERR_STATE, "tis_frames_start: the handle already writes frames");
+    TIS_CUDA(cudaSetDevice(h->prm.device));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    auto *f = new tis_frame_ring;
+    f->h = h;
+    f->every = every;
+    f->depth = depth;
+    f->R = h->R;
+    for (Group *g : h->groups) f->n += g->npk;
+    const unsigned fl = cudaHostAllocMapped | cudaHostAllocPortable;
+    cudaError_t e = cudaHostAlloc((void **)&f->pos, sizeof(double) * 3 * (size_t)f->n * depth, fl);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&f->en, sizeof(double) * 5 * (size_t)f->R * depth, fl);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&f->done, sizeof(long long) * (size_t)f->R * depth, fl);
+    if (e != cudaSuccess) {
+        ring_free(f);
+        return fail(TIS_ERR_CUDA, "tis_frames_start: pinned host memory: %s", cudaGetErrorString(e));
+    }
+    for (size_t k = 0; k < (size_t)f->R * depth; ++k) f->done[k] = -1;
+    const int rc = ring_attach(h, f);
+    if (rc) {
+        ring_attach(h, nullptr);
+        ring_free(f);
+        return rc;
+    }
+    h->ring = f;
+    *out = f;
+    return TIS_OK;
+}
+
+int tis_frames_read(tis_frame_ring *f, int64_t klok, double *x, double *y, double *z, double *energies)
+{
+    if (!f || !f->h) return fail(TIS_ERR_ARG, "tis_frames_read: null ring");
+    if (klok < f->every || klok % f->every != 0)
+        return fail(TIS_ERR_ARG, "tis_frames_read: step %lld is not a frame step (every %d)", (long long)klok, f->every);
+    const size_t slot = (size_t)((klok / f->every) % f->depth);
+    const volatile long long *done = f->done + slot * f->R;
+    auto state = [&](bool *ready, bool *gone) {
+        *ready = true;
+        *gone = false;
+        for (int r = 0; r < f->R; ++r) {
+            const long long v = done[r];
+            *ready = *ready && v == klok;
+            *gone = *gone || v > klok;
+        }
+    };
+    bool ready, gone;
+    state(&ready, &gone);
+    if (!ready && !gone) {  // not written yet: wait for the work queued so far
+        TIS_CUDA(cudaStreamSynchronize(f->h->stream));
+        state(&ready, &gone);
+    }
+    if (gone) return fail(TIS_ERR_STATE, "tis_frames_read: the frame of step %lld was overwritten", (long long)klok);
+    if (!ready) return fail(TIS_ERR_STATE, "tis_frames_read: no frame of step %lld was written", (long long)klok);
+    const size_t n = (size_t)f->n;
+    const double *p = f->pos + slot * 3 * n;
+    if (x) memcpy(x, p, sizeof(double) * n);
+    if (y) memcpy(y, p + n, sizeof(double) * n);
+    if (z) memcpy(z, p + 2 * n, sizeof(double) * n);
+    if (energies) memcpy(energies, f->en + slot * 5 * (size_t)f->R, sizeof(double) * 5 * f->R);
+    state(&ready, &gone);  // still the same frame after the copy
+    if (!ready) return fail(TIS_ERR_STATE, "tis_frames_read: the frame of step %lld was overwritten while read", (long long)klok);
+    return TIS_OK;
+}
+
+int tis_frames_stop(tis_frame_ring *f)
+{
+    if (!f || !f->h) return fail(TIS_ERR_ARG, "tis_frames_stop: null ring");
+    tis_handle *h = f->h;
+    TIS_CUDA(cudaSetDevice(h->prm.device));
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
+    ring_attach(h, nullptr);
+    h->ring = nullptr;
+    ring_free(f);
     return TIS_OK;
 }
 

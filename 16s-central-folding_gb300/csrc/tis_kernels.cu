@@ -1131,6 +1131,69 @@ __global__ void k_shift(Dev d)
     }
 }
 
+// The five Energies-file values of replica r (E:6308-6312: E2_HB, E3_HB, E2_STACK,
+// E3_STACK of the last step, Rg of the RNA at the current positions) into out[0..4],
+// by threads tid = 0 .. nthr-1 (written by tid 0)
+template <class Bar>
+__device__ void energies_block(const Dev &d, int r, double *out, int tid, int nthr, Bar bar)
+{
+    const RepParams *R = d.rp + r;
+    __shared__ double s_red[3 * 32];
+    __shared__ double s_c[3];
+    double c[3] = {0, 0, 0};
+    for (int i = tid; i < R->nrna; i += nthr) {
+        c[0] += d.x[R->p0 + i];
+        c[1] += d.y[R->p0 + i];
+        c[2] += d.z[R->p0 + i];
+    }
+    block_sum_t<3>(c, s_red, tid, nthr, bar);
+    if (tid == 0)
+        for (int k = 0; k < 3; ++k) s_c[k] = c[k] / R->nrna;
+    bar();
+    double sq[1] = {0};
+    for (int i = tid; i < R->nrna; i += nthr) {
+        const double a = d.x[R->p0 + i] - s_c[0], b = d.y[R->p0 + i] - s_c[1], e = d.z[R->p0 + i] - s_c[2];
+        sq[0] += a * a + b * b + e * e;
+    }
+    block_sum_t<1>(sq, s_red, tid, nthr, bar);
+    if (tid == 0) {
+        const RepState *S = d.rs + r;
+        out[0] = S->e2hb;
+        out[1] = S->e3hb;
+        out[2] = S->e2st;
+        out[3] = S->e3st;
+        out[4] = sqrt(sq[0] / R->nrna);
+    }
+}
+
+// The frame of replica r after step klok into its slot of the frame ring (d.fr),
+// by threads tid = 0 .. nthr-1 of one block: positions, then the five energies,
+// then, after a system-scope fence, the step number that marks the slot complete.
+template <class Bar>
+__device__ void write_frame(const Dev &d, int r, long long klok, int tid, int nthr, Bar bar)
+{
+    const FrameRing &F = d.fr;
+    const RepParams *R = d.rp + r;
+    const long long slot = (klok / F.every) % F.depth;
+    const long long base = F.pk_base + R->pk0;
+    double *px = F.pos + slot * 3 * F.n_total;
+    for (int i = tid; i < R->n; i += nthr) {
+        px[base + i] = d.x[R->p0 + i];
+        px[F.n_total + base + i] = d.y[R->p0 + i];
+        px[2 * F.n_total + base + i] = d.z[R->p0 + i];
+    }
+    __shared__ double s_e5[5];
+    energies_block(d, r, s_e5, tid, nthr, bar);
+    bar();
+    if (tid < 5) F.en[(slot * F.R_total + F.rep_base + r) * 5 + tid] = s_e5[tid];
+    __threadfence_system();
+    bar();
+    if (tid == 0) {
+        __threadfence_system();
+        *(volatile long long *)(F.done + slot * F.R_total + F.rep_base + r) = klok;
+    }
+}
+
 // move_rigid_units for particle p of replica r (leap-frog, the recentring shift
 // sh, the ions' periodic wrap, the new fixed-point position, its force sum zeroed);
 // bits: max |x - x_old|^2 as bit pattern, err: flags
@@ -1216,6 +1279,11 @@ __global__ void __launch_bounds__(kBlock / kIntPer) k_integrate(Dev d)
     if (s_last) {
         __threadfence();
         control_step(d, r);
+        if (d.fr.every > 0) {  // a frame step: this block writes the replica's frame (all its blocks are done)
+            __syncthreads();
+            const long long kl = *(volatile long long *)&d.rs[r].klok;
+            if (kl % d.fr.every == 0) write_frame(d, r, kl, (int)threadIdx.x, (int)blockDim.x, CtaBar{});
+        }
     }
 }
 
@@ -1756,6 +1824,10 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_step_fused(Dev d, int step
         if (rank == 0) control_step(d, r);  // thread 0: check_shifts, the next step's LR gate
         cluster_barrier();
         lap(4);
+        if (d.fr.every > 0 && rank == 0) {  // a frame step: the first CTA writes the replica's frame
+            const long long kl = __ldcg(&S->klok);
+            if (kl % d.fr.every == 0) write_frame(d, r, kl, tid, kFusedThreads, CtaBar{});
+        }
         if (__ldcg(&S->rebuild)) {  // populate_lists (E:1546-1737)
             if (rank == 0) cells_block<D>(d, r);
             cluster_barrier();
@@ -1847,34 +1919,7 @@ __global__ void k_list_peaks(Dev d, int *out)
 // E2_HB, E3_HB, E2_STACK, E3_STACK and Rg of every replica (one block each)
 __global__ void k_energies(Dev d, double *out)
 {
-    const int r = blockIdx.x;
-    const RepParams *R = d.rp + r;
-    __shared__ double s_red[3 * 32];
-    double c[3] = {0, 0, 0};
-    for (int i = threadIdx.x; i < R->nrna; i += blockDim.x) {
-        c[0] += d.x[R->p0 + i];
-        c[1] += d.y[R->p0 + i];
-        c[2] += d.z[R->p0 + i];
-    }
-    block_sum<3>(c, s_red);
-    __shared__ double s_c[3];
-    if (threadIdx.x == 0)
-        for (int k = 0; k < 3; ++k) s_c[k] = c[k] / R->nrna;
-    __syncthreads();
-    double sq[1] = {0};
-    for (int i = threadIdx.x; i < R->nrna; i += blockDim.x) {
-        const double a = d.x[R->p0 + i] - s_c[0], b = d.y[R->p0 + i] - s_c[1], e = d.z[R->p0 + i] - s_c[2];
-        sq[0] += a * a + b * b + e * e;
-    }
-    block_sum<1>(sq, s_red);
-    if (threadIdx.x == 0) {
-        const RepState *S = d.rs + r;
-        out[5 * r] = S->e2hb;
-        out[5 * r + 1] = S->e3hb;
-        out[5 * r + 2] = S->e2st;
-        out[5 * r + 3] = S->e3st;
-        out[5 * r + 4] = sqrt(sq[0] / R->nrna);
-    }
+    energies_block(d, blockIdx.x, out + 5 * blockIdx.x, (int)threadIdx.x, (int)blockDim.x, CtaBar{});
 }
 
 }  // namespace

@@ -6,6 +6,19 @@
 
 namespace tis {
 
+// Frames written from inside the step (tis_frames_start): every `every` steps the
+// integrator's last block of each replica writes the replica's positions, its five
+// Energies-file values and then its step number into a ring of `depth` slots in
+// pinned, device-mapped host memory (every = 0: off).
+struct FrameRing {
+    double *pos;        // depth slots of 3 x n_total doubles: x, y, z of every replica end to end
+    double *en;         // depth slots of 5 x R_total doubles
+    long long *done;    // depth slots of R_total: the step whose frame the slot holds, per replica
+    long long n_total;  // particles of the handle (unpadded)
+    long long pk_base;  // the group's first value in the handle's packed arrays
+    int R_total, rep_base, every, depth;
+};
+
 // Device pointers of one handle (all replicas packed; see tis_engine.cu).
 struct Dev {
     int R, P, nblk, C;          // replicas, padded particles, particle blocks, cells
@@ -61,6 +74,7 @@ struct Dev {
     int *hb_rec;                // when not null: 1 per H-bond candidate formed after the step's Monte Carlo, else 0
     int lanes_sr, lanes_lr;     // threads per particle of the step's SR (1, 2, 4) and LR (2, 4, 8) pair launches
     unsigned long long *fprof;  // when not null: the fused step kernel's phase times, kFusedPhases per replica (ns)
+    FrameRing fr;               // frame output from inside the step (fr.every = 0: off)
 };
 constexpr int kFusedPhases = 8;  // forces, H-bond chain, shift, move, control, rebuild, steps with LR, rebuild steps
 

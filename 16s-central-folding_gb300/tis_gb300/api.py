@@ -106,6 +106,9 @@ def _declare(L):
         "tis_profile_stages": [vp, i64, dp],
         "tis_profile_in_step": [vp, i32, dp],
         "tis_profile_fused": [vp, i32, i32, dp],
+        "tis_frames_start": [vp, i32, i32, C.POINTER(vp)],
+        "tis_frames_read": [vp, i64, dp, dp, dp, dp],
+        "tis_frames_stop": [vp],
         "tis_get_forces": [vp, i32, dp],
         "tis_pair_lists_noalloc": [vp, vp, vp, vp, C.c_int32, dp, C.c_double, C.c_double, vp, i64, vp, i64, vp, vp],
         "tis_param_grad": [vp, dp],
@@ -140,7 +143,8 @@ EXPORTED = ["tis_last_error", "tis_load_params_default", "tis_system_load", "tis
             "tis_get_states", "tis_get_all_energies", "tis_write_frame", "tis_read_last_frame", "tis_ion_counts",
             "tis_param_grad", "tis_traj_grad", "tis_autotune", "tis_density_create", "tis_density_add",
             "tis_density_get", "tis_density_write_dx", "tis_density_destroy", "tis_write_psf", "tis_write_dcd", "tis_capture_graph",
-            "tis_write_cgpdb", "tis_checkpoint_save", "tis_checkpoint_load", "tis_profile_in_step", "tis_write_ninfo", "tis_profile_fused"]
+            "tis_write_cgpdb", "tis_checkpoint_save", "tis_checkpoint_load", "tis_profile_in_step", "tis_write_ninfo", "tis_profile_fused", "tis_frames_start",
+            "tis_frames_read", "tis_frames_stop"]
 
 
 def read_last_frame(path, n):
@@ -338,6 +342,27 @@ def run_params(**kw):
     for k, v in kw.items():
         setattr(p, k, v)
     return p
+
+
+class FrameRing:
+    """The frames a handle writes from inside its steps (tis_frames_*)."""
+
+    def __init__(self, engine, handle):
+        self.engine, self.h = engine, handle
+
+    def read(self, klok):
+        """{x, y, z: packed positions, energies: (replicas, 5)} of step klok."""
+        n = sum(self.engine.n)
+        out = {k: np.zeros(n) for k in ("x", "y", "z")}
+        en = np.zeros((len(self.engine.n), 5))
+        _check(lib().tis_frames_read(self.h, int(klok), _dp(out["x"]), _dp(out["y"]), _dp(out["z"]), _dp(en)))
+        out["energies"] = en
+        return out
+
+    def stop(self):
+        if self.h and self.h.value:
+            _check(lib().tis_frames_stop(self.h))
+            self.h = C.c_void_p()
 
 
 class Engine:
@@ -549,6 +574,13 @@ class Engine:
         ms = np.zeros(len(self.STAGES))
         _check(lib().tis_profile_in_step(self.h, steps, _dp(ms)))
         return dict(zip(self.STAGES, ms))
+
+    def frames_start(self, every, depth=2):
+        """Frames written from inside the step every `every` steps into a ring of
+        `depth` host slots (tis_frames_start); returns a FrameRing."""
+        out = C.c_void_p()
+        _check(lib().tis_frames_start(self.h, every, depth, C.byref(out)))
+        return FrameRing(self, out)
 
     def profile_fused(self, steps, ctas):
         """Phase times of the persistent fused step kernel (tis_profile_fused): dict of

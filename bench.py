@@ -513,7 +513,7 @@ def gpu_arm(args):
             per_stage[k] = {"in_step_us": 1000 * in_step[k], "alone_us_per_group": 1000 * stages[k] / groups,
                             "alg_bytes_per_launch": b,
                             "achieved_gbs": b / (in_step[k] * 1e-3) / 1e9 if in_step[k] > 0 else None}
-        dom = max(in_step, key=in_step.get)
+        dom = max(stages, key=stages.get)  # the most execution time of its own (stages timed alone)
         ach = per_stage[dom]["achieved_gbs"]
         traffic = NCU_DRAM_BYTES_PER_REPLICA.get(dom)
         roofline = {"bound": "latency", "axis": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
@@ -526,8 +526,9 @@ def gpu_arm(args):
                     "step": {"alg_bytes": sum(alg.values()),
                              "achieved_gbs": sum(alg.values()) / (ms_per_step * 1e-3) / 1e9,
                              "frac": sum(alg.values()) / (ms_per_step * 1e-3) / 1e9 / peak},
-                    "note": "kernel with the longest in-step launch (tis_profile_in_step: event pairs around each "
-                            "kernel inside the concurrently replayed graphs of all groups); one launch = one "
+                    "note": "kernel with the most execution time of its own (each stage timed alone, "
+                            "tis_profile_stages), timed inside the step (tis_profile_in_step: event pairs around "
+                            "each kernel inside the concurrently replayed graphs of all groups); one launch = one "
                             "replica group (1/" + str(groups) + " of the batch) for one step; achieved = its "
                             "algorithmic bytes / its in-step duration; bound: the kernels are latency bound "
                             "(ncu: long-scoreboard stalls on dependent gathers, low DRAM and FP32-pipe use), "
@@ -673,6 +674,21 @@ def _cfg_large(args, files, tmp, local, cfg1_sys):
             "precision": "mixed"}
 
 
+def profile_fused(args):
+    """The fused step kernel's phase times on the 64-replica workload (one replica
+    group), cluster sizes 1, 2 and 4: 20 steps to settle, then args.steps timed."""
+    from tis_gb300 import PREC_MIXED, Engine
+    with tempfile.TemporaryDirectory() as tmp:
+        systems = load_systems(make_inputs(tmp), replica_specs())
+        for ctas in (1, 2, 4):
+            e = Engine(systems, precision=PREC_MIXED, groups=1, fused_ctas=ctas)
+            e.populate_lists()
+            e.profile_fused(20, ctas)
+            ph = e.profile_fused(max(1, args.steps), ctas)
+            print(json.dumps({"fused_ctas": ctas, "replicas": len(systems), "steps": args.steps, **ph}), flush=True)
+            e.close()
+
+
 def files_for_cpu():
     d = tempfile.mkdtemp()
     return make_inputs(d)
@@ -695,10 +711,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the large-system (48,899 particles x 16 replicas) throughput line")
+    ap.add_argument("--profile-fused", action="store_true",
+                    help="instead of the benchmark: the persistent fused step kernel's phase times "
+                         "(tis_profile_fused) on the workload, one line per cluster size")
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="stop after the timed loop (no e2e, stage timing, plain path): for profiler runs")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_fused:
+        profile_fused(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gpu_arm(args)

@@ -281,6 +281,24 @@ int tis_density_write_dx(tis_density *g, const char *path);
  * grid return TIS_ERR_STATE; tis_density_destroy still frees the object. */
 int tis_density_destroy(tis_density *g);
 
+/* Frames written from inside the step (the reference writes its output every
+ * 10^6 steps from the run loop, E:6276-6376, stopping the run to do it).  After
+ * tis_frames_start, every `every` steps (step numbers, klok, that are multiples of
+ * it) the step's own integrator kernel writes each replica's positions, its five
+ * Energies-file values (E2_HB, E3_HB, E2_STACK, E3_STACK, Rg) and then the step
+ * number into a ring of `depth` (>= 2) slots of pinned host memory that the GPU
+ * writes directly; it adds no launch and no synchronisation to the run, graphs
+ * included.  tis_frames_read copies the frame of step klok (positions packed as
+ * tis_get_states packs them; energies 5 per replica) once every replica's part is
+ * complete, waiting for the handle's stream only when the frame is not yet
+ * written; TIS_ERR_STATE when the ring has overwritten it (read each frame before
+ * `depth` more frames are written) or the run never wrote it.  One ring per
+ * handle; tis_frames_stop (or tis_destroy) frees it. */
+typedef struct tis_frame_ring tis_frame_ring;
+int tis_frames_start(tis_handle *h, int32_t every, int32_t depth, tis_frame_ring **out);
+int tis_frames_read(tis_frame_ring *f, int64_t klok, double *x, double *y, double *z, double *energies);
+int tis_frames_stop(tis_frame_ring *f);
+
 /* Appends one frame of a replica to the reference's three output files (any may
  * be NULL): the Contacts file ("%+.3f " per tertiary stack energy, then a
  * newline, E:6290-6294), the Coordinates file (x, y, z, each as the reference's

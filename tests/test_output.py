@@ -326,3 +326,41 @@ def test_cli_without_inputs_or_gpu_fails_cleanly(tmp_path):
     r = subprocess.run([_build.RUN, "--steps", "10"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
     assert r.returncode == 1
     assert "tis_run:" in r.stderr and "error" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fused", [0, 2])
+def test_frames_written_from_inside_the_step(synth_dir, fused):
+    """tis_frames_*: the frames the step's kernels write into the host ring equal
+    the states and Energies-file values of the same run stopped at those steps
+    (Rg within rounding: its block sum runs over other threads); an overwritten,
+    an unreached and a non-frame step are refused; the ring changes no result."""
+    specs = [dict(seed=3 + 2 * k, n_mg=10 + 4 * k, n_cl=261 + 8 * k, n_k=317) for k in range(3)]
+    systems = [load(synth_dir["small"], "small", **sp) for sp in specs]
+    kw = dict(groups=2, graph_steps=40, fused_ctas=fused)
+    a = Engine(systems, **kw)
+    ring = a.frames_start(20, depth=3)
+    a.populate_lists()
+    a.step(100)  # frames at steps 20, 40, ..., 100; the ring keeps 60, 80, 100
+    frames = {k: ring.read(k) for k in (100, 80, 60)}
+    for bad in (40, 120, 30):  # overwritten, not reached, not a frame step
+        with pytest.raises(TisError):
+            ring.read(bad)
+    b = Engine(systems, **kw)
+    b.populate_lists()
+    done = 0
+    for k in (60, 80, 100):
+        b.step(k - done)
+        done = k
+        st = b.get_states(("x", "y", "z"))
+        en = b.all_energies()
+        for c in ("x", "y", "z"):
+            assert np.array_equal(frames[k][c], st[c]), (k, c)
+        assert np.array_equal(frames[k]["energies"][:, :4], en[:, :4]), k
+        np.testing.assert_allclose(frames[k]["energies"][:, 4], en[:, 4], rtol=1e-12)
+    fa, fb = a.get_states(), b.get_states()
+    for k in fa:
+        assert np.array_equal(fa[k], fb[k]), k
+    ring.stop()
+    a.step(20)  # detached: stepping goes on without a ring
+    a.sync()
