@@ -198,15 +198,15 @@ def stage_bytes(n, sr, lr, lr_frac, nreb, nrna, items, nhb, nrep):
 # `python bench.py --steps 40 --warmup 3 --no-extras --groups 8` with --clock-control
 # none, --kernel-name-base mangled and -k set to the kernel (None: no capture of a
 # stepping launch).  Scaled to the batch by the number of replicas.
-NCU_DRAM_BYTES_PER_REPLICA = {"pair_sr": 3.04e6 / 8, "pair_lr": None, "bonded": 1.24e6 / 8, "hbond": 0.48e6 / 8,
+NCU_DRAM_BYTES_PER_REPLICA = {"pair_sr": 3.04e6 / 8, "pair_lr": None, "bonded": 1.24e6 / 8, "hbond": 0.479e6 / 8,
                               "shift": 0.04e6 / 8, "integrate": 5.35e6 / 8, "cells": 0.03e6 / 8, "search": None}
 
 
 # FP32 (FMA) pipe and issue-slot use of each kernel from its committed ncu capture
-# (`--set full`, one launch over a group of 8 replicas): sm__pipe_fma_cycles_active
-# and sm__inst_issued (issue active) as fractions of their peaks.
-NCU_FMA_PIPE = {"pair_sr": 0.036}
-NCU_ISSUE_ACTIVE = {"pair_sr": 0.142}
+# (`--set full`, one launch over a group of 8 replicas; profiles/ncu_full_*.md):
+# sm__pipe_fma_cycles_active and smsp__issue_active as fractions of their peaks.
+NCU_FMA_PIPE = {"pair_sr": 0.0371, "hbond": 0.0621, "search": 0.0526}
+NCU_ISSUE_ACTIVE = {"pair_sr": 0.1469, "hbond": 0.1379, "search": 0.1452}
 
 
 def cpu_sample(files, specs, steps, workers):
@@ -609,7 +609,7 @@ def _cfg_adjoint(args, files, tmp, local, cfg1_sys):
     import numpy as np
 
     from tis_gb300 import PREC_MIXED, Engine, System
-    # cfg 3: dU/dtheta of the 15 force-field parameters over 10^4 saved frames of the
+    # cfg 3: dU/dtheta of the 16 force-field parameters over 10^4 saved frames of the
     # central system (64 replicas with independent seeds, a frame every 10 steps),
     # uploaded 64 frames at a time from host memory; and the gradient through 200-step
     # fixed-noise trajectories with a checkpoint every 10 steps, 16 replicas
@@ -649,7 +649,7 @@ def _cfg_adjoint(args, files, tmp, local, cfg1_sys):
     t_tg = time.perf_counter() - t0
     adj.close()
     return {
-        "workload": "central system (346-nt chain + 129 Mg / 2219 Cl / 2307 K), 15 parameters",
+        "workload": "central system (346-nt chain + 129 Mg / 2219 Cl / 2307 K), 16 parameters",
         "param_grad_frames": 64 * len(batches), "param_grad_frames_per_s": 64 * len(batches) / t_pg,
         "param_grad_note": "frames uploaded from host memory 64 at a time, lists rebuilt, dU/dtheta; wall clock",
         "traj_replicas": 16, "traj_steps": 200, "checkpoint_every": 10, "traj_grad_s": t_tg,
