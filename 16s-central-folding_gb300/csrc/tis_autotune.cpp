@@ -1,7 +1,9 @@
 // tis_autotune: the launch configuration chosen by measurement (no counterpart in
 // the reference, whose loops have no launch shape).  The knobs are the replica
-// groups (how many step graphs run concurrently), the steps per captured graph and
-// the threads per particle of the SR and LR pair launches; each is tuned in turn
+// groups (how many groups' step chains run concurrently), the steps per captured
+// graph, the threads per particle of the SR and LR pair launches, and whether the
+// steps run in the persistent fused step kernel (with 1, 2 or 4 CTAs per replica)
+// instead of the chain of separate kernels; each is tuned in turn
 // with the others held (coordinate descent), every trial a fresh handle timed with
 // CUDA events on its stream after a warm-up that includes the graph capture.
 #include <algorithm>
@@ -56,13 +58,15 @@ bool cache_lookup(const char *path, const std::string &key, tis_run_params *p, d
     while (fgets(line, sizeof line, f)) {
         const char *bar = strstr(line, " | ");
         if (!bar || std::string(line, bar - line) != key) continue;
-        int g, gs, ls, ll;
+        int g, gs, ls, ll, fc;
         double r;
-        if (sscanf(bar + 3, "groups=%d graph_steps=%d lanes_sr=%d lanes_lr=%d rate=%lf", &g, &gs, &ls, &ll, &r) == 5) {
+        if (sscanf(bar + 3, "groups=%d graph_steps=%d lanes_sr=%d lanes_lr=%d fused_ctas=%d rate=%lf", &g, &gs, &ls, &ll,
+                   &fc, &r) == 6) {
             p->groups = g;
             p->graph_steps = gs;
             p->lanes_sr = ls;
             p->lanes_lr = ll;
+            p->fused_ctas = fc;
             if (rate) *rate = r;
             found = true;  // the last line for the key wins
         }
@@ -146,13 +150,14 @@ extern "C" int tis_autotune(const tis_system *const *systems, int n_replicas, co
     tune(&tis_run_params::graph_steps, {25, 50, 100, 200});
     tune(&tis_run_params::lanes_sr, {1, 2, 4});
     tune(&tis_run_params::lanes_lr, {2, 4, 8});
+    tune(&tis_run_params::fused_ctas, {0, 1, 2, 4});
     *best = p;
     if (rate) *rate = cur;
     if (cache) {
         FILE *f = fopen(cache, "a");
         if (f) {
-            fprintf(f, "%s | groups=%d graph_steps=%d lanes_sr=%d lanes_lr=%d rate=%.1f\n", key.c_str(), p.groups,
-                    p.graph_steps, p.lanes_sr, p.lanes_lr, cur);
+            fprintf(f, "%s | groups=%d graph_steps=%d lanes_sr=%d lanes_lr=%d fused_ctas=%d rate=%.1f\n", key.c_str(),
+                    p.groups, p.graph_steps, p.lanes_sr, p.lanes_lr, p.fused_ctas, cur);
             fclose(f);
         }
     }

@@ -280,7 +280,7 @@ def autotune(systems, steps=300, cache=None, **params):
     rate = C.c_double()
     _check(lib().tis_autotune(arr, len(systems), C.byref(base), int(steps),
                               os.fsencode(cache) if cache else None, C.byref(best), C.byref(rate)))
-    return {k: getattr(best, k) for k in ("groups", "graph_steps", "lanes_sr", "lanes_lr")}, rate.value
+    return {k: getattr(best, k) for k in ("groups", "graph_steps", "lanes_sr", "lanes_lr", "fused_ctas")}, rate.value
 
 
 class Density:

@@ -368,8 +368,10 @@ int tis_get_launch_count(tis_handle *h, int64_t *n);
 int tis_rand_stream(uint64_t seed, uint64_t first, int64_t n, int32_t *out);
 
 /* Measured choice of the launch configuration (no counterpart in the reference):
- * replica groups, steps per captured graph and the threads per particle of the
- * SR and LR pair launches, tuned one after another (coordinate descent) by timing
+ * replica groups, steps per captured graph, the threads per particle of the SR
+ * and LR pair launches and the step path (fused_ctas: the separate kernels, or
+ * the persistent fused kernel with 1, 2 or 4 CTAs per replica), tuned one after
+ * another (coordinate descent) by timing
  * `steps` graph-replayed steps (0: 300) of the given replicas with CUDA events on
  * the handle's stream.  *best receives base with the chosen values and *rate (if
  * not NULL) the measured replica-steps/s.  When `cache` names a file, a line for

@@ -48,6 +48,7 @@ def test_autotune_chooses_and_caches(replicas, tmp_path):
     assert 1 <= best["groups"] <= len(replicas)
     assert best["graph_steps"] in (25, 50, 100, 200)
     assert best["lanes_sr"] in (1, 2, 4) and best["lanes_lr"] in (2, 4, 8)
+    assert best["fused_ctas"] in (0, 1, 2, 4)
     assert rate > 0
     with open(cache) as f:
         assert len(f.read().splitlines()) == 1
