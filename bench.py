@@ -54,6 +54,11 @@ GEN_SEED = 2000
 METRIC = "aggregate Langevin steps/s, batched mixed-prec vs plain GPU, force rel-err <=1e-5"
 UNIT = "replica-steps/s"
 GRAPH_STEPS = 100
+# Untimed steps between the first list build and the warm-up: the build makes every
+# replica's lists fresh at once, so their next rebuilds (every ~33 steps) come in
+# bursts for the first hundred or so steps; after these steps they are spread out as
+# in a long run, and a short timed window measures the run's steady state.
+EQUIL_STEPS = 1000
 
 
 def replica_specs(n=N_REPLICAS):
@@ -283,13 +288,15 @@ def reference_arm(args):
 
 
 def timed_steps(eng, K, W, flush, stream, world, clk_device):
-    """W warm-up steps, every graph the timed region replays captured, then exactly K
+    """EQUIL_STEPS untimed steps, W warm-up steps, every graph the timed region
+    replays captured, then exactly K
     steps timed with CUDA events on the handle's stream: the step graph (graph_steps
     long) replayed K // graph_steps times and a graph of the remaining steps once,
     L2 flushed before each replay.  Returns (ms, launches, chunks, clock summary)."""
     import torch
     gs = eng.params.graph_steps
     chunks = [gs] * (K // gs) + ([K % gs] if K % gs else [])
+    eng.step(EQUIL_STEPS)
     eng.step(W)
     for c in sorted(set(chunks), reverse=True):  # captures (the last one stays as the tail graph)
         eng.step(c)
@@ -464,6 +471,7 @@ def gpu_arm(args):
         groups = eng.params.groups or (3 * N_REPLICAS + 15) // 16
         launch = {"path": "CUDA graph replay (one graph holds every replica group's branch)",
                   "graph_steps": graph_steps, "graph_launches": len(chunks), "chunks": chunks,
+                  "equilibration_steps": EQUIL_STEPS,
                   "host_enqueue_ms": host_ms, "replica_groups": groups,
                   "lanes_sr": eng.params.lanes_sr or 1, "lanes_lr": eng.params.lanes_lr or 4,
                   "fused_ctas": eng.params.fused_ctas,
