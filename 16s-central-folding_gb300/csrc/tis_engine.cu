@@ -2379,7 +2379,8 @@ int tis_profile_in_step(tis_handle *h, int32_t steps, double *ms)
 // The persistent fused step kernel run for `steps` steps with its phase timer on:
 // out[0..5] the mean microseconds per step of its phases (forces, of them the H-bond
 // chain, shift, move, control, and the rebuild per step that rebuilds), out[6] the
-// share of steps with an LR refresh, out[7] rebuilds per step; means over replicas.
+// share of steps with an LR refresh, out[7] rebuilds per step, out[8..11] the H-bond
+// chain's restraint terms, Monte Carlo, forces and Gaussians; means over replicas.
 int tis_profile_fused(tis_handle *h, int32_t steps, int32_t ctas, double *out)
 {
     if (!h || steps < 1 || ctas < 1 || ctas > 8 || !out) return fail(TIS_ERR_ARG, "tis_profile_fused: bad argument");
@@ -2410,6 +2411,7 @@ int tis_profile_fused(tis_handle *h, int32_t steps, int32_t ctas, double *out)
     out[5] = acc[7] > 0 ? acc[5] / acc[7] * 1e-3 : 0.0;
     out[6] = acc[6] / reps / st;
     out[7] = acc[7] / reps / st;
+    for (int k = 8; k < 12; ++k) out[k] = acc[k] / reps / st * 1e-3;
     return TIS_OK;
 }
 

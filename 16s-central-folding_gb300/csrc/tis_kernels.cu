@@ -834,6 +834,13 @@ __global__ void __launch_bounds__(kTopoThreads) k_bonded_stack(Dev d, int mask, 
     topo_item<D, EN>(d, blockIdx.x * blockDim.x + threadIdx.x, mask, excl_in_list);
 }
 
+__device__ __forceinline__ unsigned long long global_ns_hb()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // ---------------------------------------------------------------------------
 // hydrogen bonds of one replica per block: energies, the valence-limited Monte
 // Carlo, forces; then (fused step) this step's Gaussians
@@ -900,6 +907,16 @@ __device__ __forceinline__ void hbond_block(const Dev &d, int r, int do_hb, int 
     double e2hb = 0, e3hb = 0;
     const int hb0 = R->hb0, nhb = R->hb1 - R->hb0, ca0 = R->ca0, nca = R->ca1 - R->ca0;
     const int warp = tid >> 5, nwarp = bd >> 5, lane = tid & 31;
+    // sub-phase times of the fused kernel's phase timer (tis_profile_fused), by tid 0
+    unsigned long long *prof = (d.fprof && tid == 0) ? d.fprof + (size_t)r * kFusedPhases : nullptr;
+    unsigned long long tlap = prof ? global_ns_hb() : 0ull;
+    auto lap = [&](int k) {
+        if (prof) {
+            const unsigned long long t = global_ns_hb();
+            atomicAdd(prof + k, t - tlap);
+            tlap = t;
+        }
+    };
     HbWork w;
     const int nact = do_hb ? S->n_active : 0;
     bar();
@@ -974,6 +991,7 @@ __device__ __forceinline__ void hbond_block(const Dev &d, int r, int do_hb, int 
             w.code[kl] = (w.br[3 * kl] + 1) + 3 * (w.br[3 * kl + 1] + 1) + 9 * (w.br[3 * kl + 2] + 1);
         }
         bar();
+        lap(8);
         if (tid < 32) {  // valence-limited Monte Carlo (E:2239-2315), one warp
             const unsigned lt = (1u << lane) - 1u;
             unsigned long long ctr = s_ctr, vbase = ctr;
@@ -1053,6 +1071,7 @@ __device__ __forceinline__ void hbond_block(const Dev &d, int r, int do_hb, int 
             if (lane == 0) s_ctr = ctr;
         }
         bar();
+        lap(9);
         // forces of the bonds still formed: warp task (chunk of 32 live bonds, term 0..5)
         for (int task = warp; task < 6 * nchunk; task += nwarp) {
             const int s = task % 6, t = (task / 6) * 32 + lane;
@@ -1071,9 +1090,14 @@ __device__ __forceinline__ void hbond_block(const Dev &d, int r, int do_hb, int 
     }
     if (do_hb && d.hb_rec)  // the bonds formed after the Monte Carlo (status 0; 1 broken, -1 out of range)
         for (int i = tid; i < nhb; i += bd) d.hb_rec[hb0 + i] = w.st[i] == 0 ? 1 : 0;
+    lap(10);
     // ---- full_forces: the step's Gaussians follow the Monte Carlo draws ----
     const unsigned long long c1 = s_ctr;
     if (make_noise) gen_noise<D>(d, r, c1, tid, bd);
+    if (d.fprof) {  // the Gaussians of every thread are done (timer runs only)
+        bar();
+        lap(11);
+    }
 
     double v[2] = {e2hb, e3hb};
     block_sum_t<2>(v, s_red, tid, bd, bar);
@@ -1768,7 +1792,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_step_fused(Dev d, int step
     int err = 0;
     // phase times (tis_profile_fused): the first thread of the cluster's first CTA
     const bool timer = d.fprof && rank == 0 && tid == 0;
-    unsigned long long ph[kFusedPhases] = {0, 0, 0, 0, 0, 0, 0, 0}, t0 = timer ? global_ns() : 0ull, t1;
+    unsigned long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0}, t0 = timer ? global_ns() : 0ull, t1;
     auto lap = [&](int k) {
         if (timer) {
             t1 = global_ns();
@@ -1840,7 +1864,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_step_fused(Dev d, int step
     }
     if (err) atomicOr(&S->err, err);
     if (timer)
-        for (int k = 0; k < kFusedPhases; ++k) atomicAdd(d.fprof + (size_t)r * kFusedPhases + k, ph[k]);
+        for (int k = 0; k < 8; ++k) atomicAdd(d.fprof + (size_t)r * kFusedPhases + k, ph[k]);
 }
 
 // radius_of_gyration (E:2844-2876) of the RNA beads of one replica

@@ -76,7 +76,8 @@ struct Dev {
     unsigned long long *fprof;  // when not null: the fused step kernel's phase times, kFusedPhases per replica (ns)
     FrameRing fr;               // frame output from inside the step (fr.every = 0: off)
 };
-constexpr int kFusedPhases = 8;  // forces, H-bond chain, shift, move, control, rebuild, steps with LR, rebuild steps
+constexpr int kFusedPhases = 12;  // forces, H-bond chain, shift, move, control, rebuild, steps with LR, rebuild steps,
+                                  // and the H-bond chain's restraint terms, Monte Carlo, forces, Gaussians
 
 // Adjoint work of one handle (tis_adjoint.cu).  Arrays of 3P or 9P values are
 // component-major (c * P + p) like the state arrays.

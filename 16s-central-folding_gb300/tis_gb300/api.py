@@ -585,10 +585,11 @@ class Engine:
     def profile_fused(self, steps, ctas):
         """Phase times of the persistent fused step kernel (tis_profile_fused): dict of
         microseconds per step and the LR and rebuild rates; advances every replica."""
-        out = np.zeros(8)
+        out = np.zeros(12)
         _check(lib().tis_profile_fused(self.h, steps, ctas, _dp(out)))
         names = ["forces_us", "hbond_chain_us", "shift_us", "move_us", "control_us", "rebuild_us_per_rebuild",
-                 "lr_share", "rebuilds_per_step"]
+                 "lr_share", "rebuilds_per_step", "hbond_terms_us", "hbond_mc_us", "hbond_forces_us",
+                 "hbond_gaussians_us"]
         return dict(zip(names, out.tolist()))
 
     def launches(self):

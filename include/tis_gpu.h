@@ -354,8 +354,9 @@ int tis_profile_in_step(tis_handle *h, int32_t steps, double *ms);
  * force phase, of the H-bond chain inside it (terms, Monte Carlo, Gaussians),
  * the recentring shift, the integration, the control step, and the list rebuild
  * per step that rebuilds; out[6] = share of steps that refresh the LR force,
- * out[7] = list rebuilds per step; means over the replicas.  Advances every
- * replica by `steps` steps. */
+ * out[7] = list rebuilds per step; out[8..11] = microseconds per step of the
+ * H-bond chain's restraint terms, Monte Carlo, forces and Gaussians (out has 12
+ * values); means over the replicas.  Advances every replica by `steps` steps. */
 int tis_profile_fused(tis_handle *h, int32_t steps, int32_t ctas, double *out);
 
 /* Kernel launches enqueued by tis_step since the handle was created. */
