@@ -196,6 +196,7 @@ void drop_graphs(Group *h)
 int capture_steps(Group *h, int steps, cudaGraphExec_t *out)
 {
     cudaGraph_t g;
+    TIS_CUDA(cudaStreamSynchronize(h->stream));  // no graph of the group in flight during capture and upload
     TIS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < steps; ++s) enqueue_step(h);
     TIS_CUDA(cudaStreamEndCapture(h->stream, &g));
@@ -221,6 +222,7 @@ int grow_lists(Group *h, int cap_sr, int cap_lr)
     int rc;
     if ((rc = dalloc(h->owned, &h->dev.nbr_sr, (size_t)cap_sr * h->P))) return rc;
     if ((rc = dalloc(h->owned, &h->dev.nbr_lr, (size_t)cap_lr * h->P))) return rc;
+    TIS_CUDA(cudaDeviceSynchronize());  // the memsets (legacy stream) land before the next build
     h->dev.cap_sr = cap_sr;
     h->dev.cap_lr = cap_lr;
     drop_graphs(h);
@@ -842,6 +844,9 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
     if (cudaMallocHost((void **)&h->h_rs, sizeof(tis::RepState) * h->R) != cudaSuccess ||
         cudaMallocHost((void **)&h->h_peaks, 2 * sizeof(int)) != cudaSuccess)
         return bail(fail(TIS_ERR_NOMEM, "cudaMallocHost failed"));
+    // the allocations' memsets and the pageable uploads above run on the legacy
+    // default stream, which the group's non-blocking streams do not wait for
+    if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(TIS_ERR_CUDA, "device synchronisation failed"));
     tis::launch_quantize(h->dev, h->stream);
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess)
         return bail(fail(TIS_ERR_CUDA, "quantisation kernel failed"));
@@ -889,31 +894,6 @@ static int grp_get_state(Group *h, int r, double *x, double *y, double *z, doubl
     for (int c = 0; c < 9; ++c)
         if (dst[c]) TIS_CUDA(cudaMemcpyAsync(dst[c], src[c] + hr.p0, sizeof(double) * hr.n, cudaMemcpyDeviceToHost, h->stream));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
-    return TIS_OK;
-}
-
-// the group's part of packed host arrays: nine arrays, the group's values from offset `off`
-static int grp_set_states(Group *h, const double *const *src, int64_t off)
-{
-    for (int c = 0; c < 9; ++c)
-        TIS_CUDA(cudaMemcpyAsync(h->stage + (size_t)c * h->npk, src[c] + off, sizeof(double) * h->npk,
-                                 cudaMemcpyHostToDevice, h->stream));
-    tis::launch_put_state(h->dev, h->stream, h->stage, h->npk);
-    TIS_CUDA(cudaGetLastError());
-    h->lists_built = false;
-    return TIS_OK;
-}
-
-static int grp_get_states(Group *h, double *const *dst, int64_t off)
-{
-    unsigned mask = 0;
-    for (int c = 0; c < 9; ++c) mask |= dst[c] ? (1u << c) : 0u;
-    tis::launch_get_state(h->dev, h->stream, h->stage, h->npk, mask);
-    TIS_CUDA(cudaGetLastError());
-    for (int c = 0; c < 9; ++c)
-        if (dst[c])
-            TIS_CUDA(cudaMemcpyAsync(dst[c] + off, h->stage + (size_t)c * h->npk, sizeof(double) * h->npk,
-                                     cudaMemcpyDeviceToHost, h->stream));
     return TIS_OK;
 }
 
@@ -1365,6 +1345,7 @@ static int grp_step(Group *h, int64_t n)
         // with the same remainder (a caller stepping by a fixed count below the graph
         // length replays it every call)
         if (!h->tail || h->tail_steps != left) {
+            TIS_CUDA(cudaStreamSynchronize(h->stream));  // the old remainder graph may still run
             if (h->tail) cudaGraphExecDestroy(h->tail);
             h->tail = nullptr;
             h->tail_steps = 0;
@@ -1509,9 +1490,13 @@ struct tis_handle {
     };
     StepGraph full, tail;
     tis_frame_ring *ring = nullptr;  // frames written from inside the step (tis_frames_start)
+    int64_t npk = 0;                 // particles of all replicas (unpadded)
+    double *stage = nullptr;         // nine packed state arrays of npk values (tis_set_states / tis_get_states)
 
     ~tis_handle()
     {
+        if (stream) cudaStreamSynchronize(stream);  // graphs launched on it may still use the groups' memory
+        if (stage) cudaFree(stage);
         for (StepGraph *sg : {&full, &tail})
             if (sg->exec) cudaGraphExecDestroy(sg->exec);
         for (Group *g : groups) delete g;
@@ -1634,7 +1619,12 @@ int tis_create(const tis_system *const *systems, int n_replicas, const tis_run_p
             h->grp_of.push_back(k);
             h->loc_of.push_back(r - first);
         }
+        h->npk += g->npk;
     }
+    // one staging buffer for the whole handle: a state upload or read-back is nine
+    // copies, whatever the number of groups
+    if (cudaMalloc((void **)&h->stage, sizeof(double) * 9 * (size_t)h->npk) != cudaSuccess)
+        return bail(fail(TIS_ERR_CUDA, "cudaMalloc of the state staging buffer failed"));
     *out = h;
     return TIS_OK;
 }
@@ -1687,11 +1677,16 @@ int tis_set_states(tis_handle *h, const double *x, const double *y, const double
     const double *src[9] = {x, y, z, xo, yo, zo, vx, vy, vz};
     for (int c = 0; c < 9; ++c)
         if (!src[c]) return fail(TIS_ERR_ARG, "tis_set_states: null array %d", c);
+    const size_t n = (size_t)h->npk;
+    for (int c = 0; c < 9; ++c)
+        TIS_CUDA(cudaMemcpyAsync(h->stage + c * n, src[c], sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
     int64_t off = 0;
-    int rc = each_group(h, [&](Group *g) {
-        const int r = grp_set_states(g, src, off);
+    int rc = each_group(h, [&](Group *g) -> int {  // each group unpacks its slice (stride: the handle's npk)
+        tis::launch_put_state(g->dev, g->stream, h->stage + off, (int)n);
         off += g->npk;
-        return r;
+        g->lists_built = false;
+        TIS_CUDA(cudaGetLastError());
+        return TIS_OK;
     });
     if (rc) return rc;
     TIS_CUDA(cudaStreamSynchronize(h->stream));
@@ -1703,13 +1698,19 @@ int tis_get_states(tis_handle *h, double *x, double *y, double *z, double *xo, d
 {
     if (!h) return fail(TIS_ERR_ARG, "null handle");
     double *dst[9] = {x, y, z, xo, yo, zo, vx, vy, vz};
+    unsigned mask = 0;
+    for (int c = 0; c < 9; ++c) mask |= dst[c] ? (1u << c) : 0u;
+    const size_t n = (size_t)h->npk;
     int64_t off = 0;
-    int rc = each_group(h, [&](Group *g) {
-        const int r = grp_get_states(g, dst, off);
+    int rc = each_group(h, [&](Group *g) -> int {  // each group packs its slice into the handle's staging buffer
+        tis::launch_get_state(g->dev, g->stream, h->stage + off, (int)n, mask);
         off += g->npk;
-        return r;
+        TIS_CUDA(cudaGetLastError());
+        return TIS_OK;
     });
     if (rc) return rc;
+    for (int c = 0; c < 9; ++c)
+        if (dst[c]) TIS_CUDA(cudaMemcpyAsync(dst[c], h->stage + c * n, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
     TIS_CUDA(cudaStreamSynchronize(h->stream));
     return TIS_OK;
 }
@@ -1858,6 +1859,7 @@ int tis_density_create(tis_handle *h, int r, int kind, const double lo[3], doubl
             (e = cudaMemcpy(d->d_ref, fit_ref, sizeof(double) * 3 * n_fit, cudaMemcpyHostToDevice)) != cudaSuccess)
             return bail(e);
     }
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(e);  // memsets and uploads (legacy stream) done
     h->densities.push_back(d);
     *out = d;
     return TIS_OK;
@@ -2129,6 +2131,9 @@ int tis_checkpoint_load(tis_handle *h, const char *path)
             if (st[k].second) TIS_CUDA(cudaMemcpy(st[k].first, D.arrays[k].data(), st[k].second, cudaMemcpyHostToDevice));
         g->lists_built = D.gh[4] != 0;
     }
+    // pageable uploads may still be in flight when cudaMemcpy returns; the next
+    // step runs on non-blocking streams
+    TIS_CUDA(cudaDeviceSynchronize());
     return TIS_OK;
 }
 
@@ -2189,6 +2194,9 @@ int enqueue_fused(Group *g, int64_t steps, int ctas)
 // graph: the fork, each group's steps on its own streams, the join
 int capture_handle(tis_handle *h, int steps, tis_handle::StepGraph *sg)
 {
+    // no graph of the handle is in flight while one is replaced, captured,
+    // instantiated and uploaded
+    TIS_CUDA(cudaStreamSynchronize(h->stream));
     if (sg->exec) cudaGraphExecDestroy(sg->exec);
     sg->exec = nullptr;
     sg->steps = 0;
