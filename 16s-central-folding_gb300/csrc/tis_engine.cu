@@ -251,7 +251,11 @@ int populate_launch(Group *h)
 {
     tis::launch_clear_err(h->dev, h->stream);
     tis::launch_force_all_rebuild(h->dev, h->stream);
-    tis::launch_rebuild(h->dev, h->stream);
+    // every replica rebuilds: the search gets six blocks of four warps per SM instead
+    // of the step's one (a warp per particle is latency-bound; more warps in flight)
+    tis::Dev full = h->dev;
+    full.search_warps = h->dev.sm_count * 24;
+    tis::launch_rebuild(full, h->stream);
     TIS_CUDA(cudaMemsetAsync(h->d_peaks, 0, 2 * sizeof(int), h->stream));
     tis::launch_list_peaks(h->dev, h->stream, h->d_peaks);
     TIS_CUDA(cudaGetLastError());
@@ -1537,6 +1541,28 @@ int each_group(tis_handle *h, F fn)
     return rc ? rc : rj;
 }
 
+// populate_lists for the given groups, ordered after the work queued on the
+// handle's stream: every group's build is launched before any is checked, so the
+// builds overlap; groups whose lists had to grow build again
+int populate_groups(tis_handle *h, std::vector<Group *> pending)
+{
+    int rc = fork_groups(h);
+    if (rc) return rc;
+    for (int attempt = 0; !pending.empty(); ++attempt) {
+        for (Group *g : pending)
+            if ((rc = populate_launch(g))) return rc;
+        std::vector<Group *> again_list;
+        for (Group *g : pending) {
+            TIS_CUDA(cudaStreamSynchronize(g->stream));
+            bool again = false;
+            if ((rc = populate_check(g, attempt, &again))) return rc;
+            if (again) again_list.push_back(g);
+        }
+        pending.swap(again_list);
+    }
+    return join_groups(h);
+}
+
 // the group and its local index for replica r, after validating r
 int locate(tis_handle *h, int r, Group **g, int *loc)
 {
@@ -1732,24 +1758,8 @@ int tis_get_all_energies(tis_handle *h, double *out)
 int tis_populate_lists(tis_handle *h)
 {
     Range range("tis_populate_lists");
-    // every group's build is launched before any is checked, so the builds overlap
     if (!h) return fail(TIS_ERR_ARG, "null handle");
-    int rc = fork_groups(h);
-    if (rc) return rc;
-    std::vector<Group *> pending(h->groups);
-    for (int attempt = 0; !pending.empty(); ++attempt) {
-        for (Group *g : pending)
-            if ((rc = populate_launch(g))) return rc;
-        std::vector<Group *> again_list;
-        for (Group *g : pending) {
-            TIS_CUDA(cudaStreamSynchronize(g->stream));
-            bool again = false;
-            if ((rc = populate_check(g, attempt, &again))) return rc;
-            if (again) again_list.push_back(g);
-        }
-        pending.swap(again_list);
-    }
-    return join_groups(h);
+    return populate_groups(h, h->groups);
 }
 
 int tis_get_cells(tis_handle *h, int r, int32_t *cell, int32_t *dims)
@@ -2231,10 +2241,10 @@ int capture_handle(tis_handle *h, int steps, tis_handle::StepGraph *sg)
 // queued on the handle's stream
 int build_missing_lists(tis_handle *h)
 {
-    bool need = false;
-    for (Group *g : h->groups) need = need || !g->lists_built;
-    if (!need) return TIS_OK;
-    return each_group(h, [](Group *g) { return g->lists_built ? TIS_OK : populate(g); });
+    std::vector<Group *> need;
+    for (Group *g : h->groups)
+        if (!g->lists_built) need.push_back(g);
+    return need.empty() ? TIS_OK : populate_groups(h, need);
 }
 
 // the handle's graph of `steps` steps in slot sg, captured again when its length
