@@ -210,8 +210,8 @@ NCU_DRAM_BYTES_PER_REPLICA = {"pair_sr": 3.04e6 / 8, "pair_lr": None, "bonded": 
 # FP32 (FMA) pipe and issue-slot use of each kernel from its committed ncu capture
 # (`--set full`, one launch over a group of 8 replicas; profiles/ncu_full_*.md):
 # sm__pipe_fma_cycles_active and smsp__issue_active as fractions of their peaks.
-NCU_FMA_PIPE = {"pair_sr": 0.0371, "hbond": 0.0621, "search": 0.0526}
-NCU_ISSUE_ACTIVE = {"pair_sr": 0.1469, "hbond": 0.1379, "search": 0.1452}
+NCU_FMA_PIPE = {"pair_sr": 0.0371, "hbond": 0.0621, "search": 0.0526, "bonded": 0.0632}
+NCU_ISSUE_ACTIVE = {"pair_sr": 0.1469, "hbond": 0.1379, "search": 0.1452, "bonded": 0.1523}
 
 
 def cpu_sample(files, specs, steps, workers):
