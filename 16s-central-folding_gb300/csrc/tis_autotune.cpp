@@ -5,7 +5,10 @@
 // steps run in the persistent fused step kernel (with 1, 2 or 4 CTAs per replica)
 // instead of the chain of separate kernels; each is tuned in turn
 // with the others held (coordinate descent), every trial a fresh handle timed with
-// CUDA events on its stream after a warm-up that includes the graph capture.
+// CUDA events on its stream after a warm-up that includes the graph captures.  The
+// configuration is tuned for calls of `steps` steps: a trial times as many such
+// calls as make up at least kTrialSteps steps, so that a caller stepping a few steps
+// per call (one graph launch each) gets the shape that is fastest for that.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -20,6 +23,8 @@ using tis::fail;
 
 namespace {
 
+constexpr int64_t kTrialSteps = 1000;  // steps timed per trial at least
+
 double scalar(const tis_system *s, const char *name, double def)
 {
     int dt = 0;
@@ -32,7 +37,7 @@ double scalar(const tis_system *s, const char *name, double def)
 }
 
 // the workload's key in the cache file
-std::string key_of(const tis_system *const *systems, int n, const tis_run_params &p)
+std::string key_of(const tis_system *const *systems, int n, const tis_run_params &p, int64_t steps)
 {
     double particles = 0;
     for (int r = 0; r < n; ++r) particles += scalar(systems[r], "n_particles", 0);
@@ -43,9 +48,9 @@ std::string key_of(const tis_system *const *systems, int n, const tis_run_params
         if (c == ' ') c = '_';
     char buf[512];
     snprintf(buf, sizeof buf, "replicas=%d particles=%.0f box=%.3f rc=%.3f precision=%d noise=%d sr=%.3f skin=%.3f "
-                              "lr_interval=%d full_lists=%d device=%s",
+                              "lr_interval=%d full_lists=%d steps_per_call=%lld device=%s",
              n, particles, scalar(systems[0], "box", 0), scalar(systems[0], "rc", 0), p.precision, p.noise, p.sr,
-             p.skin, p.lr_interval, p.full_lists, dev.c_str());
+             p.skin, p.lr_interval, p.full_lists, (long long)steps, dev.c_str());
     return buf;
 }
 
@@ -75,7 +80,8 @@ bool cache_lookup(const char *path, const std::string &key, tis_run_params *p, d
     return found;
 }
 
-// replica-steps/s of one configuration, or a negative value if it failed
+// replica-steps/s of one configuration in calls of `steps` steps, or a negative
+// value if it failed
 double measure(const tis_system *const *systems, int n, const tis_run_params &p, int64_t steps)
 {
     tis_handle *h = nullptr;
@@ -84,17 +90,20 @@ double measure(const tis_system *const *systems, int n, const tis_run_params &p,
     void *sp = nullptr;
     int nr = 0, dev = 0;
     cudaEvent_t a = nullptr, b = nullptr;
+    const int64_t calls = std::max<int64_t>(1, (kTrialSteps + steps - 1) / steps);
+    // the warm-up captures the graphs the timed calls replay (a call's remainder too)
     if (tis_get_info(h, &nr, &dev, &sp) == TIS_OK && tis_populate_lists(h) == TIS_OK &&
-        tis_step(h, p.graph_steps + 10) == TIS_OK && tis_sync(h) == TIS_OK &&
-        cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess) {
+        tis_step(h, p.graph_steps + 10) == TIS_OK && (steps % p.graph_steps == 0 || tis_step(h, steps) == TIS_OK) &&
+        tis_sync(h) == TIS_OK && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess) {
         cudaStream_t s = (cudaStream_t)sp;
         cudaEventRecord(a, s);
-        const int rc = tis_step(h, steps);
+        int rc = TIS_OK;
+        for (int64_t c = 0; c < calls && rc == TIS_OK; ++c) rc = tis_step(h, steps);
         cudaEventRecord(b, s);
         float ms = 0;
         if (rc == TIS_OK && tis_sync(h) == TIS_OK && cudaEventSynchronize(b) == cudaSuccess &&
             cudaEventElapsedTime(&ms, a, b) == cudaSuccess && ms > 0)
-            rate = (double)n * (double)steps / (ms * 1e-3);
+            rate = (double)n * (double)(steps * calls) / (ms * 1e-3);
     }
     if (a) cudaEventDestroy(a);
     if (b) cudaEventDestroy(b);
@@ -117,7 +126,7 @@ extern "C" int tis_autotune(const tis_system *const *systems, int n_replicas, co
     if (p.groups <= 0) p.groups = std::min(n_replicas, (3 * n_replicas + 15) / 16);
     if (p.lanes_sr == 0) p.lanes_sr = 1;
     if (p.lanes_lr == 0) p.lanes_lr = 4;
-    const std::string key = key_of(systems, n_replicas, p);
+    const std::string key = key_of(systems, n_replicas, p, steps);
     if (cache && cache_lookup(cache, key, &p, rate)) {
         *best = p;
         return TIS_OK;
@@ -150,6 +159,7 @@ extern "C" int tis_autotune(const tis_system *const *systems, int n_replicas, co
     tune(&tis_run_params::graph_steps, {25, 50, 100, 200});
     tune(&tis_run_params::lanes_sr, {1, 2, 4});
     tune(&tis_run_params::lanes_lr, {2, 4, 8});
+    tune(&tis_run_params::groups, groups);  // again: the best grouping moves with the launch shapes
     tune(&tis_run_params::fused_ctas, {0, 1, 2, 4});
     *best = p;
     if (rate) *rate = cur;

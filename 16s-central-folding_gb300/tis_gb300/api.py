@@ -272,8 +272,9 @@ class System:
 
 
 def autotune(systems, steps=300, cache=None, **params):
-    """Measured launch configuration for these replicas: (dict of the chosen
-    groups, graph_steps, lanes_sr, lanes_lr, replica-steps/s)."""
+    """Measured launch configuration for these replicas stepped `steps` steps per
+    call: (dict of the chosen groups, graph_steps, lanes_sr, lanes_lr, fused_ctas;
+    replica-steps/s)."""
     arr = (C.c_void_p * len(systems))(*[s.h.value for s in systems])
     base = run_params(**params)
     best = RunParams()

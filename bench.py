@@ -437,8 +437,8 @@ def gpu_arm(args):
         specs = rank_replica_specs(rank)  # replicas only: every rank its own batch
         systems = load_systems(files, specs)
         # the launch configuration: measured by tis_autotune (replica groups, steps per
-        # graph, threads per particle of the pair launches; 1000 steps per trial), or
-        # fixed by --groups
+        # graph, threads per particle of the pair launches, step path) for calls of the
+        # timed step count, each trial at least 1000 steps; or fixed by --groups
         tune = {"groups": args.groups, "graph_steps": args.graph_steps, "lanes_sr": args.lanes_sr,
                 "lanes_lr": args.lanes_lr, "fused_ctas": args.fused_ctas}
         tune_s = None
@@ -446,8 +446,8 @@ def gpu_arm(args):
         if args.groups == 0:
             t0 = time.perf_counter()
             try:
-                tune, _ = autotune(systems, steps=1000, precision=PREC_MIXED, device=local)
-                tune_note = "tis_autotune (1000 steps per trial)"
+                tune, _ = autotune(systems, steps=max(1, args.steps), precision=PREC_MIXED, device=local)
+                tune_note = f"tis_autotune (calls of {max(1, args.steps)} steps, at least 1000 steps per trial)"
             except Exception as exc:  # the library's defaults if tuning fails
                 tune = {"groups": 0, "graph_steps": GRAPH_STEPS, "lanes_sr": 1, "lanes_lr": 4}
                 tune_note = f"library defaults (tis_autotune failed: {exc})"

@@ -372,12 +372,13 @@ int tis_rand_stream(uint64_t seed, uint64_t first, int64_t n, int32_t *out);
  * replica groups, steps per captured graph, the threads per particle of the SR
  * and LR pair launches and the step path (fused_ctas: the separate kernels, or
  * the persistent fused kernel with 1, 2 or 4 CTAs per replica), tuned one after
- * another (coordinate descent) by timing
- * `steps` graph-replayed steps (0: 300) of the given replicas with CUDA events on
- * the handle's stream.  *best receives base with the chosen values and *rate (if
+ * another (coordinate descent), for calls of `steps` steps (0: 300): each trial
+ * times, with CUDA events on the handle's stream, as many tis_step(steps) calls of
+ * the given replicas as make up at least 1000 steps, after a warm-up that captures
+ * the graphs they replay.  *best receives base with the chosen values and *rate (if
  * not NULL) the measured replica-steps/s.  When `cache` names a file, a line for
- * the same workload (replicas, particles, box, cutoff, precision, device) is
- * reused without trials, and a new result is appended. */
+ * the same workload (replicas, particles, box, cutoff, precision, steps per call,
+ * device) is reused without trials, and a new result is appended. */
 int tis_autotune(const tis_system *const *systems, int n_replicas, const tis_run_params *base, int64_t steps,
                  const char *cache, tis_run_params *best, double *rate);
 
