@@ -154,7 +154,9 @@ int main(int argc, char **argv)
     }
     if (tune) {
         tis_run_params best;
-        if (report(tis_autotune(sys.data(), replicas, &rp, 1000, "tis_tune.txt", &best, nullptr), "tune")) return 1;
+        // tuned for the loop's calls: one frame interval per tis_step, at most 1000 steps a trial call
+        const int64_t per_call = every < 1000 ? every : 1000;
+        if (report(tis_autotune(sys.data(), replicas, &rp, per_call, "tis_tune.txt", &best, nullptr), "tune")) return 1;
         rp = best;
     }
     tis_handle *h = nullptr;
