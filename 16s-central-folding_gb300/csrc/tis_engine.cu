@@ -126,7 +126,7 @@ struct Group {
     long long launches = 0;
     double *d_scalar = nullptr;
     int npk = 0;              // particles of the group's replicas (unpadded)
-    double *stage = nullptr;  // nine packed state arrays of npk values (tis_set_states / tis_get_states)
+    double *stage = nullptr;  // nine packed arrays of npk values (tis_traj_grad's seeds and state adjoints)
     double *d_e5 = nullptr;   // five energies per replica (tis_get_all_energies)
     tis::RepState *h_rs = nullptr;  // pinned host copy of the replicas' state (list build checks)
     int *h_peaks = nullptr;         // pinned: largest SR and LR neighbour counts of the last list build
