@@ -1465,13 +1465,6 @@ static int grp_replica_size(Group *h, int r, int *n_particles)
     return TIS_OK;
 }
 
-static int grp_get_launch_count(Group *h, int64_t *n)
-{
-    if (!h || !n) return fail(TIS_ERR_ARG, "bad argument");
-    *n = h->launches;
-    return TIS_OK;
-}
-
 
 // The public handle: replicas split into groups of consecutive replicas.  Each
 // group's work is forked from and joined back into the handle's stream, so the

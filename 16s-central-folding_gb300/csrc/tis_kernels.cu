@@ -96,8 +96,6 @@ __device__ inline Pos<true> make_pos<true>(const Dev &d, const RepParams *)
     return Pos<true>{d.x, d.y, d.z};
 }
 
-__device__ inline float acos_(float v) { return acosf(v); }
-__device__ inline double acos_(double v) { return acos(v); }
 __device__ inline float atan2_(float a, float b) { return atan2f(a, b); }
 __device__ inline double atan2_(double a, double b) { return atan2(a, b); }
 __device__ inline float exp_(float v) { return expf(v); }
