@@ -157,6 +157,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+def fp32_roofline(device, clocks, entries_per_launch, launch_ms):
+    """The SR pair kernel against the FP32 roofline: its algorithmic FLOPs per launch
+    (FLOP_PER_SR_ENTRY per list entry) over its in-step duration, and the GPU's FP32
+    peak at the SM clock sampled during the timed region (SMs x 128 lanes x 2)."""
+    import torch
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+    flops = FLOP_PER_SR_ENTRY * entries_per_launch
+    ach = flops / (launch_ms * 1e-3) / 1e12 if launch_ms > 0 else None
+    return {"kernel": "pair_sr", "alg_flops_per_launch": flops, "achieved_tflops": ach, "peak_tflops": peak,
+            "unit": "TFLOP/s", "frac": ach / peak if ach is not None else None,
+            "ncu_fma_pipe_frac": NCU_FMA_PIPE.get("pair_sr"),
+            "model": f"{FLOP_PER_SR_ENTRY} FLOP per SR list entry; peak at the sampled SM clock"}
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -205,6 +221,13 @@ def stage_bytes(n, sr, lr, lr_frac, nreb, nrna, items, nhb, nrep):
 # stepping launch).  Scaled to the batch by the number of replicas.
 NCU_DRAM_BYTES_PER_REPLICA = {"pair_sr": 3.04e6 / 8, "pair_lr": None, "bonded": 1.24e6 / 8, "hbond": 0.479e6 / 8,
                               "shift": 0.04e6 / 8, "integrate": 5.35e6 / 8, "cells": 0.03e6 / 8, "search": None}
+
+
+# Algorithmic FP32 work of the SR pair kernel per list entry evaluated: the distance
+# from the integer differences (3 conversions folded into 3 mul, 2 fma: 8), the LJ or
+# the Coulomb term (about 12: square root, reciprocal powers or the screened form),
+# and the force accumulation (6).
+FLOP_PER_SR_ENTRY = 26
 
 
 # FP32 (FMA) pipe and issue-slot use of each kernel from its committed ncu capture
@@ -530,6 +553,7 @@ def gpu_arm(args):
                     "alg_bytes_per_launch": per_stage[dom]["alg_bytes_per_launch"],
                     "launch_us_in_step": per_stage[dom]["in_step_us"],
                     "fp32_pipe_frac": NCU_FMA_PIPE.get(dom), "issue_active_frac": NCU_ISSUE_ACTIVE.get(dom),
+                    "fp32_pair_sr": fp32_roofline(local, clocks, sr * n_part / groups, in_step.get("pair_sr", 0.0)),
                     "mean_neighbours": {"sr": sr, "lr": lr}, "stages": per_stage, "in_step_source": in_step_src,
                     "step": {"alg_bytes": sum(alg.values()),
                              "achieved_gbs": sum(alg.values()) / (ms_per_step * 1e-3) / 1e9,
