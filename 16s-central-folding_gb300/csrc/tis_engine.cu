@@ -538,14 +538,18 @@ static int grp_create(const tis_system *const *systems, int n_replicas, const ti
         const tis::Array *btx0 = need(s, "bt_x0", base + r, TIS_F64, nbt);
         if (!bta || !btb || !btc || !btk0 || !btx0) return bail(TIS_ERR_ARG);
         hr.bt0 = (int)bt_idx.size();
-        for (int64_t t = 0; t < nbt; ++t) {
-            const int kd = btk->as<int32_t>()[t];
-            const int a = bta->as<int32_t>()[t], b = btb->as<int32_t>()[t], c = btc->as<int32_t>()[t];
-            if (a < 0 || a >= nrna || b < 0 || b >= nrna || (kd == 1 && (c < 0 || c >= nrna)))
-                return bail(fail(TIS_ERR_ARG, "replica %d: bonded term %lld has a bad index", base + r, (long long)t));
-            bt_idx.push_back(make_int4(p0 + a, p0 + b, kd == 1 ? p0 + c : p0 + b, kd));
-            bt_par.push_back(make_double2(btk0->as<double>()[t], btx0->as<double>()[t]));
-        }
+        // the bonds first, then the angles (each in polymer_constraints order), so that
+        // the threads of a warp run the same term; the force sums do not depend on it
+        for (int pass = 0; pass < 2; ++pass)
+            for (int64_t t = 0; t < nbt; ++t) {
+                const int kd = btk->as<int32_t>()[t];
+                if ((kd == 1) != (pass == 1)) continue;
+                const int a = bta->as<int32_t>()[t], b = btb->as<int32_t>()[t], c = btc->as<int32_t>()[t];
+                if (a < 0 || a >= nrna || b < 0 || b >= nrna || (kd == 1 && (c < 0 || c >= nrna)))
+                    return bail(fail(TIS_ERR_ARG, "replica %d: bonded term %lld has a bad index", base + r, (long long)t));
+                bt_idx.push_back(make_int4(p0 + a, p0 + b, kd == 1 ? p0 + c : p0 + b, kd));
+                bt_par.push_back(make_double2(btk0->as<double>()[t], btx0->as<double>()[t]));
+            }
         hr.bt1 = (int)bt_idx.size();
         // bonded partners whose LJ the reference adds in the SR loop and subtracts in
         // polymer_constraints (E:948, E:1132): one entry per subtraction
